@@ -1,0 +1,380 @@
+// capi.cu — the extern "C" boundary of the GB300 EVoC library.
+//
+// Each entry point validates its arguments on the host, runs the device work
+// on the context's stream, reads the device status word (kernels never trap;
+// they set bits that become error codes here) and returns a status code.
+// C++ exceptions never cross the boundary.
+#include "evoc_internal.h"
+
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+
+namespace {
+
+thread_local std::string g_thread_error = "";
+
+void set_err(evoc_ctx* ctx, const std::string& m) {
+  if (ctx)
+    ctx->last_error = m;
+  else
+    g_thread_error = m;
+}
+
+__global__ void k_validate_indices(const uint32_t* __restrict__ idx,
+                                   int64_t nnz, int64_t n,
+                                   int32_t* __restrict__ status) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < nnz && (int64_t)idx[q] >= n) atomicOr(status, (int32_t)evoc::ST_BAD_INDEX);
+}
+
+void use_device(evoc_ctx* ctx) { EVOC_CUDA(cudaSetDevice(ctx->device)); }
+
+}  // namespace
+
+#define EVOC_API_BEGIN try {
+#define EVOC_API_END(ctx)                                        \
+  }                                                              \
+  catch (const evoc::Error& e) {                                 \
+    set_err(ctx, e.what());                                      \
+    return e.code;                                               \
+  }                                                              \
+  catch (const std::bad_alloc&) {                                \
+    set_err(ctx, "host allocation failed");                      \
+    return EVOC_ERR_OUT_OF_MEMORY;                               \
+  }                                                              \
+  catch (const std::exception& e) {                              \
+    set_err(ctx, e.what());                                      \
+    return EVOC_ERR_INTERNAL;                                    \
+  }                                                              \
+  return EVOC_OK;
+
+extern "C" {
+
+int evoc_abi_version(void) { return EVOC_ABI_VERSION; }
+
+void evoc_embed_params_default(evoc_embed_params_t* p) {
+  if (!p) return;
+  p->n_epochs = 50;
+  p->noise_level = 0.5f;
+  p->negative_sample_rate = 1.0f;
+  p->initial_alpha = 0.1f;
+  p->beta1 = 0.5f;
+  p->beta2 = 0.9f;
+  p->eps = 1e-7f;
+}
+
+int evoc_ctx_create(int device, evoc_ctx_t** out) {
+  evoc_ctx* ctx = nullptr;
+  EVOC_API_BEGIN
+  if (!out) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  int count = 0;
+  cudaError_t e = cudaGetDeviceCount(&count);
+  if (e != cudaSuccess || count == 0) {
+    (void)cudaGetLastError();
+    throw evoc::Error(EVOC_ERR_NO_DEVICE, "no CUDA device available");
+  }
+  if (device < 0 || device >= count)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "device index out of range");
+  cudaDeviceProp prop;
+  EVOC_CUDA(cudaGetDeviceProperties(&prop, device));
+  if (!(prop.major == 10 && prop.minor == 3))
+    throw evoc::Error(EVOC_ERR_NO_DEVICE,
+                      std::string("this library is built for sm_103a; device is ") +
+                          prop.name + " (sm_" + std::to_string(prop.major) +
+                          std::to_string(prop.minor) + ")");
+  std::unique_ptr<evoc_ctx> c(new evoc_ctx());
+  c->device = device;
+  c->num_sms = prop.multiProcessorCount;
+  EVOC_CUDA(cudaSetDevice(device));
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;  // keep freed blocks for reuse in this process
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  (void)cudaGetLastError();
+  EVOC_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  c->status.alloc(1, c->stream);
+  EVOC_CUDA(cudaMemsetAsync(c->status.get(), 0, sizeof(int32_t), c->stream));
+  EVOC_CUDA(cudaStreamSynchronize(c->stream));
+  *out = c.release();
+  EVOC_API_END(ctx)
+}
+
+void evoc_ctx_destroy(evoc_ctx_t* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = ctx->stream;
+  ctx->status.release();
+  if (s) {
+    cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+  }
+  delete ctx;
+}
+
+const char* evoc_last_error(const evoc_ctx_t* ctx) {
+  return ctx ? ctx->last_error.c_str() : g_thread_error.c_str();
+}
+
+int evoc_smooth_knn_dist(evoc_ctx_t* ctx, const float* dists,
+                         const int32_t* row_len, int64_t n, int32_t k,
+                         uint64_t k_target, float local_connectivity,
+                         int32_t n_iter, float* sigmas, float* rhos) {
+  EVOC_API_BEGIN
+  if (!ctx) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "ctx is NULL");
+  if (n < 0 || k < 0 || n_iter < 0)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "negative size");
+  if (n == 0) return EVOC_OK;
+  if (!dists || !sigmas || !rhos || k == 0)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL array or k == 0");
+  if (local_connectivity > 0.0f && !std::isfinite(local_connectivity))
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "local_connectivity is not finite");
+  if (row_len)
+    for (int64_t i = 0; i < n; ++i)
+      if (row_len[i] < 0 || row_len[i] > k)
+        throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "row_len outside [0, k]");
+  use_device(ctx);
+  cudaStream_t s = ctx->stream;
+  evoc::DevBuf<float> d(n * (int64_t)k, s), sg(n, s), rh(n, s);
+  evoc::DevBuf<int32_t> rl;
+  EVOC_CUDA(cudaMemcpyAsync(d.get(), dists, d.bytes(), cudaMemcpyHostToDevice, s));
+  if (row_len) {
+    rl.alloc(n, s);
+    EVOC_CUDA(cudaMemcpyAsync(rl.get(), row_len, rl.bytes(), cudaMemcpyHostToDevice, s));
+  }
+  evoc::smooth_knn_device(ctx, d.get(), rl.get(), n, k, k_target,
+                          local_connectivity, n_iter, sg.get(), rh.get(),
+                          nullptr, nullptr);
+  EVOC_CUDA(cudaMemcpyAsync(sigmas, sg.get(), sg.bytes(), cudaMemcpyDeviceToHost, s));
+  EVOC_CUDA(cudaMemcpyAsync(rhos, rh.get(), rh.bytes(), cudaMemcpyDeviceToHost, s));
+  evoc::check_status(ctx, "smooth_knn_dist");
+  EVOC_API_END(ctx)
+}
+
+int evoc_fuzzy_set_device(evoc_ctx_t* ctx, const uint32_t* d_knn_idx,
+                          const float* d_knn_dist, int64_t n, int32_t k,
+                          float effective_n_neighbours, int symmetrise,
+                          float* d_sigmas, float* d_rhos,
+                          evoc_graph_t** out_graph) {
+  EVOC_API_BEGIN
+  if (!ctx || !out_graph)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "ctx or out_graph is NULL");
+  *out_graph = nullptr;
+  if (n > 0 && (!d_knn_idx || !d_knn_dist))
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL kNN array");
+  use_device(ctx);
+  std::unique_ptr<evoc_graph> g(new evoc_graph());
+  evoc::fuzzy_set_device(ctx, d_knn_idx, d_knn_dist, n, k,
+                         effective_n_neighbours, symmetrise != 0, d_sigmas,
+                         d_rhos, g.get());
+  evoc::check_status(ctx, "fuzzy set");
+  *out_graph = g.release();
+  EVOC_API_END(ctx)
+}
+
+int evoc_fuzzy_set(evoc_ctx_t* ctx, const uint32_t* knn_idx,
+                   const float* knn_dist, int64_t n, int32_t k,
+                   float effective_n_neighbours, int symmetrise,
+                   evoc_graph_t** out_graph) {
+  EVOC_API_BEGIN
+  if (!ctx || !out_graph)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "ctx or out_graph is NULL");
+  *out_graph = nullptr;
+  if (n <= 0)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT,
+                      "empty kNN graph (build_fuzzy_simplicial_set reads row 0)");
+  if (k <= 0) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "k must be positive");
+  if (!knn_idx || !knn_dist)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL kNN array");
+  use_device(ctx);
+  cudaStream_t s = ctx->stream;
+  evoc::DevBuf<uint32_t> di(n * (int64_t)k, s);
+  evoc::DevBuf<float> dd(n * (int64_t)k, s);
+  EVOC_CUDA(cudaMemcpyAsync(di.get(), knn_idx, di.bytes(), cudaMemcpyHostToDevice, s));
+  EVOC_CUDA(cudaMemcpyAsync(dd.get(), knn_dist, dd.bytes(), cudaMemcpyHostToDevice, s));
+  std::unique_ptr<evoc_graph> g(new evoc_graph());
+  evoc::fuzzy_set_device(ctx, di.get(), dd.get(), n, k, effective_n_neighbours,
+                         symmetrise != 0, nullptr, nullptr, g.get());
+  evoc::check_status(ctx, "fuzzy set");
+  *out_graph = g.release();
+  EVOC_API_END(ctx)
+}
+
+int evoc_graph_from_csr(evoc_ctx_t* ctx, const int64_t* indptr,
+                        const uint32_t* indices, const float* weights,
+                        int64_t n, evoc_graph_t** out_graph) {
+  EVOC_API_BEGIN
+  if (!ctx || !out_graph || (n > 0 && !indptr) || n < 0)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "bad argument");
+  *out_graph = nullptr;
+  if (n >= (int64_t)0xFFFFFFFFu)
+    throw evoc::Error(EVOC_ERR_UNSUPPORTED, "n must be < 2^32-1");
+  int64_t nnz = 0;
+  if (n > 0) {
+    if (indptr[0] != 0)
+      throw evoc::Error(EVOC_ERR_INVALID_INPUT, "indptr[0] must be 0");
+    for (int64_t i = 0; i < n; ++i)
+      if (indptr[i + 1] < indptr[i])
+        throw evoc::Error(EVOC_ERR_INVALID_INPUT, "indptr must be non-decreasing");
+    nnz = indptr[n];
+    if (nnz > 0 && (!indices || !weights))
+      throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL indices or weights");
+  }
+  use_device(ctx);
+  cudaStream_t s = ctx->stream;
+  std::unique_ptr<evoc_graph> g(new evoc_graph());
+  g->ctx = ctx;
+  g->n = n;
+  g->nnz = nnz;
+  g->canonical = false;
+  g->indptr.alloc(n + 1, s);
+  g->indices.alloc(nnz, s);
+  g->weights.alloc(nnz, s);
+  if (n > 0)
+    EVOC_CUDA(cudaMemcpyAsync(g->indptr.get(), indptr, (n + 1) * sizeof(int64_t),
+                              cudaMemcpyHostToDevice, s));
+  else
+    EVOC_CUDA(cudaMemsetAsync(g->indptr.get(), 0, sizeof(int64_t), s));
+  if (nnz > 0) {
+    EVOC_CUDA(cudaMemcpyAsync(g->indices.get(), indices, nnz * sizeof(uint32_t),
+                              cudaMemcpyHostToDevice, s));
+    EVOC_CUDA(cudaMemcpyAsync(g->weights.get(), weights, nnz * sizeof(float),
+                              cudaMemcpyHostToDevice, s));
+    k_validate_indices<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(
+        g->indices.get(), nnz, n, ctx->status.get());
+    EVOC_CHECK_LAUNCH();
+  }
+  evoc::check_status(ctx, "graph upload");
+  *out_graph = g.release();
+  EVOC_API_END(ctx)
+}
+
+int evoc_graph_info(const evoc_graph_t* g, int64_t* n, int64_t* nnz) {
+  if (!g) return EVOC_ERR_INVALID_ARGUMENT;
+  if (n) *n = g->n;
+  if (nnz) *nnz = g->nnz;
+  return EVOC_OK;
+}
+
+int evoc_graph_export(const evoc_graph_t* g, int64_t* indptr,
+                      uint32_t* indices, float* weights) {
+  evoc_ctx* ctx = g ? g->ctx : nullptr;
+  EVOC_API_BEGIN
+  if (!g || !indptr || (g->nnz > 0 && (!indices || !weights)))
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL argument");
+  use_device(ctx);
+  cudaStream_t s = ctx->stream;
+  EVOC_CUDA(cudaMemcpyAsync(indptr, g->indptr.get(), (g->n + 1) * sizeof(int64_t),
+                            cudaMemcpyDeviceToHost, s));
+  if (g->nnz > 0) {
+    EVOC_CUDA(cudaMemcpyAsync(indices, g->indices.get(), g->nnz * sizeof(uint32_t),
+                              cudaMemcpyDeviceToHost, s));
+    EVOC_CUDA(cudaMemcpyAsync(weights, g->weights.get(), g->nnz * sizeof(float),
+                              cudaMemcpyDeviceToHost, s));
+  }
+  EVOC_CUDA(cudaStreamSynchronize(s));
+  EVOC_API_END(ctx)
+}
+
+void evoc_graph_free(evoc_graph_t* g) {
+  if (!g) return;
+  if (g->ctx) cudaSetDevice(g->ctx->device);
+  delete g;
+}
+
+int evoc_plan_create(evoc_ctx_t* ctx, const evoc_graph_t* g, int32_t dim,
+                     const evoc_embed_params_t* params, uint64_t seed,
+                     evoc_plan_t** out_plan) {
+  EVOC_API_BEGIN
+  if (!ctx || !g || !params || !out_plan)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL argument");
+  *out_plan = nullptr;
+  use_device(ctx);
+  std::vector<evoc::ProblemDesc> probs{{g, seed}};
+  *out_plan = evoc::plan_create(ctx, probs, dim, *params);
+  EVOC_API_END(ctx)
+}
+
+int evoc_plan_run_device(evoc_plan_t* plan, const float* d_init, float* d_out) {
+  evoc_ctx* ctx = plan ? evoc::plan_ctx(plan) : nullptr;
+  EVOC_API_BEGIN
+  if (!plan || !d_out) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL argument");
+  use_device(ctx);
+  evoc::plan_run_device(plan, d_init, d_out);
+  EVOC_CUDA(cudaStreamSynchronize(ctx->stream));
+  EVOC_API_END(ctx)
+}
+
+int evoc_plan_stats(const evoc_plan_t* plan, evoc_epoch_stats_t* stats) {
+  evoc_ctx* ctx = plan ? evoc::plan_ctx(plan) : nullptr;
+  EVOC_API_BEGIN
+  if (!plan || !stats) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL argument");
+  use_device(ctx);
+  evoc::plan_stats(plan, stats);
+  EVOC_API_END(ctx)
+}
+
+int evoc_plan_debug_run(evoc_plan_t* plan, const float* init,
+                        int32_t start_epoch, int32_t end_epoch, float* out,
+                        float* grad_out) {
+  evoc_ctx* ctx = plan ? evoc::plan_ctx(plan) : nullptr;
+  EVOC_API_BEGIN
+  if (!plan || !out) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL argument");
+  use_device(ctx);
+  evoc::plan_debug_run(plan, init, start_epoch, end_epoch, out, grad_out);
+  EVOC_API_END(ctx)
+}
+
+void evoc_plan_free(evoc_plan_t* plan) {
+  if (!plan) return;
+  evoc_ctx* ctx = evoc::plan_ctx(plan);
+  if (ctx) cudaSetDevice(ctx->device);
+  evoc::plan_free(plan);
+}
+
+int evoc_embed(evoc_ctx_t* ctx, const evoc_graph_t* g, int32_t dim,
+               const evoc_embed_params_t* params, const float* init,
+               uint64_t seed, int32_t verbose, float* out) {
+  EVOC_API_BEGIN
+  if (!ctx || !g || !params)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (g->n > 0 && !out) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "out is NULL");
+  if (g->n == 0) return EVOC_OK;  // embedding.rs:61-64
+  use_device(ctx);
+  std::vector<evoc::ProblemDesc> probs{{g, seed}};
+  std::unique_ptr<evoc_plan, void (*)(evoc_plan*)> pl(
+      evoc::plan_create(ctx, probs, dim, *params), evoc::plan_free);
+  const float* inits[1] = {init};
+  float* outs[1] = {out};
+  evoc::plan_upload_init_and_run(pl.get(), inits, outs, verbose);
+  EVOC_API_END(ctx)
+}
+
+int evoc_embed_batched(evoc_ctx_t* ctx, int32_t n_problems,
+                       const evoc_graph_t* const* graphs, int32_t dim,
+                       const evoc_embed_params_t* params,
+                       const float* const* inits, const uint64_t* seeds,
+                       float* const* outs) {
+  EVOC_API_BEGIN
+  if (!ctx || n_problems < 0 || (n_problems > 0 && (!graphs || !seeds || !outs)) ||
+      !params)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "bad argument");
+  if (n_problems == 0) return EVOC_OK;
+  use_device(ctx);
+  std::vector<evoc::ProblemDesc> probs;
+  for (int32_t q = 0; q < n_problems; ++q) {
+    if (!graphs[q]) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL graph");
+    if (graphs[q]->n > 0 && !outs[q])
+      throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL output");
+    probs.push_back({graphs[q], seeds[q]});
+  }
+  std::unique_ptr<evoc_plan, void (*)(evoc_plan*)> pl(
+      evoc::plan_create(ctx, probs, dim, *params), evoc::plan_free);
+  evoc::plan_upload_init_and_run(pl.get(), inits, outs, 0);
+  EVOC_API_END(ctx)
+}
+
+}  // extern "C"

@@ -1,0 +1,1113 @@
+// embed.cu — the EVoC node-embedding optimiser on the GPU.
+//
+// Replaces evoc_embedding, src/graph/embedding.rs:48-298 (evoc-rs 0.2.7).
+//
+// Set-up (once per plan, embedding.rs:78-175):
+//   k_row_counts   warp per row: upper (i < j) and lower entries per row.
+//   k_edge_fill    warp per row: undirected edge list in adjacency order
+//                  (eidx = rank among upper entries, embedding.rs:79-90) and
+//                  the per-problem maximum weight (embedding.rs:99).
+//   k_edge_ps      thread per edge: epochs_per_sample (embedding.rs:101-111).
+//   radix sort     (general graphs only) edges by larger endpoint, stable, to
+//                  list each node's "is_smaller = false" incidences in edge
+//                  order (embedding.rs:130-135).
+//   k_inc_fill     warp per node: the per-node incidence list of
+//                  embedding.rs:121-135 (lower part in edge order, then the
+//                  node's own upper entries).
+//   k_schedule     thread per incidence entry: runs the epochs-per-sample
+//                  recurrence of embedding.rs:274-286 for every epoch and
+//                  stores, per epoch, one bit "fires" and P bits "negative
+//                  count" (embedding.rs:225-228) for each entry. Both copies of
+//                  an edge evaluate the same f32 recurrence, so they agree.
+// Epoch loop (embedding.rs:178-292), one launch per epoch, captured in a CUDA
+// graph:
+//   k_epoch        G lanes per node (pull-based): each lane takes incidence
+//                  entries q = lane, lane + G, ... of its node, reads the fire
+//                  bit, gathers partner rows (float4) and Philox negatives,
+//                  accumulates into the partial sum of virtual lane q mod 32;
+//                  partials are combined with strides 16..1 (in registers for
+//                  strides >= G, by reduce-scatter shuffles below G); the lane
+//                  that owns a dimension applies Adam (embedding.rs:256-272)
+//                  and writes the next embedding buffer (ping-pong). No float
+//                  atomics; results do not depend on G.
+#include "evoc_device.cuh"
+#include "evoc_internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+
+namespace evoc {
+
+struct ProbInfo {
+  uint32_t node_base;
+  uint32_t n;
+  uint64_t seed;
+};
+
+}  // namespace evoc
+
+struct evoc_plan {
+  evoc_ctx* ctx = nullptr;
+  int64_t n = 0;          // nodes over all problems
+  int32_t dim = 0;        // n_components
+  int32_t dimp = 0;       // padded row width (4, 8 or 16)
+  int32_t lanes = 0;      // lanes per node in k_epoch
+  evoc_embed_params_t params{};
+  int32_t n_problems = 0;
+  std::vector<int64_t> node_base;  // per problem, host
+  std::vector<uint64_t> seeds;     // per problem, host
+  bool has_edges = false;
+  int64_t n_edges = 0;
+  int64_t n_inc = 0;      // incidence entries (2 per edge)
+  int32_t P = 0;          // negative-count bit planes
+  int64_t W = 0;          // 32-bit words per plane
+  uint64_t max_neg = 0;
+  evoc::DevBuf<int64_t> inc_ptr;
+  evoc::DevBuf<uint32_t> inc_other;
+  evoc::DevBuf<int64_t> eidx_base;
+  evoc::DevBuf<uint32_t> planes;
+  evoc::DevBuf<uint32_t> prob_of_node;  // batched only
+  evoc::DevBuf<evoc::ProbInfo> prob;    // batched only
+  evoc::DevBuf<float> e0, e1, m, v, grad;
+  std::vector<float> lr_ad, epsc, gamma;
+  float one_m_b1 = 0, one_m_b2 = 0;
+  std::vector<evoc_epoch_stats_t> stats;
+  bool active_counted = false;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+};
+
+namespace evoc {
+namespace {
+
+constexpr int64_t NEG_LIMIT = 1 << 20;
+
+__device__ __forceinline__ float ps_from_w(float w, float max_w) {
+  const float norm = fdiv(w, max_w);
+  return (norm > 0.0f) ? fdiv(1.0f, norm) : 1e8f;
+}
+
+__device__ __forceinline__ uint32_t prob_of(const uint32_t* pon, uint32_t v) {
+  return pon ? pon[v] : 0u;
+}
+
+// ---------------------------------------------------------------------------
+// Set-up kernels
+// ---------------------------------------------------------------------------
+__global__ void k_row_counts(const int64_t* __restrict__ indptr,
+                             const uint32_t* __restrict__ indices, int64_t n,
+                             int32_t* __restrict__ ucnt,
+                             int32_t* __restrict__ lcnt_own) {
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (r >= n) return;
+  const int64_t a = indptr[r], b = indptr[r + 1];
+  int32_t u = 0, l = 0;
+  for (int64_t p = a + lane; p < b; p += 32) {
+    const uint32_t c = indices[p];
+    u += (int64_t)c > r;
+    l += (int64_t)c < r;
+  }
+  u = __reduce_add_sync(0xffffffffu, (unsigned)u);
+  l = __reduce_add_sync(0xffffffffu, (unsigned)l);
+  if (lane == 0) {
+    ucnt[r] = u;
+    lcnt_own[r] = l;
+  }
+}
+
+__global__ void k_edge_fill(const int64_t* __restrict__ indptr,
+                            const uint32_t* __restrict__ indices,
+                            const float* __restrict__ weights, int64_t n,
+                            const int64_t* __restrict__ uptr,
+                            const uint32_t* __restrict__ prob_of_node,
+                            float* __restrict__ e_w, uint32_t* __restrict__ e_dst,
+                            uint32_t* __restrict__ e_src,
+                            int32_t* __restrict__ max_w_bits,
+                            int32_t* __restrict__ lcnt /* general only */) {
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (r >= n) return;
+  const int64_t a = indptr[r], b = indptr[r + 1];
+  int64_t e = uptr[r];
+  int32_t mx = 0;
+  const uint32_t lt = (1u << lane) - 1u;
+  for (int64_t base = a; base < b; base += 32) {
+    const int64_t p = base + lane;
+    uint32_t c = 0;
+    float w = 0.0f;
+    bool up = false;
+    if (p < b) {
+      c = indices[p];
+      w = weights[p];
+      up = (int64_t)c > r;
+    }
+    const uint32_t bal = __ballot_sync(0xffffffffu, up);
+    if (up) {
+      const int64_t q = e + __popc(bal & lt);
+      e_w[q] = w;
+      e_dst[q] = c;
+      e_src[q] = (uint32_t)r;
+      if (w == w) mx = max(mx, __float_as_int(w));  // f32::max ignores NaN
+      if (lcnt) atomicAdd(&lcnt[c], 1);
+    }
+    e += __popc(bal);
+  }
+  mx = __reduce_max_sync(0xffffffffu, mx);
+  if (lane == 0 && mx > 0) atomicMax(&max_w_bits[prob_of(prob_of_node, (uint32_t)r)], mx);
+}
+
+__global__ void k_edge_ps(const float* __restrict__ e_w,
+                          const uint32_t* __restrict__ e_src, int64_t U,
+                          const uint32_t* __restrict__ prob_of_node,
+                          const int32_t* __restrict__ max_w_bits,
+                          float* __restrict__ e_ps) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= U) return;
+  const float mw = __int_as_float(max_w_bits[prob_of(prob_of_node, e_src[e])]);
+  e_ps[e] = ps_from_w(e_w[e], mw);
+}
+
+// Problem edge base: uptr at each problem's first node.
+__global__ void k_prob_ebase(const int64_t* __restrict__ uptr,
+                             const ProbInfo* __restrict__ prob, int32_t np,
+                             int64_t* __restrict__ ebase) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < np) ebase[q] = prob ? uptr[prob[q].node_base] : 0;
+}
+
+__global__ void k_inc_fill(const int64_t* __restrict__ indptr,
+                           const uint32_t* __restrict__ indices,
+                           const float* __restrict__ weights, int64_t n,
+                           const int64_t* __restrict__ uptr,
+                           const int32_t* __restrict__ lcnt,
+                           const int64_t* __restrict__ lptr,   // general
+                           const uint2* __restrict__ lower,    // general
+                           const float* __restrict__ e_ps,
+                           const int64_t* __restrict__ inc_ptr,
+                           const uint32_t* __restrict__ prob_of_node,
+                           const int32_t* __restrict__ max_w_bits,
+                           const int64_t* __restrict__ ebase,
+                           uint32_t* __restrict__ inc_other,
+                           float* __restrict__ inc_ps,
+                           uint8_t* __restrict__ inc_up,
+                           int64_t* __restrict__ eidx_base) {
+  const int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (v >= n) return;
+  const uint32_t pr = prob_of(prob_of_node, (uint32_t)v);
+  const float mw = __int_as_float(max_w_bits[pr]);
+  const int64_t p0 = inc_ptr[v];
+  const int64_t nl = lcnt[v];
+  const int64_t a = indptr[v], b = indptr[v + 1];
+  const uint32_t lt = (1u << lane) - 1u;
+  if (lower == nullptr) {
+    // canonical symmetric graph: lower part = own entries with column < v
+    int64_t o = p0;
+    for (int64_t base = a; base < b; base += 32) {
+      const int64_t p = base + lane;
+      const bool lo = p < b && (int64_t)indices[p] < v;
+      const uint32_t bal = __ballot_sync(0xffffffffu, lo);
+      if (lo) {
+        const int64_t q = o + __popc(bal & lt);
+        inc_other[q] = indices[p];
+        inc_ps[q] = ps_from_w(weights[p], mw);
+        inc_up[q] = 0;
+      }
+      o += __popc(bal);
+    }
+  } else {
+    const int64_t l0 = lptr[v];
+    for (int64_t j = lane; j < nl; j += 32) {
+      const uint2 pe = lower[l0 + j];  // (eidx, smaller endpoint)
+      inc_other[p0 + j] = pe.y;
+      inc_ps[p0 + j] = e_ps[pe.x];
+      inc_up[p0 + j] = 0;
+    }
+  }
+  int64_t o = p0 + nl;
+  for (int64_t base = a; base < b; base += 32) {
+    const int64_t p = base + lane;
+    const bool up = p < b && (int64_t)indices[p] > v;
+    const uint32_t bal = __ballot_sync(0xffffffffu, up);
+    if (up) {
+      const int64_t q = o + __popc(bal & lt);
+      inc_other[q] = indices[p];
+      inc_ps[q] = ps_from_w(weights[p], mw);
+      inc_up[q] = 1;
+    }
+    o += __popc(bal);
+  }
+  if (lane == 0) eidx_base[v] = (uptr[v] - ebase[pr]) - (p0 + nl);
+}
+
+// Epochs-per-sample recurrence of one incidence entry (embedding.rs:274-286)
+// and the negative count of embedding.rs:225-228.
+struct Sched {
+  float ps, pn, ns, nn;
+  bool up;
+  __device__ __forceinline__ void init(float ps_, float neg_factor, bool up_) {
+    ps = ps_;
+    pn = fmul(ps_, neg_factor);
+    ns = ps;
+    nn = pn;
+    up = up_;
+  }
+  // Returns fired; *nneg gets the negative count (upper entries only).
+  __device__ __forceinline__ bool step(float tf, uint64_t* nneg) {
+    const bool fire = !(ns > tf);
+    uint64_t cnt = 0;
+    if (ns <= tf) {
+      ns = fadd(ns, ps);
+      if (up) {
+        cnt = to_usize_or0(floorf(fdiv(fsub(tf, nn), pn)));
+        nn = fadd(nn, fmul((float)cnt, pn));
+      }
+    }
+    *nneg = (fire && up) ? cnt : 0;
+    return fire;
+  }
+};
+
+__global__ void k_schedule_scan(const float* __restrict__ inc_ps,
+                                const uint8_t* __restrict__ inc_up,
+                                int64_t n_inc, int32_t n_epochs,
+                                float neg_factor,
+                                unsigned long long* __restrict__ max_neg,
+                                unsigned long long* __restrict__ st_fired,
+                                unsigned long long* __restrict__ st_neg) {
+  extern __shared__ unsigned long long sst[];  // [2 * n_epochs] or empty
+  const bool stats = st_fired != nullptr;
+  if (stats) {
+    for (int t = threadIdx.x; t < 2 * n_epochs; t += blockDim.x) sst[t] = 0;
+    __syncthreads();
+  }
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = p < n_inc;
+  Sched s;
+  s.init(valid ? inc_ps[p] : 3.0e38f, neg_factor, valid && inc_up[p]);
+  unsigned long long mx = 0;
+  for (int32_t t = 0; t < n_epochs; ++t) {
+    uint64_t nn;
+    const bool f = valid && s.step((float)t, &nn);
+    if (nn > mx) mx = nn;
+    if (stats) {
+      const unsigned fu = __reduce_add_sync(0xffffffffu, (f && s.up) ? 1u : 0u);
+      const unsigned long long ng = (unsigned long long)nn;
+      unsigned long long ngs = ng;
+      for (int o = 16; o > 0; o >>= 1) ngs += __shfl_xor_sync(0xffffffffu, ngs, o);
+      if ((threadIdx.x & 31) == 0) {
+        if (fu) atomicAdd(&sst[t], (unsigned long long)fu);
+        if (ngs) atomicAdd(&sst[n_epochs + t], ngs);
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long y = __shfl_xor_sync(0xffffffffu, mx, o);
+    mx = y > mx ? y : mx;
+  }
+  if ((threadIdx.x & 31) == 0 && mx) atomicMax(max_neg, mx);
+  if (stats) {
+    __syncthreads();
+    for (int t = threadIdx.x; t < n_epochs; t += blockDim.x) {
+      if (sst[t]) atomicAdd(&st_fired[t], sst[t]);
+      if (sst[n_epochs + t]) atomicAdd(&st_neg[t], sst[n_epochs + t]);
+    }
+  }
+}
+
+// Writes, per epoch t, the fire plane and P negative-count planes:
+// planes[(t * (1 + P) + b) * W + word].
+__global__ void k_schedule_write(const float* __restrict__ inc_ps,
+                                 const uint8_t* __restrict__ inc_up,
+                                 int64_t n_inc, int32_t n_epochs,
+                                 float neg_factor, int32_t P, int64_t W,
+                                 uint32_t* __restrict__ planes) {
+  const int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t word = p >> 5;
+  if (word >= W) return;  // whole warps only
+  const bool valid = p < n_inc;
+  Sched s;
+  s.init(valid ? inc_ps[p] : 3.0e38f, neg_factor, valid && inc_up[p]);
+  const bool lane0 = (threadIdx.x & 31) == 0;
+  for (int32_t t = 0; t < n_epochs; ++t) {
+    uint64_t nn;
+    const bool f = valid && s.step((float)t, &nn);
+    const uint32_t fw = __ballot_sync(0xffffffffu, f);
+    uint32_t* base = planes + (size_t)t * (1 + P) * W + word;
+    if (lane0) base[0] = fw;
+    for (int32_t b = 0; b < P; ++b) {
+      const uint32_t bw = __ballot_sync(0xffffffffu, (nn >> b) & 1ull);
+      if (lane0) base[(size_t)(1 + b) * W] = bw;
+    }
+  }
+}
+
+// Active nodes per epoch: nodes with at least one fired incidence entry.
+__global__ void k_active_count(const int64_t* __restrict__ inc_ptr, int64_t n,
+                               const uint32_t* __restrict__ planes,
+                               int32_t n_epochs, int32_t P, int64_t W,
+                               unsigned long long* __restrict__ st_active) {
+  const int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const bool valid = v < n;
+  const int64_t p0 = valid ? inc_ptr[v] : 0, p1 = valid ? inc_ptr[v + 1] : 0;
+  for (int32_t t = 0; t < n_epochs; ++t) {
+    const uint32_t* fire = planes + (size_t)t * (1 + P) * W;
+    bool any = false;
+    for (int64_t p = p0 + lane; p < p1; p += 32) any |= (fire[p >> 5] >> (p & 31)) & 1u;
+    any = __any_sync(0xffffffffu, any);
+    if (lane == 0 && any) atomicAdd(&st_active[t], 1ull);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Random initialisation, padding and unpadding.
+// ---------------------------------------------------------------------------
+__global__ void k_init_random(float* __restrict__ e, int64_t n, int32_t dim,
+                              int32_t dimp,
+                              const uint32_t* __restrict__ prob_of_node,
+                              const ProbInfo* __restrict__ prob, uint64_t seed) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n * dimp) return;
+  const int64_t v = q / dimp;
+  const int32_t d = (int32_t)(q - v * dimp);
+  float val = 0.0f;
+  if (d < dim) {
+    uint64_t sd = seed;
+    int64_t local = v;
+    if (prob_of_node) {
+      const ProbInfo pi = prob[prob_of_node[v]];
+      sd = pi.seed;
+      local = v - pi.node_base;
+    }
+    val = init_value(sd, (uint64_t)(local * dim + d));
+  }
+  e[q] = val;
+}
+
+__global__ void k_pad(const float* __restrict__ src, float* __restrict__ dst,
+                      int64_t n, int32_t dim, int32_t dimp) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n * dimp) return;
+  const int64_t v = q / dimp;
+  const int32_t d = (int32_t)(q - v * dimp);
+  dst[q] = (d < dim) ? src[v * dim + d] : 0.0f;
+}
+
+__global__ void k_unpad(const float* __restrict__ src, float* __restrict__ dst,
+                        int64_t n, int32_t dim, int32_t dimp) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n * dim) return;
+  const int64_t v = q / dim;
+  const int32_t d = (int32_t)(q - v * dim);
+  dst[q] = src[v * dimp + d];
+}
+
+// ---------------------------------------------------------------------------
+// The fused epoch kernel.
+// ---------------------------------------------------------------------------
+struct EpochArgs {
+  const int64_t* inc_ptr;
+  const uint32_t* inc_other;
+  const int64_t* eidx_base;
+  const uint32_t* fire;  // fire plane of this epoch; neg planes follow
+  int64_t W;
+  int32_t P;
+  const float* e_cur;
+  float* e_next;
+  float* m;
+  float* v;
+  float* grad_out;
+  const uint32_t* prob_of_node;
+  const ProbInfo* prob;
+  uint32_t n_total;
+  uint32_t epoch;
+  uint64_t seed;
+  float noise, gamma, lr_ad, epsc, one_m_b1, one_m_b2;
+};
+
+template <int DIMP>
+__device__ __forceinline__ void load_row(const float* __restrict__ p, float (&r)[DIMP]) {
+  const float4* p4 = reinterpret_cast<const float4*>(p);
+#pragma unroll
+  for (int i = 0; i < DIMP / 4; ++i) {
+    const float4 x = __ldg(p4 + i);
+    r[4 * i + 0] = x.x;
+    r[4 * i + 1] = x.y;
+    r[4 * i + 2] = x.z;
+    r[4 * i + 3] = x.w;
+  }
+}
+
+template <int DIMP, int G>
+__global__ void __launch_bounds__(256) k_epoch(EpochArgs a) {
+  constexpr int VL = 32 / G;
+  const int lane = threadIdx.x & 31;
+  const int gl = lane & (G - 1);
+  const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
+  if (gid >= a.n_total) return;  // groups exit whole
+  const unsigned gmask =
+      (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
+  const uint32_t v = (uint32_t)gid;
+  uint32_t nb = 0, np = a.n_total;
+  uint64_t seed = a.seed;
+  if (a.prob_of_node) {
+    const ProbInfo pi = a.prob[a.prob_of_node[v]];
+    nb = pi.node_base;
+    np = pi.n;
+    seed = pi.seed;
+  }
+  const int64_t p0 = a.inc_ptr[v], p1 = a.inc_ptr[v + 1];
+  float ev[DIMP];
+  load_row<DIMP>(a.e_cur + (size_t)v * DIMP, ev);
+  float acc[VL][DIMP];
+#pragma unroll
+  for (int s = 0; s < VL; ++s)
+#pragma unroll
+    for (int d = 0; d < DIMP; ++d) acc[s][d] = 0.0f;
+  bool any = false;
+  int64_t eb = 0;
+  bool eb_loaded = false;
+  const float two_noise = fmul(2.0f, a.noise);
+  const float gamma4 = fmul(a.gamma, 4.0f);
+
+  for (int64_t base = p0; base < p1; base += 32) {
+#pragma unroll
+    for (int s = 0; s < VL; ++s) {
+      const int64_t p = base + s * G + gl;
+      if (p >= p1) continue;
+      const uint32_t word = __ldcs(a.fire + (p >> 5));
+      if (!((word >> (p & 31)) & 1u)) continue;
+      any = true;
+      const uint32_t o = __ldcs(a.inc_other + p);
+      float eo[DIMP];
+      load_row<DIMP>(a.e_cur + (size_t)o * DIMP, eo);
+      float diff[DIMP];
+      float dsq = 0.0f;
+#pragma unroll
+      for (int d = 0; d < DIMP; ++d) {
+        diff[d] = fsub(ev[d], eo[d]);
+        dsq = fadd(dsq, fmul(diff[d], diff[d]));
+      }
+      if (dsq >= 1e-8f) {  // embedding.rs:213-221
+        const float dist = fsqrt(dsq);
+        const float coeff = fdiv(fsub(-fmul(two_noise, dist), 2.0f),
+                                 fadd(fsub(fmul(2.0f, dsq), fmul(0.5f, dist)), 1.0f));
+#pragma unroll
+        for (int d = 0; d < DIMP; ++d) acc[s][d] = fadd(acc[s][d], fmul(coeff, diff[d]));
+      }
+      if (o > v) {  // embedding.rs:224-247
+        uint32_t nneg = 0;
+        for (int32_t b = 0; b < a.P; ++b)
+          nneg |= ((__ldcs(a.fire + (size_t)(1 + b) * a.W + (p >> 5)) >> (p & 31)) & 1u) << b;
+        if (nneg) {
+          if (!eb_loaded) {
+            eb = a.eidx_base[v];
+            eb_loaded = true;
+          }
+          const uint64_t eidx = (uint64_t)(p + eb);
+          for (uint32_t j = 0; j < nneg; ++j) {
+            const uint32_t kk = nb + negative_draw(seed, j, a.epoch, eidx, np);
+            if (kk == v) continue;
+            float ek[DIMP];
+            load_row<DIMP>(a.e_cur + (size_t)kk * DIMP, ek);
+            float dk = 0.0f;
+#pragma unroll
+            for (int d = 0; d < DIMP; ++d) {
+              const float df = fsub(ev[d], ek[d]);
+              dk = fadd(dk, fmul(df, df));
+            }
+            if (dk > 0.01f) {
+              const float gc = fdiv(gamma4, fmul(fadd(1.0f, fmul(0.25f, dk)), dk));
+#pragma unroll
+              for (int d = 0; d < DIMP; ++d) {
+                float c = fmul(gc, fsub(ev[d], ek[d]));
+                c = fmaxf(c, -4.0f);
+                c = fminf(c, 4.0f);
+                acc[s][d] = fadd(acc[s][d], c);
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+
+  // strides 16 .. G: partial sums held by the same lane
+#pragma unroll
+  for (int off = 16; off >= G; off >>= 1) {
+    const int half = off / G;
+#pragma unroll
+    for (int s = 0; s < VL; ++s)
+      if (s < half) {
+#pragma unroll
+        for (int d = 0; d < DIMP; ++d) acc[s][d] = fadd(acc[s][d], acc[s + half][d]);
+      }
+  }
+  // strides G/2 .. 1: reduce-scatter across the group's lanes
+  float c[DIMP];
+#pragma unroll
+  for (int d = 0; d < DIMP; ++d) c[d] = acc[0][d];
+  int width = DIMP;  // values held: dims [d0, d0 + width)
+  int d0 = 0;
+#pragma unroll
+  for (int off = G / 2; off >= 1; off >>= 1) {
+    if (width >= 2) {
+      const bool upper = (gl & off) != 0;
+      const int h = width / 2;
+#pragma unroll
+      for (int i = 0; i < DIMP / 2; ++i) {
+        if (i < h) {
+          const float send = upper ? c[i] : c[i + h];
+          const float keep = upper ? c[i + h] : c[i];
+          const float recv = __shfl_xor_sync(gmask, send, off);
+          c[i] = fadd(keep, recv);
+        }
+      }
+      width = h;
+      if (upper) d0 += h;
+    } else {
+      c[0] = fadd(c[0], __shfl_xor_sync(gmask, c[0], off));
+    }
+  }
+  any = __any_sync(gmask, any);
+  // lanes whose low bits (strides after the last halving) are zero write
+  constexpr int REPL = (G > DIMP) ? (G / DIMP) : 1;
+  if ((gl & (REPL - 1)) != 0) return;
+  const size_t nbase = (size_t)v * DIMP;
+#pragma unroll
+  for (int i = 0; i < DIMP; ++i) {
+    if (i >= width) break;
+    const size_t q = nbase + d0 + i;
+    float e = a.e_cur[q];
+    const float g = c[i];
+    if (any) {  // embedding.rs:263-271
+      float mm = __ldcs(a.m + q);
+      float vv = __ldcs(a.v + q);
+      mm = fadd(mm, fmul(a.one_m_b1, fsub(g, mm)));
+      vv = fadd(vv, fmul(a.one_m_b2, fsub(fmul(g, g), vv)));
+      e = fadd(e, fdiv(fmul(a.lr_ad, mm), fadd(fsqrt(vv), a.epsc)));
+      __stcs(a.m + q, mm);
+      __stcs(a.v + q, vv);
+    }
+    a.e_next[q] = e;
+    if (a.grad_out) a.grad_out[q] = any ? g : 0.0f;
+  }
+}
+
+using EpochKernel = void (*)(EpochArgs);
+
+EpochKernel pick_kernel(int dimp, int lanes) {
+#define EVOC_K(D, G) if (dimp == D && lanes == G) return k_epoch<D, G>;
+  EVOC_K(4, 8) EVOC_K(4, 16) EVOC_K(4, 32)
+  EVOC_K(8, 8) EVOC_K(8, 16) EVOC_K(8, 32)
+  EVOC_K(16, 16) EVOC_K(16, 32)
+#undef EVOC_K
+  return nullptr;
+}
+
+int default_lanes(int dimp, double avg_inc) {
+  int g = avg_inc <= 24.0 ? 8 : (avg_inc <= 48.0 ? 16 : 32);
+  if (dimp == 16 && g < 16) g = 16;
+  if (const char* env = std::getenv("EVOC_LANES")) {
+    int e = std::atoi(env);
+    if (pick_kernel(dimp, e)) g = e;
+  }
+  return g;
+}
+
+void launch_epoch(evoc_plan* pl, int32_t t, const float* e_cur, float* e_next,
+                  float* grad_out, cudaStream_t s) {
+  EpochArgs a;
+  a.inc_ptr = pl->inc_ptr.get();
+  a.inc_other = pl->inc_other.get();
+  a.eidx_base = pl->eidx_base.get();
+  a.fire = pl->planes.get() + (size_t)t * (1 + pl->P) * pl->W;
+  a.W = pl->W;
+  a.P = pl->P;
+  a.e_cur = e_cur;
+  a.e_next = e_next;
+  a.m = pl->m.get();
+  a.v = pl->v.get();
+  a.grad_out = grad_out;
+  a.prob_of_node = pl->n_problems > 1 ? pl->prob_of_node.get() : nullptr;
+  a.prob = pl->n_problems > 1 ? pl->prob.get() : nullptr;
+  a.n_total = (uint32_t)pl->n;
+  a.epoch = (uint32_t)t;
+  a.seed = pl->seeds.empty() ? 0 : pl->seeds[0];
+  a.noise = pl->params.noise_level;
+  a.gamma = pl->gamma[t];
+  a.lr_ad = pl->lr_ad[t];
+  a.epsc = pl->epsc[t];
+  a.one_m_b1 = pl->one_m_b1;
+  a.one_m_b2 = pl->one_m_b2;
+  EpochKernel k = pick_kernel(pl->dimp, pl->lanes);
+  const int64_t threads = pl->n * pl->lanes;
+  k<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(a);
+  EVOC_CHECK_LAUNCH();
+}
+
+unsigned blocks_for(int64_t threads, int bs = 256) {
+  return (unsigned)((threads + bs - 1) / bs);
+}
+
+}  // namespace
+
+void concat_graph(const evoc_graph* g, int64_t node_off, int64_t entry_off,
+                  int64_t* dptr, uint32_t* didx, cudaStream_t s);
+void fill_eidx_src(uint2* out, const uint32_t* e_src, int64_t U, cudaStream_t s);
+void add_counts(const int32_t* a, const int32_t* b, int32_t* out, int64_t n,
+                cudaStream_t s);
+
+evoc_ctx* plan_ctx(const evoc_plan* p) { return p->ctx; }
+int64_t plan_n(const evoc_plan* p) { return p->n; }
+int32_t plan_n_epochs(const evoc_plan* p) { return p->params.n_epochs; }
+bool plan_has_edges(const evoc_plan* p) { return p->has_edges; }
+
+evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
+                       int32_t dim, const evoc_embed_params_t& params) {
+  cudaStream_t s = ctx->stream;
+  if (probs.empty()) throw Error(EVOC_ERR_INVALID_ARGUMENT, "no problems");
+  if (dim < 1 || dim > 16)
+    throw Error(EVOC_ERR_UNSUPPORTED, "dim must be in 1..16");
+  if (params.n_epochs < 0)
+    throw Error(EVOC_ERR_INVALID_ARGUMENT, "n_epochs must be >= 0");
+  std::unique_ptr<evoc_plan> pl(new evoc_plan());
+  pl->ctx = ctx;
+  pl->dim = dim;
+  pl->dimp = dim <= 4 ? 4 : (dim <= 8 ? 8 : 16);
+  pl->params = params;
+  pl->n_problems = (int32_t)probs.size();
+  int64_t n = 0, nnz = 0;
+  bool canonical = true;
+  for (auto& p : probs) {
+    if (!p.graph || p.graph->ctx != ctx)
+      throw Error(EVOC_ERR_INVALID_ARGUMENT, "graph belongs to another context");
+    pl->node_base.push_back(n);
+    pl->seeds.push_back(p.seed);
+    n += p.graph->n;
+    nnz += p.graph->nnz;
+    canonical = canonical && p.graph->canonical;
+  }
+  if (n >= (int64_t)0xFFFFFFFFu)
+    throw Error(EVOC_ERR_UNSUPPORTED, "more than 2^32-2 nodes in total");
+  pl->n = n;
+
+  // per-epoch constants (embedding.rs:141-160, :179)
+  const int32_t ne = params.n_epochs;
+  pl->one_m_b1 = 1.0f - params.beta1;
+  pl->one_m_b2 = 1.0f - params.beta2;
+  const float denom = (float)std::max(ne - 1, 1);
+  const float ne_f = (float)ne;
+  for (int32_t ep = 0; ep < ne; ++ep) {
+    const float t = (float)(ep + 1);
+    const float b1t = std::pow(params.beta1, t);
+    const float b2t = std::pow(params.beta2, t);
+    const float sqrt_b2 = std::sqrt(1.0f - b2t);
+    const float ad_scale = sqrt_b2 / (1.0f - b1t);
+    pl->epsc.push_back(sqrt_b2 * params.eps);
+    const float lr = params.initial_alpha * (1.0f - (float)ep / ne_f);
+    pl->lr_ad.push_back(lr * ad_scale);
+    pl->gamma.push_back(0.5f + (float)ep / denom);
+  }
+  pl->stats.assign(ne, evoc_epoch_stats_t{0, 0, 0});
+  if (n == 0) return pl.release();
+
+  // concatenated graph (batched) or the single graph's buffers
+  const int64_t* indptr;
+  const uint32_t* indices;
+  const float* weights;
+  DevBuf<int64_t> cat_ptr;
+  DevBuf<uint32_t> cat_idx;
+  DevBuf<float> cat_w;
+  if (probs.size() == 1) {
+    indptr = probs[0].graph->indptr.get();
+    indices = probs[0].graph->indices.get();
+    weights = probs[0].graph->weights.get();
+  } else {
+    cat_ptr.alloc(n + 1, s);
+    cat_idx.alloc(nnz, s);
+    cat_w.alloc(nnz, s);
+    std::vector<uint32_t> pon_host;
+    std::vector<ProbInfo> info;
+    int64_t eoff = 0;
+    for (size_t q = 0; q < probs.size(); ++q) {
+      const evoc_graph* g = probs[q].graph;
+      const int64_t nb = pl->node_base[q];
+      info.push_back(ProbInfo{(uint32_t)nb, (uint32_t)g->n, probs[q].seed});
+      if (g->n == 0) continue;
+      concat_graph(g, nb, eoff, cat_ptr.get(), cat_idx.get(), s);
+      if (g->nnz)
+        EVOC_CUDA(cudaMemcpyAsync(cat_w.get() + eoff, g->weights.get(),
+                                  g->nnz * sizeof(float),
+                                  cudaMemcpyDeviceToDevice, s));
+      eoff += g->nnz;
+    }
+    EVOC_CUDA(cudaMemcpyAsync(cat_ptr.get() + n, &nnz, sizeof(int64_t),
+                              cudaMemcpyHostToDevice, s));
+    pon_host.resize(n);
+    for (size_t q = 0; q < probs.size(); ++q)
+      for (int64_t i = 0; i < probs[q].graph->n; ++i)
+        pon_host[pl->node_base[q] + i] = (uint32_t)q;
+    pl->prob_of_node.alloc(n, s);
+    pl->prob.alloc(info.size(), s);
+    EVOC_CUDA(cudaMemcpyAsync(pl->prob_of_node.get(), pon_host.data(),
+                              n * sizeof(uint32_t), cudaMemcpyHostToDevice, s));
+    EVOC_CUDA(cudaMemcpyAsync(pl->prob.get(), info.data(),
+                              info.size() * sizeof(ProbInfo),
+                              cudaMemcpyHostToDevice, s));
+    EVOC_CUDA(cudaStreamSynchronize(s));  // host vectors go out of scope
+    indptr = cat_ptr.get();
+    indices = cat_idx.get();
+    weights = cat_w.get();
+  }
+  const uint32_t* pon = pl->n_problems > 1 ? pl->prob_of_node.get() : nullptr;
+
+  // upper / lower counts and the edge list
+  DevBuf<int32_t> ucnt(n, s), lcnt(n, s);
+  k_row_counts<<<blocks_for(n * 32), 256, 0, s>>>(indptr, indices, n, ucnt.get(),
+                                                  lcnt.get());
+  EVOC_CHECK_LAUNCH();
+  DevBuf<int64_t> uptr(n + 1, s);
+  exclusive_scan_i32_to_i64(ucnt.get(), uptr.get(), n, s);
+  int64_t U = 0;
+  EVOC_CUDA(cudaMemcpyAsync(&U, uptr.get() + n, sizeof(int64_t),
+                            cudaMemcpyDeviceToHost, s));
+  EVOC_CUDA(cudaStreamSynchronize(s));
+  pl->n_edges = U;
+  pl->e0.alloc(n * pl->dimp, s);
+  pl->e1.alloc(n * pl->dimp, s);
+  if (U == 0) {  // embedding.rs:92-96
+    pl->has_edges = false;
+    return pl.release();
+  }
+  if (U >= (int64_t)0xFFFFFFFFu)
+    throw Error(EVOC_ERR_UNSUPPORTED, "more than 2^32-2 edges");
+  pl->has_edges = true;
+
+  DevBuf<float> e_w(U, s), e_ps(U, s);
+  DevBuf<uint32_t> e_dst(U, s), e_src(U, s);
+  DevBuf<int32_t> max_w(pl->n_problems, s);
+  EVOC_CUDA(cudaMemsetAsync(max_w.get(), 0, pl->n_problems * sizeof(int32_t), s));
+  if (!canonical) EVOC_CUDA(cudaMemsetAsync(lcnt.get(), 0, n * sizeof(int32_t), s));
+  k_edge_fill<<<blocks_for(n * 32), 256, 0, s>>>(
+      indptr, indices, weights, n, uptr.get(), pon, e_w.get(), e_dst.get(),
+      e_src.get(), max_w.get(), canonical ? nullptr : lcnt.get());
+  EVOC_CHECK_LAUNCH();
+  k_edge_ps<<<blocks_for(U), 256, 0, s>>>(e_w.get(), e_src.get(), U, pon,
+                                          max_w.get(), e_ps.get());
+  EVOC_CHECK_LAUNCH();
+  e_w.release();
+
+  DevBuf<int64_t> lptr;
+  DevBuf<uint2> lower;
+  if (!canonical) {
+    DevBuf<uint32_t> keys(U, s);
+    lower.alloc(U, s);
+    EVOC_CUDA(cudaMemcpyAsync(keys.get(), e_dst.get(), U * sizeof(uint32_t),
+                              cudaMemcpyDeviceToDevice, s));
+    fill_eidx_src(lower.get(), e_src.get(), U, s);
+    radix_sort_pairs(keys.get(), lower.get(), U, bits_for((uint64_t)(n - 1)), s);
+    lptr.alloc(n + 1, s);
+    exclusive_scan_i32_to_i64(lcnt.get(), lptr.get(), n, s);
+  }
+  e_dst.release();
+  e_src.release();
+
+  // incidence lists
+  DevBuf<int32_t> deg(n, s);
+  add_counts(ucnt.get(), lcnt.get(), deg.get(), n, s);
+  pl->inc_ptr.alloc(n + 1, s);
+  exclusive_scan_i32_to_i64(deg.get(), pl->inc_ptr.get(), n, s);
+  deg.release();
+  int64_t n_inc = 0;
+  EVOC_CUDA(cudaMemcpyAsync(&n_inc, pl->inc_ptr.get() + n, sizeof(int64_t),
+                            cudaMemcpyDeviceToHost, s));
+  EVOC_CUDA(cudaStreamSynchronize(s));
+  if (n_inc != 2 * U)
+    throw Error(EVOC_ERR_INTERNAL, "incidence count mismatch (graph not symmetric?)");
+  pl->n_inc = n_inc;
+  DevBuf<int64_t> ebase(pl->n_problems, s);
+  k_prob_ebase<<<blocks_for(pl->n_problems), 256, 0, s>>>(
+      uptr.get(), pl->n_problems > 1 ? pl->prob.get() : nullptr,
+      pl->n_problems, ebase.get());
+  EVOC_CHECK_LAUNCH();
+  pl->inc_other.alloc(n_inc, s);
+  pl->eidx_base.alloc(n, s);
+  DevBuf<float> inc_ps(n_inc, s);
+  DevBuf<uint8_t> inc_up(n_inc, s);
+  k_inc_fill<<<blocks_for(n * 32), 256, 0, s>>>(
+      indptr, indices, weights, n, uptr.get(), lcnt.get(), lptr.get(),
+      lower.get(), e_ps.get(), pl->inc_ptr.get(), pon, max_w.get(), ebase.get(),
+      pl->inc_other.get(), inc_ps.get(), inc_up.get(), pl->eidx_base.get());
+  EVOC_CHECK_LAUNCH();
+  lower.release();
+  lptr.release();
+  e_ps.release();
+
+  // schedule planes
+  const float neg_factor = 1.5f / params.negative_sample_rate;  // embedding.rs:116
+  pl->W = (n_inc + 31) / 32;
+  DevBuf<unsigned long long> mx(1, s), st(2 * std::max(ne, 1), s);
+  EVOC_CUDA(cudaMemsetAsync(mx.get(), 0, sizeof(unsigned long long), s));
+  EVOC_CUDA(cudaMemsetAsync(st.get(), 0, st.bytes(), s));
+  if (ne > 0) {
+    const bool want_stats = ne <= 4096;
+    const size_t smem = want_stats ? 2 * ne * sizeof(unsigned long long) : 0;
+    if (smem > 48 * 1024)
+      EVOC_CUDA(cudaFuncSetAttribute((const void*)k_schedule_scan,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem));
+    k_schedule_scan<<<blocks_for(n_inc), 256, smem, s>>>(
+        inc_ps.get(), inc_up.get(), n_inc, ne, neg_factor, mx.get(),
+        want_stats ? st.get() : nullptr, want_stats ? st.get() + ne : nullptr);
+    EVOC_CHECK_LAUNCH();
+    unsigned long long maxneg = 0;
+    std::vector<unsigned long long> sth(2 * ne);
+    EVOC_CUDA(cudaMemcpyAsync(&maxneg, mx.get(), sizeof(maxneg),
+                              cudaMemcpyDeviceToHost, s));
+    EVOC_CUDA(cudaMemcpyAsync(sth.data(), st.get(), 2 * ne * sizeof(unsigned long long),
+                              cudaMemcpyDeviceToHost, s));
+    EVOC_CUDA(cudaStreamSynchronize(s));
+    if (maxneg > (unsigned long long)NEG_LIMIT)
+      throw Error(EVOC_ERR_UNSUPPORTED,
+                  "more than 2^20 negative samples per edge and epoch "
+                  "(negative_sample_rate too large)");
+    pl->max_neg = maxneg;
+    pl->P = bits_for(maxneg);
+    for (int32_t t = 0; t < ne; ++t) {
+      pl->stats[t].fired_edges = (int64_t)sth[t];
+      pl->stats[t].negatives = (int64_t)sth[ne + t];
+    }
+    pl->planes.alloc((size_t)ne * (1 + pl->P) * pl->W, s);
+    k_schedule_write<<<blocks_for(pl->W * 32), 256, 0, s>>>(
+        inc_ps.get(), inc_up.get(), n_inc, ne, neg_factor, pl->P, pl->W,
+        pl->planes.get());
+    EVOC_CHECK_LAUNCH();
+  }
+
+  pl->m.alloc(n * pl->dimp, s);
+  pl->v.alloc(n * pl->dimp, s);
+  pl->lanes = default_lanes(pl->dimp, (double)n_inc / (double)n);
+  EVOC_CUDA(cudaStreamSynchronize(s));
+  return pl.release();
+}
+
+void plan_stats(const evoc_plan* cpl, evoc_epoch_stats_t* out) {
+  evoc_plan* pl = const_cast<evoc_plan*>(cpl);
+  const int32_t ne = pl->params.n_epochs;
+  if (pl->has_edges && !pl->active_counted && ne > 0) {
+    cudaStream_t s = pl->ctx->stream;
+    DevBuf<unsigned long long> act(ne, s);
+    EVOC_CUDA(cudaMemsetAsync(act.get(), 0, act.bytes(), s));
+    k_active_count<<<blocks_for(pl->n * 32), 256, 0, s>>>(
+        pl->inc_ptr.get(), pl->n, pl->planes.get(), ne, pl->P, pl->W, act.get());
+    EVOC_CHECK_LAUNCH();
+    std::vector<unsigned long long> h(ne);
+    EVOC_CUDA(cudaMemcpyAsync(h.data(), act.get(), ne * sizeof(unsigned long long),
+                              cudaMemcpyDeviceToHost, s));
+    EVOC_CUDA(cudaStreamSynchronize(s));
+    for (int32_t t = 0; t < ne; ++t) pl->stats[t].active_nodes = (int64_t)h[t];
+    pl->active_counted = true;
+  }
+  for (int32_t t = 0; t < ne; ++t) out[t] = pl->stats[t];
+}
+
+// Initial embedding into e0 (padded): from d_init (n*dim) or random.
+static void load_init(evoc_plan* pl, const float* d_init, cudaStream_t s) {
+  const int64_t tot = pl->n * pl->dimp;
+  if (d_init) {
+    k_pad<<<blocks_for(tot), 256, 0, s>>>(d_init, pl->e0.get(), pl->n, pl->dim,
+                                          pl->dimp);
+  } else {
+    k_init_random<<<blocks_for(tot), 256, 0, s>>>(
+        pl->e0.get(), pl->n, pl->dim, pl->dimp,
+        pl->n_problems > 1 ? pl->prob_of_node.get() : nullptr,
+        pl->n_problems > 1 ? pl->prob.get() : nullptr,
+        pl->seeds.empty() ? 0 : pl->seeds[0]);
+  }
+  EVOC_CHECK_LAUNCH();
+}
+
+void plan_run_device(evoc_plan* pl, const float* d_init, float* d_out) {
+  cudaStream_t s = pl->ctx->stream;
+  const int64_t n = pl->n;
+  if (n == 0) return;
+  const int32_t ne = pl->params.n_epochs;
+  load_init(pl, d_init, s);
+  if (pl->has_edges && ne > 0) {
+    EVOC_CUDA(cudaMemsetAsync(pl->m.get(), 0, pl->m.bytes(), s));
+    EVOC_CUDA(cudaMemsetAsync(pl->v.get(), 0, pl->v.bytes(), s));
+    if (!pl->graph_exec) {
+      EVOC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      try {
+        for (int32_t t = 0; t < ne; ++t) {
+          const float* cur = (t & 1) ? pl->e1.get() : pl->e0.get();
+          float* nxt = (t & 1) ? pl->e0.get() : pl->e1.get();
+          launch_epoch(pl, t, cur, nxt, nullptr, s);
+        }
+      } catch (...) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(s, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+      }
+      EVOC_CUDA(cudaStreamEndCapture(s, &pl->graph));
+      EVOC_CUDA(cudaGraphInstantiate(&pl->graph_exec, pl->graph, 0));
+    }
+    EVOC_CUDA(cudaGraphLaunch(pl->graph_exec, s));
+  }
+  const float* fin = (pl->has_edges && (ne & 1)) ? pl->e1.get() : pl->e0.get();
+  k_unpad<<<blocks_for(n * pl->dim), 256, 0, s>>>(fin, d_out, n, pl->dim, pl->dimp);
+  EVOC_CHECK_LAUNCH();
+}
+
+void plan_debug_run(evoc_plan* pl, const float* h_init, int32_t start_epoch,
+                    int32_t end_epoch, float* h_out, float* h_grad) {
+  cudaStream_t s = pl->ctx->stream;
+  const int64_t n = pl->n;
+  if (n == 0) return;
+  const int32_t ne = pl->params.n_epochs;
+  const int64_t nd = n * pl->dim;
+  DevBuf<float> io(nd, s);
+  if (h_init) {
+    EVOC_CUDA(cudaMemcpyAsync(io.get(), h_init, nd * sizeof(float),
+                              cudaMemcpyHostToDevice, s));
+    load_init(pl, io.get(), s);
+  } else {
+    load_init(pl, nullptr, s);
+  }
+  const int32_t e0 = std::max(0, std::min(start_epoch, ne));
+  const int32_t e1 = std::max(e0, std::min(end_epoch, ne));
+  DevBuf<float> grad;
+  if (h_grad) {
+    grad.alloc(n * pl->dimp, s);
+    EVOC_CUDA(cudaMemsetAsync(grad.get(), 0, grad.bytes(), s));
+  }
+  const float* fin = pl->e0.get();
+  if (pl->has_edges && e1 > e0) {
+    EVOC_CUDA(cudaMemsetAsync(pl->m.get(), 0, pl->m.bytes(), s));
+    EVOC_CUDA(cudaMemsetAsync(pl->v.get(), 0, pl->v.bytes(), s));
+    for (int32_t t = e0; t < e1; ++t) {
+      const int k = t - e0;
+      const float* cur = (k & 1) ? pl->e1.get() : pl->e0.get();
+      float* nxt = (k & 1) ? pl->e0.get() : pl->e1.get();
+      launch_epoch(pl, t, cur, nxt, (t == e1 - 1) ? grad.get() : nullptr, s);
+      fin = nxt;
+    }
+  }
+  k_unpad<<<blocks_for(nd), 256, 0, s>>>(fin, io.get(), n, pl->dim, pl->dimp);
+  EVOC_CHECK_LAUNCH();
+  EVOC_CUDA(cudaMemcpyAsync(h_out, io.get(), nd * sizeof(float),
+                            cudaMemcpyDeviceToHost, s));
+  if (h_grad) {
+    k_unpad<<<blocks_for(nd), 256, 0, s>>>(grad.get(), io.get(), n, pl->dim,
+                                           pl->dimp);
+    EVOC_CHECK_LAUNCH();
+    EVOC_CUDA(cudaMemcpyAsync(h_grad, io.get(), nd * sizeof(float),
+                              cudaMemcpyDeviceToHost, s));
+  }
+  EVOC_CUDA(cudaStreamSynchronize(s));
+}
+
+void plan_upload_init_and_run(evoc_plan* pl, const float* const* h_inits,
+                              float* const* h_outs, int verbose) {
+  cudaStream_t s = pl->ctx->stream;
+  const int64_t n = pl->n;
+  if (n == 0) return;
+  const int64_t nd = n * pl->dim;
+  DevBuf<float> io(nd, s);
+  bool all_init = true, any_init = false;
+  for (int32_t q = 0; q < pl->n_problems; ++q) {
+    all_init = all_init && h_inits && h_inits[q];
+    any_init = any_init || (h_inits && h_inits[q]);
+  }
+  if (any_init && !all_init)
+    throw Error(EVOC_ERR_INVALID_ARGUMENT,
+                "either every problem or none must have an initial embedding");
+  if (all_init) {
+    for (int32_t q = 0; q < pl->n_problems; ++q) {
+      const int64_t nq = (q + 1 < pl->n_problems ? pl->node_base[q + 1] : n) -
+                         pl->node_base[q];
+      if (nq)
+        EVOC_CUDA(cudaMemcpyAsync(io.get() + pl->node_base[q] * pl->dim,
+                                  h_inits[q], nq * pl->dim * sizeof(float),
+                                  cudaMemcpyHostToDevice, s));
+    }
+  }
+  plan_run_device(pl, all_init ? io.get() : nullptr, io.get());
+  for (int32_t q = 0; q < pl->n_problems; ++q) {
+    const int64_t nq = (q + 1 < pl->n_problems ? pl->node_base[q + 1] : n) -
+                       pl->node_base[q];
+    if (nq)
+      EVOC_CUDA(cudaMemcpyAsync(h_outs[q], io.get() + pl->node_base[q] * pl->dim,
+                                nq * pl->dim * sizeof(float),
+                                cudaMemcpyDeviceToHost, s));
+  }
+  EVOC_CUDA(cudaStreamSynchronize(s));
+  if (verbose == 2) {  // embedding.rs:288-291
+    const int32_t ne = pl->params.n_epochs;
+    for (int32_t e = 0; e < ne; ++e)
+      if ((e + 1) % 10 == 0 || e + 1 == ne)
+        std::printf("   Embedding epoch %d/%d\n", e + 1, ne);
+    std::fflush(stdout);
+  }
+}
+
+void plan_free(evoc_plan* pl) {
+  if (!pl) return;
+  if (pl->graph_exec) cudaGraphExecDestroy(pl->graph_exec);
+  if (pl->graph) cudaGraphDestroy(pl->graph);
+  delete pl;
+}
+
+// ---- small helpers used by plan_create --------------------------------------
+namespace {
+__global__ void k_concat(const int64_t* __restrict__ src_ptr,
+                         const uint32_t* __restrict__ src_idx, int64_t n,
+                         int64_t nnz, int64_t node_off, int64_t entry_off,
+                         int64_t* __restrict__ dptr, uint32_t* __restrict__ didx) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < n) dptr[node_off + q] = entry_off + src_ptr[q];
+  if (q < nnz) didx[entry_off + q] = (uint32_t)(src_idx[q] + node_off);
+}
+__global__ void k_fill_eidx_src(uint2* __restrict__ out,
+                                const uint32_t* __restrict__ e_src, int64_t U) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < U) out[e] = make_uint2((uint32_t)e, e_src[e]);
+}
+__global__ void k_add_counts(const int32_t* __restrict__ a,
+                             const int32_t* __restrict__ b,
+                             int32_t* __restrict__ out, int64_t n) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = a[i] + b[i];
+}
+}  // namespace
+
+void concat_graph(const evoc_graph* g, int64_t node_off, int64_t entry_off,
+                  int64_t* dptr, uint32_t* didx, cudaStream_t s) {
+  const int64_t m = std::max(g->n, g->nnz);
+  k_concat<<<blocks_for(m), 256, 0, s>>>(g->indptr.get(), g->indices.get(),
+                                         g->n, g->nnz, node_off, entry_off,
+                                         dptr, didx);
+  EVOC_CHECK_LAUNCH();
+}
+
+void fill_eidx_src(uint2* out, const uint32_t* e_src, int64_t U,
+                   cudaStream_t s) {
+  k_fill_eidx_src<<<blocks_for(U), 256, 0, s>>>(out, e_src, U);
+  EVOC_CHECK_LAUNCH();
+}
+
+void add_counts(const int32_t* a, const int32_t* b, int32_t* out, int64_t n,
+                cudaStream_t s) {
+  k_add_counts<<<blocks_for(n), 256, 0, s>>>(a, b, out, n);
+  EVOC_CHECK_LAUNCH();
+}
+
+}  // namespace evoc

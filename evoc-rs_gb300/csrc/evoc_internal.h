@@ -1,0 +1,168 @@
+// evoc_internal.h — shared declarations of the GB300 EVoC library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/evoc_gb300.h"
+
+namespace evoc {
+
+// ---------------------------------------------------------------------------
+// Errors: internal code throws Error; the C ABI catches it and returns code.
+// ---------------------------------------------------------------------------
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] void throw_cuda(cudaError_t e, const char* what, const char* file,
+                             int line);
+
+#define EVOC_CUDA(call)                                           \
+  do {                                                            \
+    cudaError_t _e = (call);                                      \
+    if (_e != cudaSuccess) ::evoc::throw_cuda(_e, #call, __FILE__, __LINE__); \
+  } while (0)
+
+#define EVOC_CHECK_LAUNCH() EVOC_CUDA(cudaGetLastError())
+
+// Device-side status flags (one int32 word per condition). Kernels set a
+// flag with atomicOr and never trap; the host reads the words after a call.
+enum StatusBit : int32_t {
+  ST_BAD_INDEX = 1,      // kNN / graph index >= n
+  ST_BAD_VALUE = 2,      // NaN distance / weight where not allowed
+  ST_EMPTY_ROW = 4,      // empty kNN row with local_connectivity > 0
+  ST_TOO_MANY_NEG = 8,   // negative count per edge-epoch above the limit
+  ST_INTERNAL = 16,      // self-check failed
+};
+
+// ---------------------------------------------------------------------------
+// Stream-ordered device buffer.
+// ---------------------------------------------------------------------------
+template <typename T>
+struct DevBuf {
+  T* ptr = nullptr;
+  size_t count = 0;
+  cudaStream_t stream = nullptr;
+  DevBuf() = default;
+  DevBuf(size_t n, cudaStream_t s) { alloc(n, s); }
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept { *this = std::move(o); }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) {
+      release();
+      ptr = o.ptr; count = o.count; stream = o.stream;
+      o.ptr = nullptr; o.count = 0;
+    }
+    return *this;
+  }
+  ~DevBuf() { release(); }
+  void alloc(size_t n, cudaStream_t s) {
+    release();
+    stream = s;
+    count = n;
+    if (n == 0) return;
+    cudaError_t e = cudaMallocAsync((void**)&ptr, n * sizeof(T), s);
+    if (e != cudaSuccess) {
+      ptr = nullptr;
+      count = 0;
+      (void)cudaGetLastError();
+      throw Error(EVOC_ERR_OUT_OF_MEMORY,
+                  "device allocation of " + std::to_string(n * sizeof(T)) +
+                      " bytes failed: " + cudaGetErrorString(e));
+    }
+  }
+  void release() {
+    if (ptr) cudaFreeAsync(ptr, stream);
+    ptr = nullptr;
+    count = 0;
+  }
+  size_t bytes() const { return count * sizeof(T); }
+  T* get() const { return ptr; }
+};
+
+}  // namespace evoc
+
+// ---------------------------------------------------------------------------
+// Opaque handles of the C ABI.
+// ---------------------------------------------------------------------------
+struct evoc_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+  evoc::DevBuf<int32_t> status;  // device status word
+};
+
+struct evoc_graph {
+  evoc_ctx* ctx = nullptr;
+  int64_t n = 0;
+  int64_t nnz = 0;
+  // true when rows are sorted by column, free of duplicates and self loops,
+  // and symmetric with identical weights in both directions (the output of
+  // the fuzzy union). The embedding set-up then skips its transpose.
+  bool canonical = false;
+  evoc::DevBuf<int64_t> indptr;
+  evoc::DevBuf<uint32_t> indices;
+  evoc::DevBuf<float> weights;
+};
+
+namespace evoc {
+
+// ---- primitives.cu ---------------------------------------------------------
+// out[0..n] = exclusive prefix sum of in[0..n-1]; out[n] = total.
+void exclusive_scan_i32_to_i64(const int32_t* in, int64_t* out, int64_t n,
+                               cudaStream_t s);
+void exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n,
+                        cudaStream_t s);
+// Stable LSD radix sort of (key, value) pairs by key, keys < 2^key_bits.
+// Results are written back to keys/vals.
+void radix_sort_pairs(uint32_t* keys, uint2* vals, int64_t n, int key_bits,
+                      cudaStream_t s);
+int bits_for(uint64_t max_value);
+// Read the context's status word and reset it; throw on any set bit.
+void check_status(evoc_ctx* ctx, const char* where);
+
+// ---- fuzzy_set.cu ----------------------------------------------------------
+void smooth_knn_device(evoc_ctx* ctx, const float* d_dist,
+                       const int32_t* d_row_len, int64_t n, int32_t k,
+                       uint64_t k_target, float local_connectivity,
+                       int32_t n_iter, float* d_sigma, float* d_rho,
+                       float* d_weights_out, const uint32_t* d_idx_for_len);
+void fuzzy_set_device(evoc_ctx* ctx, const uint32_t* d_idx,
+                      const float* d_dist, int64_t n, int32_t k,
+                      float effective_n_neighbours, bool symmetrise,
+                      float* d_sigmas_out, float* d_rhos_out, evoc_graph* out);
+
+// ---- embed.cu --------------------------------------------------------------
+struct ProblemDesc {
+  const evoc_graph* graph;
+  uint64_t seed;
+};
+
+}  // namespace evoc
+
+struct evoc_plan;  // defined in embed.cu
+
+namespace evoc {
+evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
+                       int32_t dim, const evoc_embed_params_t& params);
+void plan_run_device(evoc_plan* plan, const float* d_init, float* d_out);
+void plan_debug_run(evoc_plan* plan, const float* h_init, int32_t start_epoch,
+                    int32_t end_epoch, float* h_out, float* h_grad);
+void plan_stats(const evoc_plan* plan, evoc_epoch_stats_t* stats);
+void plan_free(evoc_plan* plan);
+evoc_ctx* plan_ctx(const evoc_plan* plan);
+int64_t plan_n(const evoc_plan* plan);
+int32_t plan_n_epochs(const evoc_plan* plan);
+bool plan_has_edges(const evoc_plan* plan);
+void plan_upload_init_and_run(evoc_plan* plan, const float* const* h_inits,
+                              float* const* h_outs, int verbose);
+}  // namespace evoc

@@ -1,0 +1,500 @@
+// fuzzy_set.cu — fuzzy simplicial set on the GPU.
+//
+// Replaces, in evoc-rs 0.2.7:
+//   smooth_knn_dist            src/graph/fuzzy_graph.rs:33-98
+//   knn_to_coo                 src/graph/fuzzy_graph.rs:114-159
+//   symmetrise_graph           src/graph/fuzzy_graph.rs:174-228
+//   coo_to_adjacency_list      src/graph/fuzzy_graph.rs:242-256
+//   build_fuzzy_simplicial_set src/graph/fuzzy_graph.rs:275-295
+//
+// Pipeline (all on the context stream):
+//   k_knn_rowlen     warp per row: row length (first EVOC_KNN_PAD) and index
+//                    validation.
+//   k_smooth_knn     thread per row: rho, the sigma bisection with the row's
+//                    distances staged in shared memory, then the membership
+//                    weights. The sum over the row is serial in row order, as
+//                    in the reference (fuzzy_graph.rs:72-76), so sigma is
+//                    bit-identical to a serial CPU evaluation.
+//   k_forward_rows   thread per row: drop self loops, sort by column keeping
+//                    the last of equal columns (HashMap::insert overwrites,
+//                    fuzzy_graph.rs:189), count in-degrees.
+//   radix sort       stable sort of the forward entries by column: each
+//                    column bucket lists its source rows in ascending order,
+//                    which is the backward map of fuzzy_graph.rs:190.
+//   k_union          thread per row: merge the sorted forward and backward
+//                    lists, w = w_ij + w_ji - w_ij * w_ji, keep w > 0
+//                    (fuzzy_graph.rs:196-204); once to count, once to write.
+#include "evoc_device.cuh"
+#include "evoc_internal.h"
+
+#include <algorithm>
+#include <cmath>
+
+namespace evoc {
+namespace {
+
+constexpr uint32_t PAD = EVOC_KNN_PAD;
+
+// ---------------------------------------------------------------------------
+// Row lengths and index validation (warp per row, coalesced).
+// ---------------------------------------------------------------------------
+__global__ void k_knn_rowlen(const uint32_t* __restrict__ idx, int64_t n,
+                             int32_t k, int32_t* __restrict__ row_len,
+                             int32_t* __restrict__ status) {
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const uint32_t* r = idx + row * (int64_t)k;
+  int32_t len = k;
+  for (int32_t base = 0; base < k; base += 32) {
+    const int32_t j = base + lane;
+    const uint32_t c = (j < k) ? r[j] : PAD;
+    const uint32_t pads = __ballot_sync(0xffffffffu, j < k && c == PAD);
+    if (pads) {
+      const int32_t first = base + __ffs(pads) - 1;
+      if (j < first && (int64_t)c >= n) set_status(status, ST_BAD_INDEX);
+      len = first;
+      break;
+    }
+    if (j < k && (int64_t)c >= n) set_status(status, ST_BAD_INDEX);
+  }
+  if (lane == 0) row_len[row] = len;
+}
+
+// ---------------------------------------------------------------------------
+// smooth_knn_dist + membership weights (thread per row).
+// Shared memory holds R rows with an odd stride kp so that threads reading
+// the same column index of different rows hit different banks.
+// ---------------------------------------------------------------------------
+__global__ void k_smooth_knn(const float* __restrict__ dist,
+                             const int32_t* __restrict__ row_len, int64_t n,
+                             int32_t k, int32_t kp, double target, float lc,
+                             int32_t n_iter, float* __restrict__ sigma_out,
+                             float* __restrict__ rho_out,
+                             float* __restrict__ w_out,
+                             int32_t* __restrict__ status) {
+  extern __shared__ float sm[];
+  const int R = blockDim.x;
+  const int64_t row0 = (int64_t)blockIdx.x * R;
+  const int64_t rows_here = min((int64_t)R, n - row0);
+  const int64_t elems = rows_here * k;
+  const float* src = dist + row0 * (int64_t)k;
+  for (int64_t e = threadIdx.x; e < elems; e += R) {
+    const int64_t r = e / k;
+    sm[r * kp + (e - r * k)] = src[e];
+  }
+  __syncthreads();
+  const int64_t i = row0 + threadIdx.x;
+  if (threadIdx.x < rows_here) {
+    float* d = sm + threadIdx.x * kp;
+    const int32_t len = row_len ? row_len[i] : k;
+    bool ok = true;
+    for (int32_t j = 0; j < len; ++j)
+      if (d[j] != d[j]) ok = false;
+    if (!ok) set_status(status, ST_BAD_VALUE);
+    float rho = 0.0f;
+    if (lc > 0.0f) {  // fuzzy_graph.rs:49-62
+      if (len <= 0) {
+        set_status(status, ST_EMPTY_ROW);
+        ok = false;
+      } else {
+        const float lm1 = max0(fsub(lc, 1.0f));
+        const float fl = floorf(lm1);
+        int64_t id = (int64_t)fl;
+        if (id > len - 1) id = len - 1;
+        const float frac = fsub(lm1, fl);
+        if (frac > 0.0f && id + 1 < len)
+          rho = fadd(fmul(d[id], fsub(1.0f, frac)), fmul(d[id + 1], frac));
+        else
+          rho = d[id];
+      }
+    }
+    float lo = 0.0f, hi = 3.40282347e+38f, mid = 1.0f;
+    if (ok) {
+      for (int32_t it = 0; it < n_iter; ++it) {  // fuzzy_graph.rs:71-93
+        float val = 0.0f;
+        for (int32_t j = 0; j < len; ++j) {
+          const float adjusted = max0(fsub(d[j], rho));
+          val = fadd(val, evoc_expf(-fdiv(adjusted, mid)));
+        }
+        const double vd = (double)val;
+        if (fabs(vd - target) < 1e-5) break;
+        if (vd > target) {
+          hi = mid;
+          mid = fdiv(fadd(lo, hi), 2.0f);
+        } else {
+          lo = mid;
+          if (hi == 3.40282347e+38f)
+            mid = fmul(mid, 2.0f);
+          else
+            mid = fdiv(fadd(lo, hi), 2.0f);
+        }
+      }
+    } else {
+      mid = 0.0f;
+      rho = 0.0f;
+    }
+    sigma_out[i] = mid;
+    rho_out[i] = rho;
+    if (w_out) {  // knn_to_coo weights, fuzzy_graph.rs:138-145
+      for (int32_t j = 0; j < len; ++j) {
+        const float adjusted = max0(fsub(d[j], rho));
+        float w;
+        if (mid > 0.0f)
+          w = evoc_expf(-fdiv(adjusted, mid));
+        else
+          w = (adjusted > 0.0f) ? 0.0f : 1.0f;
+        d[j] = w;
+      }
+    }
+  }
+  if (w_out) {
+    __syncthreads();
+    float* dst = w_out + row0 * (int64_t)k;
+    for (int64_t e = threadIdx.x; e < elems; e += R) {
+      const int64_t r = e / k;
+      dst[e] = sm[r * kp + (e - r * k)];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Forward lists: drop self loops, stable insertion sort by column, keep the
+// last entry of each column, count in-degrees. Rows stay padded to k.
+// ---------------------------------------------------------------------------
+__global__ void k_forward_rows(const uint32_t* __restrict__ idx,
+                               const float* __restrict__ w,
+                               const int32_t* __restrict__ row_len, int64_t n,
+                               int32_t k, int32_t kp,
+                               uint32_t* __restrict__ fcol,
+                               float* __restrict__ fw,
+                               int32_t* __restrict__ fcnt,
+                               int32_t* __restrict__ indeg) {
+  extern __shared__ uint32_t smu[];
+  const int R = blockDim.x;
+  uint32_t* sc = smu;
+  float* sw = reinterpret_cast<float*>(smu + (size_t)R * kp);
+  const int64_t row0 = (int64_t)blockIdx.x * R;
+  const int64_t rows_here = min((int64_t)R, n - row0);
+  const int64_t elems = rows_here * k;
+  for (int64_t e = threadIdx.x; e < elems; e += R) {
+    const int64_t r = e / k, j = e - r * k;
+    sc[r * kp + j] = idx[row0 * (int64_t)k + e];
+    sw[r * kp + j] = w[row0 * (int64_t)k + e];
+  }
+  __syncthreads();
+  if (threadIdx.x < rows_here) {
+    const int64_t i = row0 + threadIdx.x;
+    uint32_t* c = sc + threadIdx.x * kp;
+    float* ww = sw + threadIdx.x * kp;
+    const int32_t len = row_len[i];
+    int32_t m = 0;  // compact: drop self loops (fuzzy_graph.rs:135)
+    for (int32_t j = 0; j < len; ++j)
+      if ((int64_t)c[j] != i) {
+        c[m] = c[j];
+        ww[m] = ww[j];
+        ++m;
+      }
+    for (int32_t j = 1; j < m; ++j) {  // stable insertion sort by column
+      const uint32_t cj = c[j];
+      const float wj = ww[j];
+      int32_t q = j - 1;
+      while (q >= 0 && c[q] > cj) {
+        c[q + 1] = c[q];
+        ww[q + 1] = ww[q];
+        --q;
+      }
+      c[q + 1] = cj;
+      ww[q + 1] = wj;
+    }
+    int32_t cnt = 0;  // keep the last of each run of equal columns
+    for (int32_t j = 0; j < m; ++j)
+      if (j + 1 == m || c[j + 1] != c[j]) {
+        c[cnt] = c[j];
+        ww[cnt] = ww[j];
+        ++cnt;
+      }
+    fcnt[i] = cnt;
+    for (int32_t j = 0; j < cnt; ++j) atomicAdd(&indeg[c[j]], 1);
+    for (int32_t j = cnt; j < k; ++j) c[j] = PAD;
+  }
+  __syncthreads();
+  for (int64_t e = threadIdx.x; e < elems; e += R) {
+    const int64_t r = e / k, j = e - r * k;
+    fcol[row0 * (int64_t)k + e] = sc[r * kp + j];
+    fw[row0 * (int64_t)k + e] = sw[r * kp + j];
+  }
+}
+
+// Compact the padded forward lists into (column key, (row, weight)) pairs in
+// row-major order: the input of the stable transpose.
+__global__ void k_forward_compact(const uint32_t* __restrict__ fcol,
+                                  const float* __restrict__ fw,
+                                  const int64_t* __restrict__ fptr, int64_t n,
+                                  int32_t k, uint32_t* __restrict__ keys,
+                                  uint2* __restrict__ vals) {
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const int64_t o = fptr[row];
+  const int32_t cnt = (int32_t)(fptr[row + 1] - o);
+  for (int32_t j = lane; j < cnt; j += 32) {
+    keys[o + j] = fcol[row * (int64_t)k + j];
+    vals[o + j] = make_uint2((uint32_t)row, __float_as_uint(fw[row * (int64_t)k + j]));
+  }
+}
+
+// Fuzzy union of row i: forward list (sorted by column) merged with the
+// backward list (sorted by source row). WRITE = false counts, true writes.
+template <bool WRITE>
+__global__ void k_union(const uint32_t* __restrict__ fcol,
+                        const float* __restrict__ fw,
+                        const int32_t* __restrict__ fcnt,
+                        const int64_t* __restrict__ bptr,
+                        const uint2* __restrict__ bvals, int64_t n, int32_t k,
+                        int32_t* __restrict__ out_cnt,
+                        const int64_t* __restrict__ out_ptr,
+                        uint32_t* __restrict__ out_idx,
+                        float* __restrict__ out_w) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t* fa = fcol + i * (int64_t)k;
+  const float* fwa = fw + i * (int64_t)k;
+  const int32_t na = fcnt[i];
+  const int64_t b0 = bptr[i], b1 = bptr[i + 1];
+  int32_t ia = 0;
+  int64_t ib = b0;
+  int64_t o = WRITE ? out_ptr[i] : 0;
+  int32_t cnt = 0;
+  uint32_t ca = (ia < na) ? fa[ia] : PAD;
+  uint2 bv = (ib < b1) ? bvals[ib] : make_uint2(PAD, 0);
+  while (ia < na || ib < b1) {
+    float w_ij = 0.0f, w_ji = 0.0f;
+    uint32_t j;
+    const uint32_t cb = (ib < b1) ? bv.x : PAD;
+    if (ia < na && (ib >= b1 || ca < cb)) {
+      j = ca;
+      w_ij = fwa[ia];
+      ++ia;
+    } else if (ia >= na || cb < ca) {
+      j = cb;
+      w_ji = __uint_as_float(bv.y);
+      ++ib;
+    } else {
+      j = ca;
+      w_ij = fwa[ia];
+      w_ji = __uint_as_float(bv.y);
+      ++ia;
+      ++ib;
+    }
+    if (ia < na) ca = fa[ia];
+    if (ib < b1) bv = bvals[ib];
+    const float w_sym = fsub(fadd(w_ij, w_ji), fmul(w_ij, w_ji));
+    if (w_sym > 0.0f) {
+      if (WRITE) {
+        out_idx[o] = j;
+        out_w[o] = w_sym;
+        ++o;
+      }
+      ++cnt;
+    }
+  }
+  if (!WRITE) out_cnt[i] = cnt;
+}
+
+// symmetrise == false: the directed COO of knn_to_coo in kNN order.
+template <bool WRITE>
+__global__ void k_directed(const uint32_t* __restrict__ idx,
+                           const float* __restrict__ w,
+                           const int32_t* __restrict__ row_len, int64_t n,
+                           int32_t k, int32_t* __restrict__ out_cnt,
+                           const int64_t* __restrict__ out_ptr,
+                           uint32_t* __restrict__ out_idx,
+                           float* __restrict__ out_w) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int32_t len = row_len[i];
+  int64_t o = WRITE ? out_ptr[i] : 0;
+  int32_t cnt = 0;
+  for (int32_t j = 0; j < len; ++j) {
+    const uint32_t c = idx[i * (int64_t)k + j];
+    if ((int64_t)c == i) continue;
+    if (WRITE) {
+      out_idx[o] = c;
+      out_w[o] = w[i * (int64_t)k + j];
+      ++o;
+    }
+    ++cnt;
+  }
+  if (!WRITE) out_cnt[i] = cnt;
+}
+
+int rows_per_block(int32_t kp) {
+  if ((size_t)128 * kp * 8 <= 48 * 1024) return 128;
+  if ((size_t)64 * kp * 8 <= 96 * 1024) return 64;
+  return 32;
+}
+
+void set_smem_limit(const void* fn, size_t bytes) {
+  if (bytes > 48 * 1024)
+    EVOC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)bytes));
+}
+
+}  // namespace
+
+void smooth_knn_device(evoc_ctx* ctx, const float* d_dist,
+                       const int32_t* d_row_len, int64_t n, int32_t k,
+                       uint64_t k_target, float local_connectivity,
+                       int32_t n_iter, float* d_sigma, float* d_rho,
+                       float* d_weights_out, const uint32_t* /*unused*/) {
+  if (n == 0) return;
+  const int32_t kp = k | 1;
+  const int R = rows_per_block(kp);
+  const size_t smem = (size_t)R * kp * sizeof(float);
+  if (smem > 200 * 1024)
+    throw Error(EVOC_ERR_UNSUPPORTED, "k too large (k <= 1599 supported)");
+  set_smem_limit((const void*)k_smooth_knn, smem);
+  const double target = std::log2((double)k_target);
+  const int64_t blocks = (n + R - 1) / R;
+  k_smooth_knn<<<(unsigned)blocks, R, smem, ctx->stream>>>(
+      d_dist, d_row_len, n, k, kp, target, local_connectivity, n_iter, d_sigma,
+      d_rho, d_weights_out, ctx->status.get());
+  EVOC_CHECK_LAUNCH();
+}
+
+void fuzzy_set_device(evoc_ctx* ctx, const uint32_t* d_idx,
+                      const float* d_dist, int64_t n, int32_t k,
+                      float effective_n_neighbours, bool symmetrise,
+                      float* d_sigmas_out, float* d_rhos_out, evoc_graph* out) {
+  cudaStream_t s = ctx->stream;
+  if (n <= 0)
+    throw Error(EVOC_ERR_INVALID_ARGUMENT,
+                "empty kNN graph (build_fuzzy_simplicial_set reads row 0)");
+  if (k <= 0) throw Error(EVOC_ERR_INVALID_ARGUMENT, "k must be positive");
+  if (n >= (int64_t)PAD) throw Error(EVOC_ERR_UNSUPPORTED, "n must be < 2^32-1");
+
+  DevBuf<int32_t> row_len(n, s);
+  {
+    const int64_t threads = n * 32;
+    k_knn_rowlen<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+        d_idx, n, k, row_len.get(), ctx->status.get());
+    EVOC_CHECK_LAUNCH();
+  }
+  check_status(ctx, "fuzzy set");
+
+  // k = effective_n_neighbors.to_usize().unwrap_or(knn_dists[0].len())
+  // (fuzzy_graph.rs:284-286)
+  uint64_t kk;
+  const float e = effective_n_neighbours;
+  if (e > -1.0f && e < 18446744073709551616.0f) {
+    kk = (uint64_t)e;
+  } else {
+    int32_t len0 = 0;
+    EVOC_CUDA(cudaMemcpyAsync(&len0, row_len.get(), sizeof(int32_t),
+                              cudaMemcpyDeviceToHost, s));
+    EVOC_CUDA(cudaStreamSynchronize(s));
+    kk = (uint64_t)len0;
+  }
+
+  DevBuf<float> sig_local, rho_local;
+  float* d_sig = d_sigmas_out;
+  float* d_rho = d_rhos_out;
+  if (!d_sig) { sig_local.alloc(n, s); d_sig = sig_local.get(); }
+  if (!d_rho) { rho_local.alloc(n, s); d_rho = rho_local.get(); }
+  DevBuf<float> wts(n * (int64_t)k, s);
+  smooth_knn_device(ctx, d_dist, row_len.get(), n, k, kk, 1.0f, 64, d_sig,
+                    d_rho, wts.get(), nullptr);
+  check_status(ctx, "fuzzy set");
+
+  out->ctx = ctx;
+  out->n = n;
+  out->indptr.alloc(n + 1, s);
+  const unsigned row_blocks = (unsigned)((n + 255) / 256);
+
+  if (!symmetrise) {
+    DevBuf<int32_t> cnt(n, s);
+    k_directed<false><<<row_blocks, 256, 0, s>>>(d_idx, wts.get(), row_len.get(),
+                                                  n, k, cnt.get(), nullptr,
+                                                  nullptr, nullptr);
+    EVOC_CHECK_LAUNCH();
+    exclusive_scan_i32_to_i64(cnt.get(), out->indptr.get(), n, s);
+    int64_t nnz = 0;
+    EVOC_CUDA(cudaMemcpyAsync(&nnz, out->indptr.get() + n, sizeof(int64_t),
+                              cudaMemcpyDeviceToHost, s));
+    EVOC_CUDA(cudaStreamSynchronize(s));
+    out->nnz = nnz;
+    out->indices.alloc(nnz, s);
+    out->weights.alloc(nnz, s);
+    k_directed<true><<<row_blocks, 256, 0, s>>>(
+        d_idx, wts.get(), row_len.get(), n, k, nullptr, out->indptr.get(),
+        out->indices.get(), out->weights.get());
+    EVOC_CHECK_LAUNCH();
+    out->canonical = false;
+    EVOC_CUDA(cudaStreamSynchronize(s));
+    return;
+  }
+
+  // forward lists
+  const int32_t kp = k | 1;
+  int R = rows_per_block(kp);
+  const size_t smem = (size_t)R * kp * 8;
+  if (smem > 200 * 1024)
+    throw Error(EVOC_ERR_UNSUPPORTED, "k too large (k <= 1599 supported)");
+  set_smem_limit((const void*)k_forward_rows, smem);
+  DevBuf<uint32_t> fcol(n * (int64_t)k, s);
+  DevBuf<float> fw(n * (int64_t)k, s);
+  DevBuf<int32_t> fcnt(n, s), indeg(n, s);
+  EVOC_CUDA(cudaMemsetAsync(indeg.get(), 0, n * sizeof(int32_t), s));
+  k_forward_rows<<<(unsigned)((n + R - 1) / R), R, smem, s>>>(
+      d_idx, wts.get(), row_len.get(), n, k, kp, fcol.get(), fw.get(),
+      fcnt.get(), indeg.get());
+  EVOC_CHECK_LAUNCH();
+  wts.release();
+
+  DevBuf<int64_t> fptr(n + 1, s), bptr(n + 1, s);
+  exclusive_scan_i32_to_i64(fcnt.get(), fptr.get(), n, s);
+  exclusive_scan_i32_to_i64(indeg.get(), bptr.get(), n, s);
+  int64_t nf = 0;
+  EVOC_CUDA(cudaMemcpyAsync(&nf, fptr.get() + n, sizeof(int64_t),
+                            cudaMemcpyDeviceToHost, s));
+  EVOC_CUDA(cudaStreamSynchronize(s));
+
+  // stable transpose: sort forward entries by column
+  DevBuf<uint32_t> keys(nf, s);
+  DevBuf<uint2> vals(nf, s);
+  if (nf > 0) {
+    const int64_t threads = n * 32;
+    k_forward_compact<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(
+        fcol.get(), fw.get(), fptr.get(), n, k, keys.get(), vals.get());
+    EVOC_CHECK_LAUNCH();
+    radix_sort_pairs(keys.get(), vals.get(), nf, bits_for((uint64_t)(n - 1)), s);
+  }
+  keys.release();
+  fptr.release();
+
+  DevBuf<int32_t> ucnt(n, s);
+  k_union<false><<<row_blocks, 256, 0, s>>>(fcol.get(), fw.get(), fcnt.get(),
+                                            bptr.get(), vals.get(), n, k,
+                                            ucnt.get(), nullptr, nullptr,
+                                            nullptr);
+  EVOC_CHECK_LAUNCH();
+  exclusive_scan_i32_to_i64(ucnt.get(), out->indptr.get(), n, s);
+  int64_t nnz = 0;
+  EVOC_CUDA(cudaMemcpyAsync(&nnz, out->indptr.get() + n, sizeof(int64_t),
+                            cudaMemcpyDeviceToHost, s));
+  EVOC_CUDA(cudaStreamSynchronize(s));
+  out->nnz = nnz;
+  out->indices.alloc(nnz, s);
+  out->weights.alloc(nnz, s);
+  k_union<true><<<row_blocks, 256, 0, s>>>(fcol.get(), fw.get(), fcnt.get(),
+                                           bptr.get(), vals.get(), n, k,
+                                           nullptr, out->indptr.get(),
+                                           out->indices.get(),
+                                           out->weights.get());
+  EVOC_CHECK_LAUNCH();
+  out->canonical = true;
+  EVOC_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace evoc

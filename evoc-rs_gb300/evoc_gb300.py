@@ -1,0 +1,370 @@
+"""ctypes binding of libevoc_gb300.so (the C ABI in include/evoc_gb300.h).
+
+The binding mirrors the Rust functions the library replaces in evoc-rs 0.2.7:
+
+    build_fuzzy_simplicial_set   src/graph/fuzzy_graph.rs:275-295
+    coo_to_adjacency_list        src/graph/fuzzy_graph.rs:242-256
+    smooth_knn_dist              src/graph/fuzzy_graph.rs:33-98
+    evoc_embedding               src/graph/embedding.rs:48-298
+    EvocEmbeddingParams          src/graph/mod.rs:22-67
+
+There is no CPU fallback: importing works anywhere, but creating a Context
+raises EvocError when the shared library or an sm_103 GPU is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+from pathlib import Path
+from typing import Sequence
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = Path(os.environ.get("EVOC_GB300_LIB", _HERE / "libevoc_gb300.so"))
+
+EVOC_OK = 0
+EVOC_ERR_INVALID_ARGUMENT = -1
+EVOC_ERR_INVALID_INPUT = -2
+EVOC_ERR_UNSUPPORTED = -3
+EVOC_ERR_CUDA = -4
+EVOC_ERR_OUT_OF_MEMORY = -5
+EVOC_ERR_NO_DEVICE = -6
+EVOC_ERR_INTERNAL = -7
+KNN_PAD = 0xFFFFFFFF
+
+# Every symbol declared in include/evoc_gb300.h.
+EXPORTED = [
+    "evoc_abi_version", "evoc_embed_params_default", "evoc_ctx_create",
+    "evoc_ctx_destroy", "evoc_last_error", "evoc_smooth_knn_dist",
+    "evoc_fuzzy_set", "evoc_fuzzy_set_device", "evoc_graph_from_csr",
+    "evoc_graph_info", "evoc_graph_export", "evoc_graph_free", "evoc_embed",
+    "evoc_plan_create", "evoc_plan_run_device", "evoc_plan_stats",
+    "evoc_plan_debug_run", "evoc_plan_free", "evoc_embed_batched",
+]
+
+
+class EvocError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+
+
+class EmbedParamsC(C.Structure):
+    _fields_ = [
+        ("n_epochs", C.c_int32),
+        ("noise_level", C.c_float),
+        ("negative_sample_rate", C.c_float),
+        ("initial_alpha", C.c_float),
+        ("beta1", C.c_float),
+        ("beta2", C.c_float),
+        ("eps", C.c_float),
+    ]
+
+
+class EpochStatsC(C.Structure):
+    _fields_ = [("fired_edges", C.c_int64), ("negatives", C.c_int64),
+                ("active_nodes", C.c_int64)]
+
+
+@dataclass
+class EvocEmbeddingParams:
+    """Mirror of EvocEmbeddingParams (src/graph/mod.rs:22-67) with its defaults."""
+    n_epochs: int = 50
+    noise_level: float = 0.5
+    negative_sample_rate: float = 1.0
+    initial_alpha: float = 0.1
+    beta1: float = 0.5
+    beta2: float = 0.9
+    eps: float = 1e-7
+
+    def to_c(self) -> EmbedParamsC:
+        return EmbedParamsC(int(self.n_epochs), self.noise_level,
+                            self.negative_sample_rate, self.initial_alpha,
+                            self.beta1, self.beta2, self.eps)
+
+
+_lib = None
+
+
+def load_library(path: Path | str | None = None) -> C.CDLL:
+    """Load the shared library and declare its signatures (no GPU needed)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise EvocError(EVOC_ERR_NO_DEVICE,
+                        f"{p} not found: build it with python evoc-rs_gb300/build.py")
+    lib = C.CDLL(str(p))
+    vp, i32, i64, u64, f32 = C.c_void_p, C.c_int32, C.c_int64, C.c_uint64, C.c_float
+    pp = C.POINTER(C.c_void_p)
+    sig = {
+        "evoc_abi_version": ([], C.c_int),
+        "evoc_embed_params_default": ([C.POINTER(EmbedParamsC)], None),
+        "evoc_ctx_create": ([C.c_int, pp], C.c_int),
+        "evoc_ctx_destroy": ([vp], None),
+        "evoc_last_error": ([vp], C.c_char_p),
+        "evoc_smooth_knn_dist": ([vp, vp, vp, i64, i32, u64, f32, i32, vp, vp], C.c_int),
+        "evoc_fuzzy_set": ([vp, vp, vp, i64, i32, f32, C.c_int, pp], C.c_int),
+        "evoc_fuzzy_set_device": ([vp, vp, vp, i64, i32, f32, C.c_int, vp, vp, pp], C.c_int),
+        "evoc_graph_from_csr": ([vp, vp, vp, vp, i64, pp], C.c_int),
+        "evoc_graph_info": ([vp, C.POINTER(i64), C.POINTER(i64)], C.c_int),
+        "evoc_graph_export": ([vp, vp, vp, vp], C.c_int),
+        "evoc_graph_free": ([vp], None),
+        "evoc_embed": ([vp, vp, i32, C.POINTER(EmbedParamsC), vp, u64, i32, vp], C.c_int),
+        "evoc_plan_create": ([vp, vp, i32, C.POINTER(EmbedParamsC), u64, pp], C.c_int),
+        "evoc_plan_run_device": ([vp, vp, vp], C.c_int),
+        "evoc_plan_stats": ([vp, C.POINTER(EpochStatsC)], C.c_int),
+        "evoc_plan_debug_run": ([vp, vp, i32, i32, vp, vp], C.c_int),
+        "evoc_plan_free": ([vp], None),
+        "evoc_embed_batched": ([vp, i32, vp, i32, C.POINTER(EmbedParamsC), vp, vp, vp], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    if lib.evoc_abi_version() != 1:
+        raise EvocError(EVOC_ERR_INTERNAL, "ABI version mismatch")
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class Graph:
+    """Device-resident weighted adjacency list (evoc_graph_t)."""
+
+    def __init__(self, ctx: "Context", handle: C.c_void_p):
+        self._ctx = ctx
+        self.handle = handle
+
+    @property
+    def n(self) -> int:
+        return self.info()[0]
+
+    @property
+    def nnz(self) -> int:
+        return self.info()[1]
+
+    def info(self) -> tuple[int, int]:
+        n, nnz = C.c_int64(), C.c_int64()
+        self._ctx._check(self._ctx.lib.evoc_graph_info(self.handle, C.byref(n), C.byref(nnz)))
+        return n.value, nnz.value
+
+    def export(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        n, nnz = self.info()
+        indptr = np.zeros(n + 1, dtype=np.int64)
+        indices = np.zeros(nnz, dtype=np.uint32)
+        weights = np.zeros(nnz, dtype=np.float32)
+        self._ctx._check(self._ctx.lib.evoc_graph_export(
+            self.handle, _ptr(indptr), _ptr(indices), _ptr(weights)))
+        return indptr, indices, weights
+
+    def to_coo(self) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        """CoordinateList form: (row_indices, col_indices, values)."""
+        indptr, indices, weights = self.export()
+        rows = np.repeat(np.arange(len(indptr) - 1, dtype=np.int64), np.diff(indptr))
+        return rows, indices.astype(np.int64), weights
+
+    def free(self) -> None:
+        if self.handle:
+            self._ctx.lib.evoc_graph_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Plan:
+    """Per-graph set-up of evoc_embedding, reusable across runs (evoc_plan_t)."""
+
+    def __init__(self, ctx: "Context", handle, n: int, dim: int, n_epochs: int):
+        self._ctx = ctx
+        self.handle = handle
+        self.n, self.dim, self.n_epochs = n, dim, n_epochs
+
+    def run_device(self, d_init: int | None, d_out: int) -> None:
+        self._ctx._check(self._ctx.lib.evoc_plan_run_device(
+            self.handle, C.c_void_p(d_init) if d_init else None, C.c_void_p(d_out)))
+
+    def stats(self) -> np.ndarray:
+        arr = (EpochStatsC * max(self.n_epochs, 1))()
+        self._ctx._check(self._ctx.lib.evoc_plan_stats(self.handle, arr))
+        out = np.zeros((self.n_epochs, 3), dtype=np.int64)
+        for t in range(self.n_epochs):
+            out[t] = (arr[t].fired_edges, arr[t].negatives, arr[t].active_nodes)
+        return out
+
+    def debug_run(self, init: np.ndarray | None, start_epoch: int, end_epoch: int,
+                  want_grad: bool = False):
+        out = np.zeros((self.n, self.dim), dtype=np.float32)
+        grad = np.zeros((self.n, self.dim), dtype=np.float32) if want_grad else None
+        init_c = None if init is None else _f32(init)
+        self._ctx._check(self._ctx.lib.evoc_plan_debug_run(
+            self.handle, _ptr(init_c), start_epoch, end_epoch, _ptr(out), _ptr(grad)))
+        return (out, grad) if want_grad else out
+
+    def free(self) -> None:
+        if self.handle:
+            self._ctx.lib.evoc_plan_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Context:
+    """One CUDA device and stream (evoc_ctx_t)."""
+
+    def __init__(self, device: int = 0, lib_path: str | None = None):
+        self.lib = load_library(lib_path)
+        h = C.c_void_p()
+        rc = self.lib.evoc_ctx_create(device, C.byref(h))
+        if rc != EVOC_OK:
+            raise EvocError(rc, self.lib.evoc_last_error(None).decode())
+        self.handle = h
+
+    def _check(self, rc: int) -> None:
+        if rc != EVOC_OK:
+            raise EvocError(rc, self.lib.evoc_last_error(self.handle).decode())
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            self.lib.evoc_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- fuzzy simplicial set -------------------------------------------
+    def smooth_knn_dist(self, dists, k: int, local_connectivity: float = 1.0,
+                        n_iter: int = 64, row_len=None):
+        d = _f32(dists)
+        n, kk = d.shape
+        rl = None if row_len is None else np.ascontiguousarray(row_len, dtype=np.int32)
+        sig = np.zeros(n, dtype=np.float32)
+        rho = np.zeros(n, dtype=np.float32)
+        self._check(self.lib.evoc_smooth_knn_dist(self.handle, _ptr(d), _ptr(rl), n, kk, int(k),
+                                                  float(local_connectivity), int(n_iter),
+                                                  _ptr(sig), _ptr(rho)))
+        return sig, rho
+
+    def fuzzy_set(self, knn_idx, knn_dist, effective_n_neighbours: float,
+                  symmetrise: bool = True) -> Graph:
+        idx = np.ascontiguousarray(knn_idx, dtype=np.uint32)
+        dist = _f32(knn_dist)
+        if idx.ndim != 2 or idx.shape != dist.shape:
+            raise EvocError(EVOC_ERR_INVALID_ARGUMENT, "knn_idx/knn_dist must be n x k")
+        h = C.c_void_p()
+        self._check(self.lib.evoc_fuzzy_set(self.handle, _ptr(idx), _ptr(dist), idx.shape[0],
+                                            idx.shape[1], float(effective_n_neighbours),
+                                            int(bool(symmetrise)), C.byref(h)))
+        return Graph(self, h)
+
+    def fuzzy_set_device(self, d_idx: int, d_dist: int, n: int, k: int,
+                         effective_n_neighbours: float, symmetrise: bool = True,
+                         d_sigmas: int | None = None, d_rhos: int | None = None) -> Graph:
+        h = C.c_void_p()
+        self._check(self.lib.evoc_fuzzy_set_device(
+            self.handle, C.c_void_p(d_idx), C.c_void_p(d_dist), n, k,
+            float(effective_n_neighbours), int(bool(symmetrise)),
+            C.c_void_p(d_sigmas) if d_sigmas else None,
+            C.c_void_p(d_rhos) if d_rhos else None, C.byref(h)))
+        return Graph(self, h)
+
+    def graph_from_csr(self, indptr, indices, weights) -> Graph:
+        ip = np.ascontiguousarray(indptr, dtype=np.int64)
+        ix = np.ascontiguousarray(indices, dtype=np.uint32)
+        w = _f32(weights)
+        h = C.c_void_p()
+        self._check(self.lib.evoc_graph_from_csr(self.handle, _ptr(ip), _ptr(ix), _ptr(w),
+                                                 len(ip) - 1, C.byref(h)))
+        return Graph(self, h)
+
+    def graph_from_adjacency(self, adj: Sequence[Sequence[tuple[int, float]]]) -> Graph:
+        """Upload a Vec<Vec<(usize, T)>>-style adjacency list."""
+        indptr = np.zeros(len(adj) + 1, dtype=np.int64)
+        for i, row in enumerate(adj):
+            indptr[i + 1] = indptr[i] + len(row)
+        indices = np.array([j for row in adj for j, _ in row], dtype=np.uint32)
+        weights = np.array([w for row in adj for _, w in row], dtype=np.float32)
+        return self.graph_from_csr(indptr, indices, weights)
+
+    # ---- embedding ------------------------------------------------------
+    def embed(self, graph: Graph, dim: int, params: EvocEmbeddingParams | None = None,
+              init=None, seed: int = 42, verbose: int = 0) -> np.ndarray:
+        p = (params or EvocEmbeddingParams()).to_c()
+        n = graph.n
+        out = np.zeros((n, dim), dtype=np.float32)
+        ini = None if init is None else _f32(init)
+        if ini is not None and ini.shape != (n, dim):
+            raise EvocError(EVOC_ERR_INVALID_ARGUMENT, "init must be n x dim")
+        self._check(self.lib.evoc_embed(self.handle, graph.handle, dim, C.byref(p), _ptr(ini),
+                                        C.c_uint64(seed), verbose, _ptr(out)))
+        return out
+
+    def plan(self, graph: Graph, dim: int, params: EvocEmbeddingParams | None = None,
+             seed: int = 42) -> Plan:
+        pr = params or EvocEmbeddingParams()
+        p = pr.to_c()
+        h = C.c_void_p()
+        self._check(self.lib.evoc_plan_create(self.handle, graph.handle, dim, C.byref(p),
+                                              C.c_uint64(seed), C.byref(h)))
+        return Plan(self, h, graph.n, dim, pr.n_epochs)
+
+    def embed_batched(self, graphs: Sequence[Graph], dim: int,
+                      params: EvocEmbeddingParams | None = None,
+                      inits: Sequence[np.ndarray] | None = None,
+                      seeds: Sequence[int] | None = None) -> list[np.ndarray]:
+        p = (params or EvocEmbeddingParams()).to_c()
+        m = len(graphs)
+        outs = [np.zeros((g.n, dim), dtype=np.float32) for g in graphs]
+        gh = (C.c_void_p * m)(*[g.handle for g in graphs])
+        oh = (C.c_void_p * m)(*[o.ctypes.data for o in outs])
+        sd = (C.c_uint64 * m)(*(seeds if seeds is not None else [42] * m))
+        keep = None
+        ih = None
+        if inits is not None:
+            keep = [_f32(x) for x in inits]
+            ih = (C.c_void_p * m)(*[x.ctypes.data for x in keep])
+        self._check(self.lib.evoc_embed_batched(self.handle, m, gh, dim, C.byref(p), ih, sd, oh))
+        return outs
+
+
+# ---- reference-named functions -----------------------------------------------
+def build_fuzzy_simplicial_set(ctx: Context, knn_indices, knn_dists,
+                               effective_n_neighbours: float, symmetrise: bool) -> Graph:
+    """build_fuzzy_simplicial_set (fuzzy_graph.rs:275-295); the graph stays on the GPU."""
+    return ctx.fuzzy_set(knn_indices, knn_dists, effective_n_neighbours, symmetrise)
+
+
+def coo_to_adjacency_list(graph: Graph) -> list[list[tuple[int, float]]]:
+    """coo_to_adjacency_list (fuzzy_graph.rs:242-256) of a device graph, on the host."""
+    indptr, indices, weights = graph.export()
+    return [[(int(indices[p]), float(weights[p])) for p in range(indptr[i], indptr[i + 1])]
+            for i in range(len(indptr) - 1)]
+
+
+def evoc_embedding(ctx: Context, graph: Graph, n_components: int,
+                   params: EvocEmbeddingParams | None = None, initial_embedding=None,
+                   seed: int = 42, verbose: int = 0) -> np.ndarray:
+    """evoc_embedding (embedding.rs:48-298)."""
+    return ctx.embed(graph, n_components, params, initial_embedding, seed, verbose)

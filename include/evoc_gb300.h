@@ -1,0 +1,209 @@
+/*
+ * evoc_gb300.h — C ABI of the GB300 (sm_103a) EVoC hot path.
+ *
+ * This library replaces two Rust calls of evoc-rs 0.2.7 with CUDA kernels:
+ *
+ *   build_fuzzy_simplicial_set + coo_to_adjacency_list
+ *       (src/graph/fuzzy_graph.rs:275-295 and :242-256,
+ *        called at src/lib.rs:254-256 and src/lib.rs:551-553)
+ *   evoc_embedding
+ *       (src/graph/embedding.rs:48-298,
+ *        called at src/lib.rs:302-309, src/lib.rs:603-610 and
+ *        src/graph/label_prop.rs:472-479)
+ *
+ * Conventions
+ *   - Every entry point returns EVOC_OK (0) or a negative status code.
+ *     evoc_last_error() returns a message for the last failure on a context.
+ *   - Host pointers are caller-owned. Output buffers are caller-allocated,
+ *     with sizes given by the accompanying counts.
+ *   - Graphs and embedding plans are opaque device-resident handles that are
+ *     released with their *_free function.
+ *   - Calls are synchronous: on return every output has been written.
+ *   - A context owns one CUDA stream and must be used by one host thread at a
+ *     time. Different contexts are independent.
+ *   - Node ids are uint32; n must be below 2^32 - 1. Entry offsets are int64.
+ *   - A kNN row shorter than k is padded at its end with index
+ *     EVOC_KNN_PAD; padded entries are ignored (their distance is unused).
+ *
+ * Numerics (f32 throughout, like the reference's GPU stance, README.md:125-129)
+ *   - exp() is the library's own Cody-Waite/Taylor exponential (<= 2 ulp).
+ *   - Negative samples come from a Philox4x32-10 stream keyed by the seed and
+ *     the edge id, not from rand::SmallRng (embedding.rs:173-175, :231).
+ *   - Per-node neighbour order is ascending column, not FxHashMap order
+ *     (fuzzy_graph.rs:196-205).
+ *   - The per-node gradient is summed in a fixed order (32 virtual lanes, each
+ *     summing entries q = lane mod 32 in list order, then a pairwise tree with
+ *     strides 16, 8, 4, 2, 1). Results are bit-reproducible and do not depend
+ *     on launch configuration.
+ */
+#ifndef EVOC_GB300_H
+#define EVOC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define EVOC_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define EVOC_API __attribute__((visibility("default")))
+#else
+#define EVOC_API
+#endif
+
+/* status codes */
+#define EVOC_OK 0
+#define EVOC_ERR_INVALID_ARGUMENT (-1) /* bad pointer, size or parameter     */
+#define EVOC_ERR_INVALID_INPUT (-2)    /* bad index / value in input arrays  */
+#define EVOC_ERR_UNSUPPORTED (-3)      /* valid but outside supported range  */
+#define EVOC_ERR_CUDA (-4)             /* CUDA runtime error                 */
+#define EVOC_ERR_OUT_OF_MEMORY (-5)    /* device allocation failed           */
+#define EVOC_ERR_NO_DEVICE (-6)        /* no usable sm_103 device            */
+#define EVOC_ERR_INTERNAL (-7)         /* device-side self-check failed      */
+
+#define EVOC_KNN_PAD 0xFFFFFFFFu
+
+typedef struct evoc_ctx evoc_ctx_t;
+typedef struct evoc_graph evoc_graph_t;
+typedef struct evoc_plan evoc_plan_t;
+
+/* Mirror of EvocEmbeddingParams (src/graph/mod.rs:22-49; defaults :52-67).
+ * The fields n_label_prop_iter, base_init_threshold and scaling are not read
+ * by evoc_embedding and are therefore absent. */
+typedef struct {
+  int32_t n_epochs;           /* default 50   */
+  float noise_level;          /* default 0.5  */
+  float negative_sample_rate; /* default 1.0  */
+  float initial_alpha;        /* default 0.1  */
+  float beta1;                /* default 0.5  (UMAP_BETA1, mod.rs:16) */
+  float beta2;                /* default 0.9  (UMAP_BETA2, mod.rs:18) */
+  float eps;                  /* default 1e-7 */
+} evoc_embed_params_t;
+
+/* Per-epoch work counts of an embedding run, from the deterministic
+ * epochs-per-sample schedule (embedding.rs:98-118, :274-286). */
+typedef struct {
+  int64_t fired_edges;   /* undirected edges with epoch_of_next_sample <= t */
+  int64_t negatives;     /* negative draws made at epoch t (incl. k == node) */
+  int64_t active_nodes;  /* nodes with at least one fired incident edge      */
+} evoc_epoch_stats_t;
+
+/* ---- library / context --------------------------------------------------- */
+
+/* ABI version of the loaded library (EVOC_ABI_VERSION). No counterpart. */
+EVOC_API int evoc_abi_version(void);
+
+/* Fill *p with the reference defaults (EvocEmbeddingParams::default,
+ * src/graph/mod.rs:52-67). */
+EVOC_API void evoc_embed_params_default(evoc_embed_params_t* p);
+
+/* Create a context on CUDA device `device`. Replaces the implicit rayon
+ * global pool of the reference (no counterpart function). */
+EVOC_API int evoc_ctx_create(int device, evoc_ctx_t** out);
+EVOC_API void evoc_ctx_destroy(evoc_ctx_t* ctx);
+
+/* Message of the last failure on ctx (never NULL). With ctx == NULL the
+ * message of the last failed evoc_ctx_create on this thread is returned. */
+EVOC_API const char* evoc_last_error(const evoc_ctx_t* ctx);
+
+/* ---- fuzzy simplicial set ------------------------------------------------ */
+
+/* smooth_knn_dist (src/graph/fuzzy_graph.rs:33-98) on host arrays.
+ * dists: n*k row-major; row i has row_len[i] entries (row_len may be NULL:
+ * every row has k). k_target is the usize `k` of the reference (target =
+ * log2(k_target)). Writes sigmas[n], rhos[n]. */
+EVOC_API int evoc_smooth_knn_dist(evoc_ctx_t* ctx, const float* dists,
+                         const int32_t* row_len, int64_t n, int32_t k,
+                         uint64_t k_target, float local_connectivity,
+                         int32_t n_iter, float* sigmas, float* rhos);
+
+/* build_fuzzy_simplicial_set (fuzzy_graph.rs:275-295) followed by
+ * coo_to_adjacency_list (fuzzy_graph.rs:242-256), from a host kNN graph.
+ * knn_idx/knn_dist: n*k row-major (rows padded with EVOC_KNN_PAD).
+ * effective_n_neighbours: the reference's T-valued effective k
+ * (lib.rs:253: neighbour_scale * n_neighbours). symmetrise: fuzzy union
+ * (fuzzy_graph.rs:174-228) when nonzero. The result stays on the device. */
+EVOC_API int evoc_fuzzy_set(evoc_ctx_t* ctx, const uint32_t* knn_idx,
+                   const float* knn_dist, int64_t n, int32_t k,
+                   float effective_n_neighbours, int symmetrise,
+                   evoc_graph_t** out_graph);
+
+/* Same as evoc_fuzzy_set with knn_idx/knn_dist already in device memory of
+ * the context's device. Optionally also returns sigmas/rhos (device, n each;
+ * NULL to skip). */
+EVOC_API int evoc_fuzzy_set_device(evoc_ctx_t* ctx, const uint32_t* d_knn_idx,
+                          const float* d_knn_dist, int64_t n, int32_t k,
+                          float effective_n_neighbours, int symmetrise,
+                          float* d_sigmas, float* d_rhos,
+                          evoc_graph_t** out_graph);
+
+/* Upload a weighted adjacency list (the reference's Vec<Vec<(usize, T)>>)
+ * given as CSR: indptr[n+1], indices[nnz], weights[nnz] on the host. */
+EVOC_API int evoc_graph_from_csr(evoc_ctx_t* ctx, const int64_t* indptr,
+                        const uint32_t* indices, const float* weights,
+                        int64_t n, evoc_graph_t** out_graph);
+
+/* Number of nodes and of directed entries of a graph. */
+EVOC_API int evoc_graph_info(const evoc_graph_t* g, int64_t* n, int64_t* nnz);
+
+/* Copy a graph to host CSR arrays (indptr[n+1], indices[nnz], weights[nnz]);
+ * rows hold the adjacency list of coo_to_adjacency_list in order. */
+EVOC_API int evoc_graph_export(const evoc_graph_t* g, int64_t* indptr,
+                      uint32_t* indices, float* weights);
+
+EVOC_API void evoc_graph_free(evoc_graph_t* g);
+
+/* ---- node embedding -------------------------------------------------------
+ * evoc_embedding (src/graph/embedding.rs:48-298).
+ * dim: n_components (1..16). init: host n*dim (row-major) or NULL for the
+ * uniform(-0.25, 0.25) initialisation (embedding.rs:69-76). out: host n*dim.
+ * verbose follows parse_verbosity_level (prelude.rs:54-61): 2 prints every
+ * 10 epochs like embedding.rs:288-291. */
+EVOC_API int evoc_embed(evoc_ctx_t* ctx, const evoc_graph_t* g, int32_t dim,
+               const evoc_embed_params_t* params, const float* init,
+               uint64_t seed, int32_t verbose, float* out);
+
+/* A plan holds the per-graph set-up of evoc_embedding (edge extraction,
+ * schedule, per-node incidence lists: embedding.rs:78-175) so that the epoch
+ * loop (embedding.rs:178-292) can be run repeatedly. */
+EVOC_API int evoc_plan_create(evoc_ctx_t* ctx, const evoc_graph_t* g, int32_t dim,
+                     const evoc_embed_params_t* params, uint64_t seed,
+                     evoc_plan_t** out_plan);
+
+/* Run the epoch loop from d_init (device n*dim, or NULL for the random
+ * initialisation) and write d_out (device n*dim). d_init may equal d_out. */
+EVOC_API int evoc_plan_run_device(evoc_plan_t* plan, const float* d_init, float* d_out);
+
+/* Per-epoch work counts (stats[params.n_epochs]). */
+EVOC_API int evoc_plan_stats(const evoc_plan_t* plan, evoc_epoch_stats_t* stats);
+
+/* Debug/parity hook: run epochs [start_epoch, end_epoch) from the host
+ * embedding `init` with zero Adam moments, after advancing the schedule
+ * through epochs [0, start_epoch) (embedding.rs:274-286 only). Writes the
+ * resulting embedding to out (host n*dim) and, if grad_out is not NULL, the
+ * gradient of the last epoch run (embedding.rs:187-253) to grad_out
+ * (host n*dim; zeros for inactive nodes). */
+EVOC_API int evoc_plan_debug_run(evoc_plan_t* plan, const float* init,
+                        int32_t start_epoch, int32_t end_epoch, float* out,
+                        float* grad_out);
+
+EVOC_API void evoc_plan_free(evoc_plan_t* plan);
+
+/* ---- batched embedding -----------------------------------------------------
+ * Many independent evoc_embedding problems in one launch per epoch (no
+ * counterpart in the reference). graphs[p], inits[p] (host or NULL),
+ * seeds[p], outs[p] (host n_p*dim). All problems share dim and params.
+ * Results equal those of separate evoc_embed calls bit for bit. */
+EVOC_API int evoc_embed_batched(evoc_ctx_t* ctx, int32_t n_problems,
+                       const evoc_graph_t* const* graphs, int32_t dim,
+                       const evoc_embed_params_t* params,
+                       const float* const* inits, const uint64_t* seeds,
+                       float* const* outs);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EVOC_GB300_H */

@@ -1,0 +1,197 @@
+"""ctypes wrapper of the CPU oracle (oracle/evoc_oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: used by tests/, by __graft_entry__.smoke() as the
+checker, and by bench.py's CPU baseline. The product never imports this.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+SRC = HERE / "evoc_oracle.cpp"
+
+
+class OracleParams(C.Structure):
+    _fields_ = [("n_epochs", C.c_int32), ("noise_level", C.c_float),
+                ("negative_sample_rate", C.c_float), ("initial_alpha", C.c_float),
+                ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float)]
+
+
+class OracleStats(C.Structure):
+    _fields_ = [("fired_edges", C.c_int64), ("negatives", C.c_int64),
+                ("active_nodes", C.c_int64)]
+
+
+def build() -> Path:
+    if not LIB.exists() or LIB.stat().st_mtime < SRC.stat().st_mtime:
+        subprocess.run(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp",
+                        "-ffp-contract=off", "-o", str(LIB), str(SRC)], check=True)
+    return LIB
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB))
+        vp, i32, i64, u32, u64, f32 = (C.c_void_p, C.c_int32, C.c_int64, C.c_uint32,
+                                       C.c_uint64, C.c_float)
+        sigs = {
+            "oracle_set_threads": ([C.c_int], None),
+            "oracle_max_threads": ([], C.c_int),
+            "oracle_expf": ([f32], f32),
+            "oracle_philox4x32_10": ([vp, vp, vp], None),
+            "oracle_negative_draw": ([u64, u32, u32, u64, u32], u32),
+            "oracle_init_value": ([u64, u64], f32),
+            "oracle_smooth_knn_dist": ([vp, vp, i64, i32, u64, f32, i32, C.c_int, vp, vp], C.c_int),
+            "oracle_knn_to_coo": ([vp, vp, i64, i32, vp, vp], vp),
+            "oracle_symmetrise": ([vp], vp),
+            "oracle_fuzzy_set": ([vp, vp, i64, i32, f32, C.c_int, vp, vp], vp),
+            "oracle_graph_from_csr": ([vp, vp, vp, i64], vp),
+            "oracle_graph_n": ([vp], i64),
+            "oracle_graph_nnz": ([vp], i64),
+            "oracle_graph_export": ([vp, vp, vp, vp], None),
+            "oracle_graph_free": ([vp], None),
+            "oracle_evoc_embedding": ([vp, vp, vp, i64, i32, C.POINTER(OracleParams), vp, u64,
+                                       i32, i32, vp, vp, vp], C.c_int),
+        }
+        for k, (a, r) in sigs.items():
+            f = getattr(L, k)
+            f.argtypes = a
+            f.restype = r
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def set_threads(n: int) -> None:
+    lib().oracle_set_threads(int(n))
+
+
+def max_threads() -> int:
+    return lib().oracle_max_threads()
+
+
+def expf(x: float) -> float:
+    return lib().oracle_expf(float(x))
+
+
+def expf_array(x: np.ndarray) -> np.ndarray:
+    f = lib().oracle_expf
+    return np.array([f(float(v)) for v in np.asarray(x, dtype=np.float32)], dtype=np.float32)
+
+
+def philox(ctr, key) -> np.ndarray:
+    c = np.ascontiguousarray(ctr, dtype=np.uint32)
+    k = np.ascontiguousarray(key, dtype=np.uint32)
+    o = np.zeros(4, dtype=np.uint32)
+    lib().oracle_philox4x32_10(_p(c), _p(k), _p(o))
+    return o
+
+
+def negative_draw(seed: int, j: int, epoch: int, eidx: int, n: int) -> int:
+    return lib().oracle_negative_draw(seed, j, epoch, eidx, n)
+
+
+def smooth_knn_dist(dists, k_target: int, local_connectivity: float = 1.0, n_iter: int = 64,
+                    row_len=None, libm_exp: bool = False):
+    d = np.ascontiguousarray(dists, dtype=np.float32)
+    n, k = d.shape
+    rl = None if row_len is None else np.ascontiguousarray(row_len, dtype=np.int32)
+    sig = np.zeros(n, dtype=np.float32)
+    rho = np.zeros(n, dtype=np.float32)
+    rc = lib().oracle_smooth_knn_dist(_p(d), _p(rl), n, k, int(k_target), float(local_connectivity),
+                                      int(n_iter), int(libm_exp), _p(sig), _p(rho))
+    if rc != 0:
+        raise ValueError("smooth_knn_dist: empty row with local_connectivity > 0")
+    return sig, rho
+
+
+def _export(g) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    L = lib()
+    n = L.oracle_graph_n(g)
+    nnz = L.oracle_graph_nnz(g)
+    ip = np.zeros(n + 1, dtype=np.int64)
+    ix = np.zeros(nnz, dtype=np.uint32)
+    w = np.zeros(nnz, dtype=np.float32)
+    L.oracle_graph_export(g, _p(ip), _p(ix), _p(w))
+    L.oracle_graph_free(g)
+    return ip, ix, w
+
+
+def knn_to_coo(knn_idx, knn_dist, sigmas, rhos):
+    idx = np.ascontiguousarray(knn_idx, dtype=np.uint32)
+    dist = np.ascontiguousarray(knn_dist, dtype=np.float32)
+    s = np.ascontiguousarray(sigmas, dtype=np.float32)
+    r = np.ascontiguousarray(rhos, dtype=np.float32)
+    g = lib().oracle_knn_to_coo(_p(idx), _p(dist), idx.shape[0], idx.shape[1], _p(s), _p(r))
+    return _export(g)
+
+
+def symmetrise(indptr, indices, weights):
+    ip = np.ascontiguousarray(indptr, dtype=np.int64)
+    ix = np.ascontiguousarray(indices, dtype=np.uint32)
+    w = np.ascontiguousarray(weights, dtype=np.float32)
+    L = lib()
+    g = L.oracle_graph_from_csr(_p(ip), _p(ix), _p(w), len(ip) - 1)
+    s = L.oracle_symmetrise(g)
+    L.oracle_graph_free(g)
+    return _export(s)
+
+
+def fuzzy_set(knn_idx, knn_dist, effective_n_neighbours: float, symmetrise: bool = True,
+              return_sigma_rho: bool = False):
+    idx = np.ascontiguousarray(knn_idx, dtype=np.uint32)
+    dist = np.ascontiguousarray(knn_dist, dtype=np.float32)
+    n, k = idx.shape
+    sig = np.zeros(n, dtype=np.float32)
+    rho = np.zeros(n, dtype=np.float32)
+    g = lib().oracle_fuzzy_set(_p(idx), _p(dist), n, k, float(effective_n_neighbours),
+                               int(bool(symmetrise)), _p(sig), _p(rho))
+    if not g:
+        raise ValueError("build_fuzzy_simplicial_set panics on this input")
+    out = _export(g)
+    return (out, sig, rho) if return_sigma_rho else out
+
+
+def evoc_embedding(indptr, indices, weights, dim: int, n_epochs: int = 50,
+                   noise_level: float = 0.5, negative_sample_rate: float = 1.0,
+                   initial_alpha: float = 0.1, beta1: float = 0.5, beta2: float = 0.9,
+                   eps: float = 1e-7, init=None, seed: int = 42, start_epoch: int = 0,
+                   end_epoch: int | None = None, want_grad: bool = False,
+                   want_stats: bool = False):
+    ip = np.ascontiguousarray(indptr, dtype=np.int64)
+    ix = np.ascontiguousarray(indices, dtype=np.uint32)
+    w = np.ascontiguousarray(weights, dtype=np.float32)
+    n = len(ip) - 1
+    p = OracleParams(n_epochs, noise_level, negative_sample_rate, initial_alpha, beta1, beta2,
+                     eps)
+    ini = None if init is None else np.ascontiguousarray(init, dtype=np.float32)
+    out = np.zeros((n, dim), dtype=np.float32)
+    grad = np.zeros((n, dim), dtype=np.float32) if want_grad else None
+    st = (OracleStats * max(n_epochs, 1))() if want_stats else None
+    end = n_epochs if end_epoch is None else end_epoch
+    rc = lib().oracle_evoc_embedding(_p(ip), _p(ix), _p(w), n, dim, C.byref(p), _p(ini),
+                                     C.c_uint64(seed), start_epoch, end, _p(out), _p(grad),
+                                     st if st is not None else None)
+    if rc != 0:
+        raise ValueError("oracle_evoc_embedding: invalid arguments")
+    res = [out]
+    if want_grad:
+        res.append(grad)
+    if want_stats:
+        s = np.array([(st[t].fired_edges, st[t].negatives, st[t].active_nodes)
+                      for t in range(n_epochs)], dtype=np.int64).reshape(-1, 3)
+        res.append(s)
+    return res[0] if len(res) == 1 else tuple(res)

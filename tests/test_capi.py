@@ -1,0 +1,84 @@
+"""CPU tests of the C ABI library: it builds, loads, and exports every symbol
+declared in include/evoc_gb300.h. No compute call is made without a GPU."""
+import ctypes
+import re
+import subprocess
+from pathlib import Path
+
+import pytest
+
+from conftest import ROOT, ensure_library
+
+
+def declared_functions() -> list[str]:
+    text = (ROOT / "include" / "evoc_gb300.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^EVOC_API\s+(?:const\s+)?\w+\*?\s+\*?(evoc_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declarations_found():
+    names = declared_functions()
+    assert "evoc_fuzzy_set" in names and "evoc_embed" in names and len(names) >= 15
+
+
+def test_library_exports_every_declared_symbol():
+    lib = ensure_library()
+    out = subprocess.run(["nm", "-D", "--defined-only", str(lib)], capture_output=True,
+                         text=True, check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if line.strip()}
+    missing = [n for n in declared_functions() if n not in exported]
+    assert not missing, missing
+
+
+def test_python_binding_lists_every_symbol():
+    import evoc_gb300 as E
+    assert sorted(E.EXPORTED) == declared_functions()
+
+
+def test_load_and_abi_version():
+    ensure_library()
+    import evoc_gb300 as E
+    lib = E.load_library()
+    assert lib.evoc_abi_version() == 1
+
+
+def test_default_params_match_reference():
+    """EvocEmbeddingParams::default, src/graph/mod.rs:52-67."""
+    ensure_library()
+    import evoc_gb300 as E
+    lib = E.load_library()
+    p = E.EmbedParamsC()
+    lib.evoc_embed_params_default(ctypes.byref(p))
+    assert (p.n_epochs, p.noise_level, p.negative_sample_rate, p.initial_alpha) == (50, 0.5, 1.0,
+                                                                                       pytest.approx(0.1))
+    assert p.beta1 == 0.5 and p.beta2 == pytest.approx(0.9) and p.eps == pytest.approx(1e-7)
+    d = E.EvocEmbeddingParams()
+    assert (d.n_epochs, d.noise_level, d.beta1) == (50, 0.5, 0.5)
+
+
+def _has_gpu() -> bool:
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_has_gpu(), reason="a GPU is present")
+def test_context_fails_loudly_without_gpu():
+    ensure_library()
+    import evoc_gb300 as E
+    with pytest.raises(E.EvocError) as ei:
+        E.Context(0)
+    assert ei.value.code in (E.EVOC_ERR_NO_DEVICE, E.EVOC_ERR_CUDA)
+
+
+def test_null_context_arguments_rejected():
+    ensure_library()
+    import evoc_gb300 as E
+    lib = E.load_library()
+    h = ctypes.c_void_p()
+    assert lib.evoc_fuzzy_set(None, None, None, 0, 0, 0.0, 1, ctypes.byref(h)) == E.EVOC_ERR_INVALID_ARGUMENT
+    assert lib.evoc_ctx_create(0, None) != 0
+    assert lib.evoc_last_error(None) is not None
