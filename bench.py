@@ -1,0 +1,348 @@
+#!/usr/bin/env python3
+"""EVoC node-embedding throughput on one GB300.
+
+Workload (default): 2,000,000 f32 points, 768-d, 500 clusters (50 parents x 10
+children at 0.2 rad, Zipf(1.0) sizes, 5% uniform noise), L2-normalised, cosine
+kNN k = 30 computed once on the GPU, embedding dim 8, default parameters
+(50 epochs), random initial embedding. Data are seeded synthetic (no dataset).
+
+A step is one full evoc_embedding run (set-up excluded: the plan is built
+once; the 50-epoch loop, the initialisation and the output write are timed)
+over the device-resident graph. Metric: edge-updates/s = sum over epochs of
+the undirected edges fired (epoch_of_next_sample <= t) / time.
+
+    value       device time of K steps on the library stream (CUDA events)
+    e2e         K steps through the C ABI with pinned host buffers: kNN
+                host->device, fuzzy simplicial set, plan set-up, epochs,
+                embedding device->host (wall clock, synchronised)
+    roofline    k_epoch (the dominant kernel): algorithmic HBM bytes per
+                launch / per-launch device time from CUDA events
+    cpu_baseline  the CPU oracle (C++ restatement of the reference's path)
+                on a bounded sample of epochs of the same graph
+
+--impl reference times the CPU oracle alone on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "evoc-rs_gb300"
+sys.path.insert(0, str(PKG))
+sys.path.insert(0, str(ROOT / "oracle"))
+
+METRIC = "edge-updates/s at 2M pts (EVoC node embedding, 50 epochs)"
+UNIT = "edge-updates/s"
+WORKLOADS = {
+    "hierarchical_2m": dict(n=2_000_000, d=768, k=30, dim=8, seed=2),
+    "anisotropic_200k": dict(n=200_000, d=512, k=15, dim=8, seed=1),
+    "blobs_10k": dict(n=10_000, d=384, k=15, dim=4, seed=42),
+}
+
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "src": "measured"}
+    return {"hbm_gbs": 6800.0, "src": "fallback"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled while the GPU works."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int = 0, interval_ms: int = 50):
+        self.device, self.interval = device, interval_ms
+        self.rows: list[list[str]] = []
+        self.proc = None
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", str(self.interval)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.thread.join(timeout=5)
+
+    def summary(self) -> dict:
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) >= 9
+                          for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(sm)}
+
+
+def make_workload(name: str, n_override: int | None):
+    """Points and cosine kNN graph on the GPU (untimed input preparation)."""
+    import torch
+    import workloads as W
+    cfg = dict(WORKLOADS[name])
+    if n_override:
+        cfg["n"] = n_override
+    n, d, k, seed = cfg["n"], cfg["d"], cfg["k"], cfg["seed"]
+    t0 = time.time()
+    if name == "hierarchical_2m":
+        x, _, parent = W.hierarchical_torch(n, d, 50, 10, seed)
+        groups = W.hierarchical_groups(parent)
+    elif name == "anisotropic_200k":
+        x, _ = W.anisotropic_torch(n, d, 100, seed)
+        groups = None
+    else:
+        x, _ = W.blobs_sphere_torch(n, d, 20, 0.15, seed)
+        groups = None
+    idx, dist = W.knn_torch(x, k, groups)
+    del x
+    assert int(idx.min()) >= 0
+    idx32 = idx.to(torch.int32).contiguous()  # uint32 bit pattern (n < 2^31)
+    dist = dist.contiguous()
+    torch.cuda.synchronize()
+    cfg["prep_s"] = round(time.time() - t0, 1)
+    return cfg, idx32, dist
+
+
+def algorithmic_hbm_bytes(n: int, n_inc: int, dimp: int, P: int, stats: np.ndarray) -> np.ndarray:
+    """Per-epoch bytes k_epoch must move to/from HBM (the partner-row gathers
+    are served by L2 and counted separately): incidence offsets 8(n+1),
+    fire + negative-count bit planes (1+P) n_inc/8, partner ids 4 per fired
+    directed entry (2 F_t), own row read + next row write 2*4*dimp*n, Adam
+    moments read + write 4*4*dimp*A_t."""
+    F, _, A = stats[:, 0], stats[:, 1], stats[:, 2]
+    row = 4 * dimp
+    return (8 * (n + 1) + (1 + P) * n_inc / 8 + 4 * 2 * F + 2 * row * n + 4 * row * A).astype(np.float64)
+
+
+def l2_gather_bytes(dimp: int, stats: np.ndarray) -> np.ndarray:
+    return (4 * dimp * (2 * stats[:, 0] + stats[:, 1])).astype(np.float64)
+
+
+def cpu_epochs_sample(ip, ix, w, dim, seed, stats, t0: int, n_ep: int, max_seconds: float):
+    """Oracle edge-updates/s over epochs [t0, t0 + n_ep) of the same run."""
+    import oracle as O
+    cores = O.max_threads()
+    _, st, secs = O.evoc_embedding(ip, ix, w, dim, seed=seed, start_epoch=t0,
+                                   end_epoch=t0 + n_ep, want_stats=True, want_times=True)
+    sel = slice(t0, t0 + n_ep)
+    fired = float(st[sel, 0].sum())
+    tsec = float(secs[sel].sum())
+    return fired / tsec, cores, tsec
+
+
+def run_ours(args) -> dict:
+    import torch
+    import evoc_gb300 as E
+    torch.cuda.init()
+    cfg, idx32, dist = make_workload(args.workload, args.n)
+    n, k, dim = cfg["n"], cfg["k"], cfg["dim"]
+    params = E.EvocEmbeddingParams()
+    ctx = E.Context(0)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    # fuzzy simplicial set from the device-resident kNN graph
+    torch.cuda.synchronize()
+    t = time.time()
+    graph = ctx.fuzzy_set_device(idx32.data_ptr(), dist.data_ptr(), n, k, float(k), True)
+    fuzzy_s = time.time() - t
+    plan = ctx.plan(graph, dim, params, seed=cfg["seed"])
+    stats = plan.stats()
+    n_epochs = params.n_epochs
+    fired_per_step = float(stats[:, 0].sum())
+    out = torch.empty(n, dim, dtype=torch.float32, device="cuda")
+
+    for _ in range(args.warmup):
+        plan.enqueue_device(None, out.data_ptr())
+    torch.cuda.synchronize()
+
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler() as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            plan.enqueue_device(None, out.data_ptr())
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms_total = ev0.elapsed_time(ev1)
+
+        # end to end through the C ABI with pinned host buffers
+        idx_h = torch.empty(n, k, dtype=torch.int32, pin_memory=True)
+        dist_h = torch.empty(n, k, dtype=torch.float32, pin_memory=True)
+        idx_h.copy_(idx32)
+        dist_h.copy_(dist)
+        out_h = torch.empty(n, dim, dtype=torch.float32, pin_memory=True)
+        idx_np = idx_h.numpy().view(np.uint32)
+        dist_np = dist_h.numpy()
+        out_np = out_h.numpy()
+        e2e_steps = max(1, min(args.steps, args.e2e_steps))
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(e2e_steps):
+            g = ctx.fuzzy_set(idx_np, dist_np, float(k), True)
+            ctx.embed(g, dim, params, seed=cfg["seed"], out=out_np)
+            g.free()
+        torch.cuda.synchronize()
+        e2e_s = (time.perf_counter() - t) / e2e_steps
+    ms_step = ms_total / args.steps
+
+    # dominant kernel: per-launch device times of the same epoch loop
+    epoch_ms = plan.profile_epochs(None, out.data_ptr())
+    dimp = 4 if dim <= 4 else (8 if dim <= 8 else 16)
+    info = plan.info()
+    hbm = algorithmic_hbm_bytes(n, info["n_incidence"], dimp, info["neg_planes"], stats)
+    l2b = l2_gather_bytes(dimp, stats)
+    act = slice(1, n_epochs)  # epoch 0 fires no edge
+    t_launch = float(epoch_ms[act].mean()) / 1e3
+    bytes_launch = float(hbm[act].mean())
+    pk = peaks()
+    achieved = bytes_launch / t_launch / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"],
+                "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": None,
+                "peak_src": pk["src"], "kernel": "k_epoch",
+                "launch_ms": round(t_launch * 1e3, 4), "lanes_per_node": info["lanes"],
+                "l2_gather_gbs": round(float(l2b[act].mean()) / t_launch / 1e9, 1)}
+
+    res = {
+        "metric": METRIC, "value": fired_per_step / (ms_step / 1e3), "unit": UNIT,
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms_step, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, no dataset)",
+        "config": {"workload": args.workload, "n": n, "d": cfg["d"], "k": k, "dim": dim,
+                   "n_epochs": n_epochs, "init": "random", "nnz": int(graph.nnz),
+                   "edge_updates_per_step": int(fired_per_step),
+                   "l2": "inputs larger than L2 (graph + schedule > 1 GB)",
+                   "fuzzy_set_ms": round(fuzzy_s * 1e3, 2), "input_prep_s": cfg["prep_s"]},
+        "e2e": {"value": fired_per_step / e2e_s, "unit": UNIT,
+                "ms_per_step": round(e2e_s * 1e3, 3),
+                "h2d_bytes_per_step": int(n * k * 8), "d2h_bytes_per_step": int(n * dim * 4)},
+        "gpu_launches": int(args.steps * (n_epochs + 2)),
+        "roofline": roofline,
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        ip, ix, w = graph.export()
+        val, cores, tsec = cpu_epochs_sample(ip, ix, w, dim, cfg["seed"], stats,
+                                             args.cpu_t0, args.cpu_epochs, 30.0)
+        res["cpu_baseline"] = {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": f"epochs {args.cpu_t0}..{args.cpu_t0 + args.cpu_epochs - 1}"
+                                         f" of the same 50-epoch run on the same graph "
+                                         f"({tsec:.1f} s of CPU time)"}
+    plan.free()
+    graph.free()
+    ctx.close()
+    return res
+
+
+def run_reference(args) -> dict:
+    """The reference's CPU path (the C++ restatement; Rust is not available)
+    on the same workload: each step is one epoch of the embedding loop
+    (epochs W .. W+K-1 of the 50-epoch schedule, state fast-forwarded)."""
+    import oracle as O
+    cfg, idx32, dist = make_workload(args.workload, args.n)
+    n, k, dim = cfg["n"], cfg["k"], cfg["dim"]
+    idx = idx32.cpu().numpy().view(np.uint32)
+    d = dist.cpu().numpy()
+    del idx32, dist
+    t = time.time()
+    ip, ix, w = O.fuzzy_set(idx, d, float(k), True)
+    fuzzy_s = time.time() - t
+    t0 = max(1, args.cpu_t0 - args.warmup)
+    n_ep = args.warmup + args.steps
+    _, st, secs = O.evoc_embedding(ip, ix, w, dim, seed=cfg["seed"], start_epoch=t0,
+                                   end_epoch=min(50, t0 + n_ep), want_stats=True, want_times=True)
+    timed = slice(t0 + args.warmup, min(50, t0 + n_ep))
+    fired = float(st[timed, 0].sum())
+    tsec = float(secs[timed].sum())
+    cores = O.max_threads()
+    val = fired / tsec
+    steps = timed.stop - timed.start
+    return {
+        "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": 1, "steps": steps,
+        "warmup": args.warmup, "ms_per_step": round(tsec / max(steps, 1) * 1e3, 2),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded, no dataset)", "impl": "reference",
+        "config": {"workload": args.workload, "n": n, "d": cfg["d"], "k": k, "dim": dim,
+                   "n_epochs": 50, "init": "random", "cpu_fuzzy_set_s": round(fuzzy_s, 2),
+                   "l2": "inputs larger than L2"},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"epochs {timed.start}..{timed.stop - 1} of the 50-epoch run "
+                                   f"(C++ restatement of the reference's CPU path, {cores} threads)"},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="hierarchical_2m")
+    ap.add_argument("--n", type=int, default=None, help="override the point count")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-t0", type=int, default=25)
+    ap.add_argument("--cpu-epochs", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(run_reference(args)))
+        return
+    if world > 1:
+        # The path has no exchange step: N GPUs run N independent replicas.
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+        res = run_ours(args)
+        t = torch.tensor([res["ms_per_step"]], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        per_step = res["config"]["edge_updates_per_step"]
+        res["ms_per_step"] = float(t.item())
+        res["value"] = world * per_step / (res["ms_per_step"] / 1e3)
+        res["n_gpus"] = world
+        if rank == 0:
+            print(json.dumps(res))
+        dist.destroy_process_group()
+        return
+    print(json.dumps(run_ours(args)))
+
+
+if __name__ == "__main__":
+    main()

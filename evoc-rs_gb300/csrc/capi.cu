@@ -119,6 +119,10 @@ const char* evoc_last_error(const evoc_ctx_t* ctx) {
   return ctx ? ctx->last_error.c_str() : g_thread_error.c_str();
 }
 
+void* evoc_ctx_stream(const evoc_ctx_t* ctx) {
+  return ctx ? (void*)ctx->stream : nullptr;
+}
+
 int evoc_smooth_knn_dist(evoc_ctx_t* ctx, const float* dists,
                          const int32_t* row_len, int64_t n, int32_t k,
                          uint64_t k_target, float local_connectivity,
@@ -306,6 +310,34 @@ int evoc_plan_run_device(evoc_plan_t* plan, const float* d_init, float* d_out) {
   evoc::plan_run_device(plan, d_init, d_out);
   EVOC_CUDA(cudaStreamSynchronize(ctx->stream));
   EVOC_API_END(ctx)
+}
+
+int evoc_plan_enqueue_device(evoc_plan_t* plan, const float* d_init,
+                             float* d_out) {
+  evoc_ctx* ctx = plan ? evoc::plan_ctx(plan) : nullptr;
+  EVOC_API_BEGIN
+  if (!plan || !d_out) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL argument");
+  use_device(ctx);
+  evoc::plan_run_device(plan, d_init, d_out);
+  EVOC_API_END(ctx)
+}
+
+int evoc_plan_profile_epochs(evoc_plan_t* plan, const float* d_init,
+                             float* d_out, float* epoch_ms) {
+  evoc_ctx* ctx = plan ? evoc::plan_ctx(plan) : nullptr;
+  EVOC_API_BEGIN
+  if (!plan || !d_out || !epoch_ms)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL argument");
+  use_device(ctx);
+  evoc::plan_profile_epochs(plan, d_init, d_out, epoch_ms);
+  EVOC_API_END(ctx)
+}
+
+int evoc_plan_info(const evoc_plan_t* plan, int64_t* n_edges,
+                   int64_t* n_incidence, int32_t* neg_planes, int32_t* lanes) {
+  if (!plan) return EVOC_ERR_INVALID_ARGUMENT;
+  evoc::plan_info(plan, n_edges, n_incidence, neg_planes, lanes);
+  return EVOC_OK;
 }
 
 int evoc_plan_stats(const evoc_plan_t* plan, evoc_epoch_stats_t* stats) {

@@ -292,7 +292,7 @@ __global__ void k_schedule_scan(const float* __restrict__ inc_ps,
   s.init(valid ? inc_ps[p] : 3.0e38f, neg_factor, valid && inc_up[p]);
   unsigned long long mx = 0;
   for (int32_t t = 0; t < n_epochs; ++t) {
-    uint64_t nn;
+    uint64_t nn = 0;
     const bool f = valid && s.step((float)t, &nn);
     if (nn > mx) mx = nn;
     if (stats) {
@@ -335,7 +335,7 @@ __global__ void k_schedule_write(const float* __restrict__ inc_ps,
   s.init(valid ? inc_ps[p] : 3.0e38f, neg_factor, valid && inc_up[p]);
   const bool lane0 = (threadIdx.x & 31) == 0;
   for (int32_t t = 0; t < n_epochs; ++t) {
-    uint64_t nn;
+    uint64_t nn = 0;
     const bool f = valid && s.step((float)t, &nn);
     const uint32_t fw = __ballot_sync(0xffffffffu, f);
     uint32_t* base = planes + (size_t)t * (1 + P) * W + word;
@@ -665,6 +665,13 @@ void add_counts(const int32_t* a, const int32_t* b, int32_t* out, int64_t n,
                 cudaStream_t s);
 
 evoc_ctx* plan_ctx(const evoc_plan* p) { return p->ctx; }
+void plan_info(const evoc_plan* p, int64_t* n_edges, int64_t* n_inc,
+               int32_t* planes, int32_t* lanes) {
+  if (n_edges) *n_edges = p->n_edges;
+  if (n_inc) *n_inc = p->n_inc;
+  if (planes) *planes = p->P;
+  if (lanes) *lanes = p->lanes;
+}
 int64_t plan_n(const evoc_plan* p) { return p->n; }
 int32_t plan_n_epochs(const evoc_plan* p) { return p->params.n_epochs; }
 bool plan_has_edges(const evoc_plan* p) { return p->has_edges; }
@@ -965,6 +972,44 @@ void plan_run_device(evoc_plan* pl, const float* d_init, float* d_out) {
   const float* fin = (pl->has_edges && (ne & 1)) ? pl->e1.get() : pl->e0.get();
   k_unpad<<<blocks_for(n * pl->dim), 256, 0, s>>>(fin, d_out, n, pl->dim, pl->dimp);
   EVOC_CHECK_LAUNCH();
+}
+
+void plan_profile_epochs(evoc_plan* pl, const float* d_init, float* d_out,
+                         float* epoch_ms) {
+  cudaStream_t s = pl->ctx->stream;
+  const int64_t n = pl->n;
+  const int32_t ne = pl->params.n_epochs;
+  for (int32_t t = 0; t < ne; ++t) epoch_ms[t] = 0.0f;
+  if (n == 0) return;
+  load_init(pl, d_init, s);
+  const float* fin = pl->e0.get();
+  if (pl->has_edges && ne > 0) {
+    EVOC_CUDA(cudaMemsetAsync(pl->m.get(), 0, pl->m.bytes(), s));
+    EVOC_CUDA(cudaMemsetAsync(pl->v.get(), 0, pl->v.bytes(), s));
+    std::vector<cudaEvent_t> ev(ne + 1, nullptr);
+    try {
+      for (auto& e : ev) EVOC_CUDA(cudaEventCreate(&e));
+      EVOC_CUDA(cudaEventRecord(ev[0], s));
+      for (int32_t t = 0; t < ne; ++t) {
+        const float* cur = (t & 1) ? pl->e1.get() : pl->e0.get();
+        float* nxt = (t & 1) ? pl->e0.get() : pl->e1.get();
+        launch_epoch(pl, t, cur, nxt, nullptr, s);
+        EVOC_CUDA(cudaEventRecord(ev[t + 1], s));
+        fin = nxt;
+      }
+      EVOC_CUDA(cudaEventSynchronize(ev[ne]));
+      for (int32_t t = 0; t < ne; ++t)
+        EVOC_CUDA(cudaEventElapsedTime(&epoch_ms[t], ev[t], ev[t + 1]));
+    } catch (...) {
+      for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
+      throw;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+  }
+  k_unpad<<<blocks_for(n * pl->dim), 256, 0, s>>>(fin, d_out, n, pl->dim, pl->dimp);
+  EVOC_CHECK_LAUNCH();
+  EVOC_CUDA(cudaStreamSynchronize(s));
 }
 
 void plan_debug_run(evoc_plan* pl, const float* h_init, int32_t start_epoch,

@@ -155,11 +155,15 @@ namespace evoc {
 evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
                        int32_t dim, const evoc_embed_params_t& params);
 void plan_run_device(evoc_plan* plan, const float* d_init, float* d_out);
+void plan_profile_epochs(evoc_plan* plan, const float* d_init, float* d_out,
+                         float* epoch_ms);
 void plan_debug_run(evoc_plan* plan, const float* h_init, int32_t start_epoch,
                     int32_t end_epoch, float* h_out, float* h_grad);
 void plan_stats(const evoc_plan* plan, evoc_epoch_stats_t* stats);
 void plan_free(evoc_plan* plan);
 evoc_ctx* plan_ctx(const evoc_plan* plan);
+void plan_info(const evoc_plan* plan, int64_t* n_edges, int64_t* n_inc,
+               int32_t* planes, int32_t* lanes);
 int64_t plan_n(const evoc_plan* plan);
 int32_t plan_n_epochs(const evoc_plan* plan);
 bool plan_has_edges(const evoc_plan* plan);

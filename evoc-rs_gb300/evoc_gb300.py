@@ -37,10 +37,11 @@ KNN_PAD = 0xFFFFFFFF
 # Every symbol declared in include/evoc_gb300.h.
 EXPORTED = [
     "evoc_abi_version", "evoc_embed_params_default", "evoc_ctx_create",
-    "evoc_ctx_destroy", "evoc_last_error", "evoc_smooth_knn_dist",
+    "evoc_ctx_destroy", "evoc_last_error", "evoc_ctx_stream", "evoc_smooth_knn_dist",
     "evoc_fuzzy_set", "evoc_fuzzy_set_device", "evoc_graph_from_csr",
     "evoc_graph_info", "evoc_graph_export", "evoc_graph_free", "evoc_embed",
-    "evoc_plan_create", "evoc_plan_run_device", "evoc_plan_stats",
+    "evoc_plan_create", "evoc_plan_run_device", "evoc_plan_enqueue_device",
+    "evoc_plan_profile_epochs", "evoc_plan_info", "evoc_plan_stats",
     "evoc_plan_debug_run", "evoc_plan_free", "evoc_embed_batched",
 ]
 
@@ -106,6 +107,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "evoc_ctx_create": ([C.c_int, pp], C.c_int),
         "evoc_ctx_destroy": ([vp], None),
         "evoc_last_error": ([vp], C.c_char_p),
+        "evoc_ctx_stream": ([vp], C.c_void_p),
         "evoc_smooth_knn_dist": ([vp, vp, vp, i64, i32, u64, f32, i32, vp, vp], C.c_int),
         "evoc_fuzzy_set": ([vp, vp, vp, i64, i32, f32, C.c_int, pp], C.c_int),
         "evoc_fuzzy_set_device": ([vp, vp, vp, i64, i32, f32, C.c_int, vp, vp, pp], C.c_int),
@@ -116,6 +118,10 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "evoc_embed": ([vp, vp, i32, C.POINTER(EmbedParamsC), vp, u64, i32, vp], C.c_int),
         "evoc_plan_create": ([vp, vp, i32, C.POINTER(EmbedParamsC), u64, pp], C.c_int),
         "evoc_plan_run_device": ([vp, vp, vp], C.c_int),
+        "evoc_plan_enqueue_device": ([vp, vp, vp], C.c_int),
+        "evoc_plan_profile_epochs": ([vp, vp, vp, vp], C.c_int),
+        "evoc_plan_info": ([vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i32),
+                            C.POINTER(i32)], C.c_int),
         "evoc_plan_stats": ([vp, C.POINTER(EpochStatsC)], C.c_int),
         "evoc_plan_debug_run": ([vp, vp, i32, i32, vp, vp], C.c_int),
         "evoc_plan_free": ([vp], None),
@@ -199,6 +205,25 @@ class Plan:
         self._ctx._check(self._ctx.lib.evoc_plan_run_device(
             self.handle, C.c_void_p(d_init) if d_init else None, C.c_void_p(d_out)))
 
+    def enqueue_device(self, d_init: int | None, d_out: int) -> None:
+        """Enqueue the epoch loop on the context stream without waiting."""
+        self._ctx._check(self._ctx.lib.evoc_plan_enqueue_device(
+            self.handle, C.c_void_p(d_init) if d_init else None, C.c_void_p(d_out)))
+
+    def profile_epochs(self, d_init: int | None, d_out: int) -> np.ndarray:
+        """Device milliseconds of each epoch launch (separate launches, events between)."""
+        ms = np.zeros(max(self.n_epochs, 1), dtype=np.float32)
+        self._ctx._check(self._ctx.lib.evoc_plan_profile_epochs(
+            self.handle, C.c_void_p(d_init) if d_init else None, C.c_void_p(d_out), _ptr(ms)))
+        return ms[: self.n_epochs]
+
+    def info(self) -> dict:
+        e, i, p, l = C.c_int64(), C.c_int64(), C.c_int32(), C.c_int32()
+        self._ctx._check(self._ctx.lib.evoc_plan_info(self.handle, C.byref(e), C.byref(i),
+                                                      C.byref(p), C.byref(l)))
+        return {"n_edges": e.value, "n_incidence": i.value, "neg_planes": p.value,
+                "lanes": l.value}
+
     def stats(self) -> np.ndarray:
         arr = (EpochStatsC * max(self.n_epochs, 1))()
         self._ctx._check(self._ctx.lib.evoc_plan_stats(self.handle, arr))
@@ -238,6 +263,11 @@ class Context:
         if rc != EVOC_OK:
             raise EvocError(rc, self.lib.evoc_last_error(None).decode())
         self.handle = h
+
+    @property
+    def stream(self) -> int:
+        """The context's cudaStream_t as an integer handle."""
+        return self.lib.evoc_ctx_stream(self.handle) or 0
 
     def _check(self, rc: int) -> None:
         if rc != EVOC_OK:
@@ -310,10 +340,14 @@ class Context:
 
     # ---- embedding ------------------------------------------------------
     def embed(self, graph: Graph, dim: int, params: EvocEmbeddingParams | None = None,
-              init=None, seed: int = 42, verbose: int = 0) -> np.ndarray:
+              init=None, seed: int = 42, verbose: int = 0,
+              out: np.ndarray | None = None) -> np.ndarray:
         p = (params or EvocEmbeddingParams()).to_c()
         n = graph.n
-        out = np.zeros((n, dim), dtype=np.float32)
+        if out is None:
+            out = np.zeros((n, dim), dtype=np.float32)
+        elif out.shape != (n, dim) or out.dtype != np.float32 or not out.flags.c_contiguous:
+            raise EvocError(EVOC_ERR_INVALID_ARGUMENT, "out must be a contiguous f32 n x dim array")
         ini = None if init is None else _f32(init)
         if ini is not None and ini.shape != (n, dim):
             raise EvocError(EVOC_ERR_INVALID_ARGUMENT, "init must be n x dim")

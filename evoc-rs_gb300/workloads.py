@@ -118,7 +118,8 @@ def anisotropic_torch(n: int, d: int, n_clusters: int, seed: int, noise_frac: fl
 def hierarchical_torch(n: int, d: int, n_parents: int, n_children: int, seed: int,
                        angle: float = 0.2, spread: float = 0.015, noise_frac: float = 0.05,
                        zipf: float = 1.0, device="cuda"):
-    """Children at angle `angle` from their parent; isotropic spread per coordinate."""
+    """Children at angle `angle` from their parent; isotropic spread per
+    coordinate. Returns (points, child label, parent label); noise is -1."""
     torch = _torch()
     rng = np.random.default_rng(seed)
     g = torch.Generator(device=device).manual_seed(seed)
@@ -141,43 +142,68 @@ def hierarchical_torch(n: int, d: int, n_parents: int, n_children: int, seed: in
     perm = torch.randperm(n, generator=g, device=device)
     x = x[perm]
     x = x / x.norm(dim=1, keepdim=True)
-    return x, lab[perm]
+    lab = lab[perm]
+    parent = torch.where(lab >= 0, lab // n_children, lab)
+    return x, lab, parent
 
 
-def knn_torch(x, k: int, chunk: int = 8192, candidates=None):
-    """Exact cosine kNN on the GPU: bf16 matmul screening of k + 16 candidates
-    per query, re-ranked with f32 distances. Returns (idx uint32 as int64
-    tensor, dist float32) with the query itself removed.
+def knn_torch(x, k: int, groups=None, max_sim_elems: int = 1 << 31):
+    """Cosine kNN on the GPU: a bf16 matmul screens k + 17 candidates per
+    query, which are re-ranked with f32 distances (ties by index). Returns
+    (idx int64, dist float32), each n x k, the query itself removed.
 
-    `candidates`, if given, is a list of index tensors; each query group is
-    searched only within its candidate set (used for the 2M-point workload,
-    whose clusters are far apart)."""
+    `groups` is a list of (query_idx, key_idx) index tensors: each group's
+    queries are searched among its keys only (None: every point against every
+    point). The 2M-point workload searches each parent cluster within itself
+    and the noise points against all points; its parents are nearly orthogonal
+    on the sphere, so this equals the exact kNN."""
     torch = _torch()
     n = x.shape[0]
     dev = x.device
-    out_i = torch.empty(n, k, dtype=torch.int64, device=dev)
-    out_d = torch.empty(n, k, dtype=torch.float32, device=dev)
-    groups = candidates if candidates is not None else [torch.arange(n, device=dev)]
-    extra = 16
-    for grp in groups:
-        xs = x[grp]
-        xb = xs.to(torch.bfloat16)
-        m = grp.numel()
-        kk = min(k + 1 + extra, m)
-        for a in range(0, m, chunk):
-            b = min(m, a + chunk)
-            sim = xb[a:b] @ xb.T
-            cand = torch.topk(sim, kk, dim=1).indices
-            exact = (xs[a:b, None, :] * xs[cand]).sum(-1)
-            rows = torch.arange(a, b, device=dev)
-            exact = torch.where(cand == rows[:, None], torch.full_like(exact, -4.0), exact)
-            # stable re-rank: by similarity, then by index
-            order = torch.argsort(cand, dim=1)
-            cand = torch.gather(cand, 1, order)
+    out_i = torch.full((n, k), -1, dtype=torch.int64, device=dev)
+    out_d = torch.zeros(n, k, dtype=torch.float32, device=dev)
+    if groups is None:
+        a = torch.arange(n, device=dev)
+        groups = [(a, a)]
+    xb_all = x.to(torch.bfloat16)
+    for q_idx, key_idx in groups:
+        m = key_idx.numel()
+        if q_idx.numel() == 0 or m == 0:
+            continue
+        kb = xb_all[key_idx]
+        kk = min(k + 17, m)
+        chunk = int(max(128, min(8192, max_sim_elems // max(m, 1))))
+        for a in range(0, q_idx.numel(), chunk):
+            qi = q_idx[a:a + chunk]
+            sim = xb_all[qi] @ kb.T
+            cand = torch.topk(sim, kk, dim=1).indices          # local key positions
+            del sim
+            gk = key_idx[cand]                                  # global key ids
+            exact = (x[qi][:, None, :] * x[gk]).sum(-1)
+            exact = torch.where(gk == qi[:, None], torch.full_like(exact, -4.0), exact)
+            order = torch.argsort(gk, dim=1)                    # ties broken by index
+            gk = torch.gather(gk, 1, order)
             exact = torch.gather(exact, 1, order)
             top = torch.sort(exact, dim=1, descending=True, stable=True)
             sel = top.indices[:, :k]
-            ci = torch.gather(cand, 1, sel)
-            out_i[grp[a:b]] = grp[ci]
-            out_d[grp[a:b]] = (1.0 - top.values[:, :k]).clamp_min(0.0)
+            out_i[qi] = torch.gather(gk, 1, sel)
+            out_d[qi] = (1.0 - top.values[:, :k]).clamp_min(0.0)
     return out_i, out_d
+
+
+def hierarchical_groups(parent):
+    """(query, key) groups for knn_torch: one per parent cluster, plus the
+    noise points (parent -1) against all points."""
+    torch = _torch()
+    dev = parent.device
+    allidx = torch.arange(parent.numel(), device=dev)
+    order = torch.argsort(parent, stable=True)
+    ps = parent[order]
+    uniq, counts = torch.unique_consecutive(ps, return_counts=True)
+    groups = []
+    start = 0
+    for u, c in zip(uniq.tolist(), counts.tolist()):
+        idx = order[start:start + c]
+        start += c
+        groups.append((idx, allidx) if u < 0 else (idx, idx))
+    return groups

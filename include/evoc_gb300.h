@@ -108,6 +108,10 @@ EVOC_API void evoc_ctx_destroy(evoc_ctx_t* ctx);
  * message of the last failed evoc_ctx_create on this thread is returned. */
 EVOC_API const char* evoc_last_error(const evoc_ctx_t* ctx);
 
+/* The context's cudaStream_t (as void*), for callers that enqueue their own
+ * work or events around the library's (no counterpart). */
+EVOC_API void* evoc_ctx_stream(const evoc_ctx_t* ctx);
+
 /* ---- fuzzy simplicial set ------------------------------------------------ */
 
 /* smooth_knn_dist (src/graph/fuzzy_graph.rs:33-98) on host arrays.
@@ -175,6 +179,26 @@ EVOC_API int evoc_plan_create(evoc_ctx_t* ctx, const evoc_graph_t* g, int32_t di
 /* Run the epoch loop from d_init (device n*dim, or NULL for the random
  * initialisation) and write d_out (device n*dim). d_init may equal d_out. */
 EVOC_API int evoc_plan_run_device(evoc_plan_t* plan, const float* d_init, float* d_out);
+
+/* As evoc_plan_run_device but only enqueues the work on the context's stream
+ * and returns without waiting (no counterpart; for callers that overlap or
+ * time the loop with their own events on evoc_ctx_stream). */
+EVOC_API int evoc_plan_enqueue_device(evoc_plan_t* plan, const float* d_init,
+                                      float* d_out);
+
+/* Runs the epoch loop like evoc_plan_run_device, launching each epoch
+ * separately with CUDA events between launches, and writes the device time of
+ * every epoch launch in milliseconds to epoch_ms[params.n_epochs]
+ * (measurement hook, no counterpart). */
+EVOC_API int evoc_plan_profile_epochs(evoc_plan_t* plan, const float* d_init,
+                                      float* d_out, float* epoch_ms);
+
+/* Layout facts of a plan (any pointer may be NULL): undirected edges,
+ * per-node incidence entries (2 per edge), negative-count bit planes per
+ * epoch, and lanes per node used by the epoch kernel (no counterpart). */
+EVOC_API int evoc_plan_info(const evoc_plan_t* plan, int64_t* n_edges,
+                            int64_t* n_incidence, int32_t* neg_planes,
+                            int32_t* lanes);
 
 /* Per-epoch work counts (stats[params.n_epochs]). */
 EVOC_API int evoc_plan_stats(const evoc_plan_t* plan, evoc_epoch_stats_t* stats);

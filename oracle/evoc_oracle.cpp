@@ -455,14 +455,15 @@ void oracle_graph_free(OracleGraph* g) { delete g; }
 // Epochs [0, start_epoch) only advance the schedule (embedding.rs:274-286);
 // epochs [start_epoch, end_epoch) run in full. grad_out (optional) receives
 // the gradient of the last epoch run. stats (optional, n_epochs entries)
-// receives per-epoch counts for the epochs run in full.
+// receives per-epoch counts for the epochs run in full, epoch_seconds
+// (optional, n_epochs entries) the wall time of each epoch run in full.
 // Returns 0, or -1 for invalid arguments.
 int oracle_evoc_embedding(const int64_t* indptr, const uint32_t* indices,
                           const float* weights, int64_t n, int32_t dim,
                           const OracleEmbedParams* params, const float* init,
                           uint64_t seed, int32_t start_epoch,
                           int32_t end_epoch, float* out, float* grad_out,
-                          OracleEpochStats* stats) {
+                          OracleEpochStats* stats, double* epoch_seconds) {
   if (n == 0) return 0;  // :61-64
   if (dim <= 0 || !params) return -1;
   const int64_t D = dim;
@@ -559,6 +560,9 @@ int oracle_evoc_embedding(const int64_t* indptr, const uint32_t* indices,
   for (int32_t epoch = 0; epoch < e0; ++epoch) schedule_update(epoch);
 
   for (int32_t epoch = e0; epoch < e1; ++epoch) {
+#ifdef _OPENMP
+    const double t_start = omp_get_wtime();
+#endif
     const float lr = params->initial_alpha * (1.0f - (float)epoch / n_epochs_f);
     const float epoch_t = (float)epoch;
     const float ads = ad_scale[epoch], epc = epsc[epoch], gam = gamma[epoch];
@@ -659,6 +663,11 @@ int oracle_evoc_embedding(const int64_t* indptr, const uint32_t* indices,
 
     schedule_update(epoch);  // :274-286
     if (stats) stats[epoch] = {fired_edges, negs, act};
+#ifdef _OPENMP
+    if (epoch_seconds) epoch_seconds[epoch] = omp_get_wtime() - t_start;
+#else
+    if (epoch_seconds) epoch_seconds[epoch] = 0.0;
+#endif
   }
   std::memcpy(out, embd.data(), n * D * sizeof(float));
   return 0;

@@ -61,7 +61,7 @@ def lib() -> C.CDLL:
             "oracle_graph_export": ([vp, vp, vp, vp], None),
             "oracle_graph_free": ([vp], None),
             "oracle_evoc_embedding": ([vp, vp, vp, i64, i32, C.POINTER(OracleParams), vp, u64,
-                                       i32, i32, vp, vp, vp], C.c_int),
+                                       i32, i32, vp, vp, vp, vp], C.c_int),
         }
         for k, (a, r) in sigs.items():
             f = getattr(L, k)
@@ -170,7 +170,7 @@ def evoc_embedding(indptr, indices, weights, dim: int, n_epochs: int = 50,
                    initial_alpha: float = 0.1, beta1: float = 0.5, beta2: float = 0.9,
                    eps: float = 1e-7, init=None, seed: int = 42, start_epoch: int = 0,
                    end_epoch: int | None = None, want_grad: bool = False,
-                   want_stats: bool = False):
+                   want_stats: bool = False, want_times: bool = False):
     ip = np.ascontiguousarray(indptr, dtype=np.int64)
     ix = np.ascontiguousarray(indices, dtype=np.uint32)
     w = np.ascontiguousarray(weights, dtype=np.float32)
@@ -181,10 +181,11 @@ def evoc_embedding(indptr, indices, weights, dim: int, n_epochs: int = 50,
     out = np.zeros((n, dim), dtype=np.float32)
     grad = np.zeros((n, dim), dtype=np.float32) if want_grad else None
     st = (OracleStats * max(n_epochs, 1))() if want_stats else None
+    times = np.zeros(max(n_epochs, 1), dtype=np.float64) if want_times else None
     end = n_epochs if end_epoch is None else end_epoch
     rc = lib().oracle_evoc_embedding(_p(ip), _p(ix), _p(w), n, dim, C.byref(p), _p(ini),
                                      C.c_uint64(seed), start_epoch, end, _p(out), _p(grad),
-                                     st if st is not None else None)
+                                     st if st is not None else None, _p(times))
     if rc != 0:
         raise ValueError("oracle_evoc_embedding: invalid arguments")
     res = [out]
@@ -194,4 +195,6 @@ def evoc_embedding(indptr, indices, weights, dim: int, n_epochs: int = 50,
         s = np.array([(st[t].fired_edges, st[t].negatives, st[t].active_nodes)
                       for t in range(n_epochs)], dtype=np.int64).reshape(-1, 3)
         res.append(s)
+    if want_times:
+        res.append(times[:n_epochs])
     return res[0] if len(res) == 1 else tuple(res)
