@@ -21,15 +21,15 @@
 //                  an edge evaluate the same f32 recurrence, so they agree.
 // Epoch loop (embedding.rs:178-292), one launch per epoch, captured in a CUDA
 // graph:
-//   k_epoch        G lanes per node (pull-based): each lane takes incidence
-//                  entries q = lane, lane + G, ... of its node, reads the fire
-//                  bit, gathers partner rows (float4) and Philox negatives,
-//                  accumulates into the partial sum of virtual lane q mod 32;
-//                  partials are combined with strides 16..1 (in registers for
-//                  strides >= G, by reduce-scatter shuffles below G); the lane
-//                  that owns a dimension applies Adam (embedding.rs:256-272)
-//                  and writes the next embedding buffer (ping-pong). No float
-//                  atomics; results do not depend on G.
+//   k_epoch        G lanes per node (pull-based): the node's fire words are
+//                  read G at a time and its fired entries compacted (prefix
+//                  sum + __fns), so each lane takes a fired entry, gathers the
+//                  partner row (float4) and the Philox negatives, and adds into
+//                  partial sum (fired rank mod 32) in shared memory; the 32
+//                  partials are combined by a pairwise tree (strides 16..1);
+//                  the lane that owns a dimension applies Adam
+//                  (embedding.rs:256-272) and writes the next embedding buffer
+//                  (ping-pong). No float atomics; results do not depend on G.
 #include "evoc_device.cuh"
 #include "evoc_internal.h"
 
@@ -55,7 +55,7 @@ struct evoc_plan {
   int64_t n = 0;          // nodes over all problems
   int32_t dim = 0;        // n_components
   int32_t dimp = 0;       // padded row width (4, 8 or 16)
-  int32_t lanes = 0;      // lanes per node in k_epoch
+  int32_t lanes = 0;      // warps (32-node tiles) per thread block of k_epoch
   evoc_embed_params_t params{};
   int32_t n_problems = 0;
   std::vector<int64_t> node_base;  // per problem, host
@@ -444,181 +444,299 @@ __device__ __forceinline__ void load_row(const float* __restrict__ p, float (&r)
   }
 }
 
-template <int DIMP, int G>
-__global__ void __launch_bounds__(256) k_epoch(EpochArgs a) {
-  constexpr int VL = 32 / G;
+// ---------------------------------------------------------------------------
+// One epoch, one warp per tile of 32 consecutive nodes.
+//
+// Phase A (lane = node): incidence offsets and the tile's own rows are loaded
+// coalesced into shared memory; running gradients start at +0.
+// Phase B (lane = fired entry): the tile's fire words are read 32 at a time;
+// fired entries (in incidence order, across node boundaries) are handed to
+// lanes 32 at a time by a warp prefix sum + __fns. Each lane gathers its
+// partner row and, for the smaller endpoint, its Philox negatives, and writes
+// one contribution vector per slot (slot 0 = attraction, slot j+1 = negative
+// j; skipped terms are +0) into a CAP-slot buffer. Then the slots of every
+// node are added to its running gradient serially in slot order, one lane per
+// (node, dim) segment: the reference's running sum (embedding.rs:194-248),
+// term for term. An entry whose slots do not fit continues in the next chunk.
+// Phase C (lane = node): Adam (embedding.rs:256-272) and the next embedding.
+// ---------------------------------------------------------------------------
+constexpr int TILE = 32;
+constexpr int CAP = 64;
+
+template <int DIMP>
+struct alignas(16) TileSmem {
+  float rows[TILE][DIMP];       // e_cur rows of the tile's nodes
+  float S[TILE][DIMP + 1];      // running gradients
+  float contrib[CAP][DIMP + 1]; // contribution slots of the current chunk
+  int64_t pbeg[TILE + 1];       // incidence offsets of the tile
+  uint8_t slot_node[CAP];       // tile-local node of each slot
+};
+
+template <int DIMP>
+__global__ void __launch_bounds__(128) k_epoch(EpochArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  const int gl = lane & (G - 1);
-  const int64_t gid = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
-  if (gid >= a.n_total) return;  // groups exit whole
-  const unsigned gmask =
-      (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << (lane & ~(G - 1)));
-  const uint32_t v = (uint32_t)gid;
-  uint32_t nb = 0, np = a.n_total;
-  uint64_t seed = a.seed;
-  if (a.prob_of_node) {
-    const ProbInfo pi = a.prob[a.prob_of_node[v]];
-    nb = pi.node_base;
-    np = pi.n;
-    seed = pi.seed;
+  TileSmem<DIMP>& sm = reinterpret_cast<TileSmem<DIMP>*>(smem_raw)[threadIdx.x >> 5];
+  const int64_t v0 = ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * TILE;
+  if (v0 >= (int64_t)a.n_total) return;  // whole warp
+  const int nt = (int)min((int64_t)TILE, (int64_t)a.n_total - v0);
+  const bool has_node = lane < nt;
+
+  // ---- phase A
+  if (has_node) sm.pbeg[lane] = a.inc_ptr[v0 + lane];
+  if (lane == 0) sm.pbeg[nt] = a.inc_ptr[v0 + nt];
+  {
+    const float4* src = reinterpret_cast<const float4*>(a.e_cur + (size_t)v0 * DIMP);
+    float4* dst = reinterpret_cast<float4*>(&sm.rows[0][0]);
+    for (int i = lane; i < nt * (DIMP / 4); i += 32) dst[i] = __ldg(src + i);
   }
-  const int64_t p0 = a.inc_ptr[v], p1 = a.inc_ptr[v + 1];
-  float ev[DIMP];
-  load_row<DIMP>(a.e_cur + (size_t)v * DIMP, ev);
-  float acc[VL][DIMP];
-#pragma unroll
-  for (int s = 0; s < VL; ++s)
-#pragma unroll
-    for (int d = 0; d < DIMP; ++d) acc[s][d] = 0.0f;
-  bool any = false;
-  int64_t eb = 0;
-  bool eb_loaded = false;
+  for (int i = lane; i < TILE * (DIMP + 1); i += 32) (&sm.S[0][0])[i] = 0.0f;
+  __syncwarp();
+  const int64_t P0 = sm.pbeg[0], P1 = sm.pbeg[nt];
   const float two_noise = fmul(2.0f, a.noise);
   const float gamma4 = fmul(a.gamma, 4.0f);
+  uint32_t touched = 0;
 
-  for (int64_t base = p0; base < p1; base += 32) {
-#pragma unroll
-    for (int s = 0; s < VL; ++s) {
-      const int64_t p = base + s * G + gl;
-      if (p >= p1) continue;
-      const uint32_t word = __ldcs(a.fire + (p >> 5));
-      if (!((word >> (p & 31)) & 1u)) continue;
-      any = true;
-      const uint32_t o = __ldcs(a.inc_other + p);
-      float eo[DIMP];
-      load_row<DIMP>(a.e_cur + (size_t)o * DIMP, eo);
-      float diff[DIMP];
-      float dsq = 0.0f;
-#pragma unroll
-      for (int d = 0; d < DIMP; ++d) {
-        diff[d] = fsub(ev[d], eo[d]);
-        dsq = fadd(dsq, fmul(diff[d], diff[d]));
+  // ---- phase B
+  if (P1 > P0) {
+    const int64_t W0 = P0 >> 5, W1 = (P1 - 1) >> 5;
+    for (int64_t wb = W0; wb <= W1; wb += 32) {
+      const int64_t w = wb + lane;
+      uint32_t word = 0;
+      if (w <= W1) {
+        word = __ldcs(a.fire + w);
+        if (w == W0) word &= FULL << (P0 & 31);
+        if (w == W1) {
+          const int hi = (int)((P1 - 1) & 31);
+          word &= (hi == 31) ? FULL : ((2u << hi) - 1u);
+        }
       }
-      if (dsq >= 1e-8f) {  // embedding.rs:213-221
-        const float dist = fsqrt(dsq);
-        const float coeff = fdiv(fsub(-fmul(two_noise, dist), 2.0f),
-                                 fadd(fsub(fmul(2.0f, dsq), fmul(0.5f, dist)), 1.0f));
+      const int cnt = __popc(word);
+      int incl = cnt;
 #pragma unroll
-        for (int d = 0; d < DIMP; ++d) acc[s][d] = fadd(acc[s][d], fmul(coeff, diff[d]));
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
       }
-      if (o > v) {  // embedding.rs:224-247
-        uint32_t nneg = 0;
-        for (int32_t b = 0; b < a.P; ++b)
-          nneg |= ((__ldcs(a.fire + (size_t)(1 + b) * a.W + (p >> 5)) >> (p & 31)) & 1u) << b;
-        if (nneg) {
-          if (!eb_loaded) {
-            eb = a.eidx_base[v];
-            eb_loaded = true;
+      const int excl = incl - cnt;
+      const int tot = __shfl_sync(FULL, incl, 31);
+      int fi = 0;  // first fired entry (index in this round) of the next chunk
+      int so = 0;  // slots of that entry consumed by earlier chunks
+      while (fi < tot) {
+        const int f = fi + lane;
+        const bool valid = f < tot;
+        int u = 0;  // lane whose word holds fired entry f
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+          const int e_ = __shfl_sync(FULL, excl, u + step);
+          if (e_ <= f) u += step;
+        }
+        const uint32_t wu = __shfl_sync(FULL, word, u);
+        const int eu = __shfl_sync(FULL, excl, u);
+        int64_t p = 0;
+        int node = 0;
+        uint32_t o = 0, nneg = 0;
+        if (valid) {
+          p = ((wb + u) << 5) + (int64_t)__fns(wu, 0u, f - eu + 1);
+          int lo = 0, hi = nt - 1;  // last node whose list starts at or before p
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (sm.pbeg[mid] <= p) lo = mid; else hi = mid - 1;
           }
-          const uint64_t eidx = (uint64_t)(p + eb);
-          for (uint32_t j = 0; j < nneg; ++j) {
-            const uint32_t kk = nb + negative_draw(seed, j, a.epoch, eidx, np);
-            if (kk == v) continue;
-            float ek[DIMP];
-            load_row<DIMP>(a.e_cur + (size_t)kk * DIMP, ek);
-            float dk = 0.0f;
+          node = lo;
+          o = __ldcs(a.inc_other + p);
+          if ((int64_t)o > v0 + node)
+            for (int32_t b = 0; b < a.P; ++b)
+              nneg |= ((__ldcs(a.fire + (size_t)(1 + b) * a.W + (p >> 5)) >> (p & 31)) & 1u) << b;
+        }
+        const int k_first = (lane == 0) ? so : 0;
+        const int cc = valid ? (int)(1 + nneg) - k_first : 0;
+        int cincl = cc;
+#pragma unroll
+        for (int s2 = 1; s2 < 32; s2 <<= 1) {
+          const int y = __shfl_up_sync(FULL, cincl, s2);
+          if (lane >= s2) cincl += y;
+        }
+        const int cexcl = cincl - cc;
+        const int nslots = max(0, min(cincl, CAP) - cexcl);
+        if (nslots > 0) {
+          const uint32_t vg = (uint32_t)(v0 + node);
+          float ev[DIMP];
+#pragma unroll
+          for (int d = 0; d < DIMP; ++d) ev[d] = sm.rows[node][d];
+          uint32_t nb = 0, np = a.n_total;
+          uint64_t seed = a.seed;
+          uint64_t eidx = 0;
+          if (k_first + nslots > 1) {  // negatives in this chunk
+            if (a.prob_of_node) {
+              const ProbInfo pi = a.prob[a.prob_of_node[vg]];
+              nb = pi.node_base;
+              np = pi.n;
+              seed = pi.seed;
+            }
+            eidx = (uint64_t)(p + a.eidx_base[vg]);
+          }
+          for (int t = 0; t < nslots; ++t) {
+            const int k = k_first + t;
+            float* dst = sm.contrib[cexcl + t];
+            sm.slot_node[cexcl + t] = (uint8_t)node;
+            float row[DIMP];
+            bool skip = false;
+            uint32_t src;
+            if (k == 0) {
+              src = o;
+            } else {
+              src = nb + negative_draw(seed, (uint32_t)(k - 1), a.epoch, eidx, np);
+              skip = (src == vg);
+            }
+            if (skip) {
+#pragma unroll
+              for (int d = 0; d < DIMP; ++d) dst[d] = 0.0f;
+              continue;
+            }
+            load_row<DIMP>(a.e_cur + (size_t)src * DIMP, row);
+            float diff[DIMP];
+            float dsq = 0.0f;
 #pragma unroll
             for (int d = 0; d < DIMP; ++d) {
-              const float df = fsub(ev[d], ek[d]);
-              dk = fadd(dk, fmul(df, df));
+              diff[d] = fsub(ev[d], row[d]);
+              dsq = fadd(dsq, fmul(diff[d], diff[d]));
             }
-            if (dk > 0.01f) {
-              const float gc = fdiv(gamma4, fmul(fadd(1.0f, fmul(0.25f, dk)), dk));
+            if (k == 0) {  // attraction, embedding.rs:213-221
+              if (dsq >= 1e-8f) {
+                const float dist = fsqrt(dsq);
+                const float coeff = fdiv(fsub(-fmul(two_noise, dist), 2.0f),
+                                         fadd(fsub(fmul(2.0f, dsq), fmul(0.5f, dist)), 1.0f));
 #pragma unroll
-              for (int d = 0; d < DIMP; ++d) {
-                float c = fmul(gc, fsub(ev[d], ek[d]));
-                c = fmaxf(c, -4.0f);
-                c = fminf(c, 4.0f);
-                acc[s][d] = fadd(acc[s][d], c);
+                for (int d = 0; d < DIMP; ++d) dst[d] = fmul(coeff, diff[d]);
+              } else {
+#pragma unroll
+                for (int d = 0; d < DIMP; ++d) dst[d] = 0.0f;
+              }
+            } else {  // repulsion, embedding.rs:237-245
+              if (dsq > 0.01f) {
+                const float gc = fdiv(gamma4, fmul(fadd(1.0f, fmul(0.25f, dsq)), dsq));
+#pragma unroll
+                for (int d = 0; d < DIMP; ++d) {
+                  float c = fmul(gc, diff[d]);
+                  c = fmaxf(c, -4.0f);
+                  dst[d] = fminf(c, 4.0f);
+                }
+              } else {
+#pragma unroll
+                for (int d = 0; d < DIMP; ++d) dst[d] = 0.0f;
               }
             }
           }
         }
+        touched |= __reduce_or_sync(FULL, valid ? (1u << node) : 0u);
+        const int ndone = __popc(__ballot_sync(FULL, valid && cincl <= CAP));
+        const int used = min(__shfl_sync(FULL, cincl, 31), CAP);
+        const int cex_nd = __shfl_sync(FULL, cexcl, ndone & 31);
+        const int kf_nd = __shfl_sync(FULL, k_first, ndone & 31);
+        __syncwarp();
+        // serial accumulation of slots [0, used), one lane per (node, dim)
+        {
+          const int sa = lane, sb = lane + 32;
+          const bool st_a = sa < used && (sa == 0 || sm.slot_node[sa] != sm.slot_node[sa - 1]);
+          const bool st_b = sb < used && sm.slot_node[sb] != sm.slot_node[sb - 1];
+          const uint32_t ma = __ballot_sync(FULL, st_a), mb = __ballot_sync(FULL, st_b);
+          const int na = __popc(ma), nseg = na + __popc(mb);
+          for (int tsk = lane; tsk < nseg * DIMP; tsk += 32) {
+            const int seg = tsk / DIMP, d = tsk - seg * DIMP;
+            const int start = (seg < na) ? (int)__fns(ma, 0u, seg + 1)
+                                         : 32 + (int)__fns(mb, 0u, seg - na + 1);
+            int end = used;
+            if (seg + 1 < nseg)
+              end = (seg + 1 < na) ? (int)__fns(ma, 0u, seg + 2)
+                                   : 32 + (int)__fns(mb, 0u, seg + 1 - na + 1);
+            const int nd = sm.slot_node[start];
+            float acc = sm.S[nd][d];
+            for (int s2 = start; s2 < end; ++s2) acc = fadd(acc, sm.contrib[s2][d]);
+            sm.S[nd][d] = acc;
+          }
+        }
+        __syncwarp();
+        int next_so = 0;
+        if (ndone < 32 && fi + ndone < tot) next_so = kf_nd + max(0, CAP - cex_nd);
+        fi += ndone;
+        so = next_so;
       }
     }
   }
 
-  // strides 16 .. G: partial sums held by the same lane
+  // ---- phase C
+  if (has_node) {
+    const size_t q = (size_t)(v0 + lane) * DIMP;
+    const bool act = (touched >> lane) & 1u;
+    float e[DIMP], g[DIMP];
 #pragma unroll
-  for (int off = 16; off >= G; off >>= 1) {
-    const int half = off / G;
-#pragma unroll
-    for (int s = 0; s < VL; ++s)
-      if (s < half) {
-#pragma unroll
-        for (int d = 0; d < DIMP; ++d) acc[s][d] = fadd(acc[s][d], acc[s + half][d]);
-      }
-  }
-  // strides G/2 .. 1: reduce-scatter across the group's lanes
-  float c[DIMP];
-#pragma unroll
-  for (int d = 0; d < DIMP; ++d) c[d] = acc[0][d];
-  int width = DIMP;  // values held: dims [d0, d0 + width)
-  int d0 = 0;
-#pragma unroll
-  for (int off = G / 2; off >= 1; off >>= 1) {
-    if (width >= 2) {
-      const bool upper = (gl & off) != 0;
-      const int h = width / 2;
-#pragma unroll
-      for (int i = 0; i < DIMP / 2; ++i) {
-        if (i < h) {
-          const float send = upper ? c[i] : c[i + h];
-          const float keep = upper ? c[i + h] : c[i];
-          const float recv = __shfl_xor_sync(gmask, send, off);
-          c[i] = fadd(keep, recv);
-        }
-      }
-      width = h;
-      if (upper) d0 += h;
-    } else {
-      c[0] = fadd(c[0], __shfl_xor_sync(gmask, c[0], off));
+    for (int d = 0; d < DIMP; ++d) {
+      e[d] = sm.rows[lane][d];
+      g[d] = act ? sm.S[lane][d] : 0.0f;
     }
-  }
-  any = __any_sync(gmask, any);
-  // lanes whose low bits (strides after the last halving) are zero write
-  constexpr int REPL = (G > DIMP) ? (G / DIMP) : 1;
-  if ((gl & (REPL - 1)) != 0) return;
-  const size_t nbase = (size_t)v * DIMP;
+    if (act) {
+      const float4* m4 = reinterpret_cast<const float4*>(a.m + q);
+      const float4* v4 = reinterpret_cast<const float4*>(a.v + q);
+      float mm[DIMP], vv[DIMP];
 #pragma unroll
-  for (int i = 0; i < DIMP; ++i) {
-    if (i >= width) break;
-    const size_t q = nbase + d0 + i;
-    float e = a.e_cur[q];
-    const float g = c[i];
-    if (any) {  // embedding.rs:263-271
-      float mm = __ldcs(a.m + q);
-      float vv = __ldcs(a.v + q);
-      mm = fadd(mm, fmul(a.one_m_b1, fsub(g, mm)));
-      vv = fadd(vv, fmul(a.one_m_b2, fsub(fmul(g, g), vv)));
-      e = fadd(e, fdiv(fmul(a.lr_ad, mm), fadd(fsqrt(vv), a.epsc)));
-      __stcs(a.m + q, mm);
-      __stcs(a.v + q, vv);
+      for (int i = 0; i < DIMP / 4; ++i) {
+        const float4 x = __ldcs(m4 + i), y = __ldcs(v4 + i);
+        mm[4 * i] = x.x; mm[4 * i + 1] = x.y; mm[4 * i + 2] = x.z; mm[4 * i + 3] = x.w;
+        vv[4 * i] = y.x; vv[4 * i + 1] = y.y; vv[4 * i + 2] = y.z; vv[4 * i + 3] = y.w;
+      }
+#pragma unroll
+      for (int d = 0; d < DIMP; ++d) {  // embedding.rs:266-271
+        mm[d] = fadd(mm[d], fmul(a.one_m_b1, fsub(g[d], mm[d])));
+        vv[d] = fadd(vv[d], fmul(a.one_m_b2, fsub(fmul(g[d], g[d]), vv[d])));
+        e[d] = fadd(e[d], fdiv(fmul(a.lr_ad, mm[d]), fadd(fsqrt(vv[d]), a.epsc)));
+      }
+      float4* mo = reinterpret_cast<float4*>(a.m + q);
+      float4* vo = reinterpret_cast<float4*>(a.v + q);
+#pragma unroll
+      for (int i = 0; i < DIMP / 4; ++i) {
+        __stcs(mo + i, make_float4(mm[4 * i], mm[4 * i + 1], mm[4 * i + 2], mm[4 * i + 3]));
+        __stcs(vo + i, make_float4(vv[4 * i], vv[4 * i + 1], vv[4 * i + 2], vv[4 * i + 3]));
+      }
     }
-    a.e_next[q] = e;
-    if (a.grad_out) a.grad_out[q] = any ? g : 0.0f;
+    float4* eo = reinterpret_cast<float4*>(a.e_next + q);
+#pragma unroll
+    for (int i = 0; i < DIMP / 4; ++i)
+      eo[i] = make_float4(e[4 * i], e[4 * i + 1], e[4 * i + 2], e[4 * i + 3]);
+    if (a.grad_out) {
+      float4* go = reinterpret_cast<float4*>(a.grad_out + q);
+#pragma unroll
+      for (int i = 0; i < DIMP / 4; ++i)
+        go[i] = make_float4(g[4 * i], g[4 * i + 1], g[4 * i + 2], g[4 * i + 3]);
+    }
   }
 }
 
 using EpochKernel = void (*)(EpochArgs);
 
-EpochKernel pick_kernel(int dimp, int lanes) {
-#define EVOC_K(D, G) if (dimp == D && lanes == G) return k_epoch<D, G>;
-  EVOC_K(4, 8) EVOC_K(4, 16) EVOC_K(4, 32)
-  EVOC_K(8, 8) EVOC_K(8, 16) EVOC_K(8, 32)
-  EVOC_K(16, 16) EVOC_K(16, 32)
-#undef EVOC_K
+EpochKernel pick_kernel(int dimp) {
+  if (dimp == 4) return k_epoch<4>;
+  if (dimp == 8) return k_epoch<8>;
+  if (dimp == 16) return k_epoch<16>;
   return nullptr;
 }
 
-int default_lanes(int dimp, double avg_inc) {
-  int g = avg_inc <= 24.0 ? 8 : (avg_inc <= 48.0 ? 16 : 32);
-  if (dimp == 16 && g < 16) g = 16;
-  if (const char* env = std::getenv("EVOC_LANES")) {
-    int e = std::atoi(env);
-    if (pick_kernel(dimp, e)) g = e;
+size_t tile_smem(int dimp) {
+  if (dimp == 4) return sizeof(TileSmem<4>);
+  if (dimp == 8) return sizeof(TileSmem<8>);
+  return sizeof(TileSmem<16>);
+}
+
+// Warps (node tiles) per thread block of k_epoch; EVOC_WARPS_PER_BLOCK
+// overrides (1, 2 or 4). Results do not depend on it.
+int default_wpb() {
+  int w = 2;
+  if (const char* env = std::getenv("EVOC_WARPS_PER_BLOCK")) {
+    const int e = std::atoi(env);
+    if (e == 1 || e == 2 || e == 4) w = e;
   }
-  return g;
+  return w;
 }
 
 void launch_epoch(evoc_plan* pl, int32_t t, const float* e_cur, float* e_next,
@@ -646,9 +764,10 @@ void launch_epoch(evoc_plan* pl, int32_t t, const float* e_cur, float* e_next,
   a.epsc = pl->epsc[t];
   a.one_m_b1 = pl->one_m_b1;
   a.one_m_b2 = pl->one_m_b2;
-  EpochKernel k = pick_kernel(pl->dimp, pl->lanes);
-  const int64_t threads = pl->n * pl->lanes;
-  k<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(a);
+  const int wpb = pl->lanes;
+  const int64_t tiles = (pl->n + TILE - 1) / TILE;
+  pick_kernel(pl->dimp)<<<(unsigned)((tiles + wpb - 1) / wpb), 32 * wpb,
+                          wpb * tile_smem(pl->dimp), s>>>(a);
   EVOC_CHECK_LAUNCH();
 }
 
@@ -900,7 +1019,7 @@ evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
 
   pl->m.alloc(n * pl->dimp, s);
   pl->v.alloc(n * pl->dimp, s);
-  pl->lanes = default_lanes(pl->dimp, (double)n_inc / (double)n);
+  pl->lanes = default_wpb();
   EVOC_CUDA(cudaStreamSynchronize(s));
   return pl.release();
 }

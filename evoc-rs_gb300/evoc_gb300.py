@@ -222,7 +222,7 @@ class Plan:
         self._ctx._check(self._ctx.lib.evoc_plan_info(self.handle, C.byref(e), C.byref(i),
                                                       C.byref(p), C.byref(l)))
         return {"n_edges": e.value, "n_incidence": i.value, "neg_planes": p.value,
-                "lanes": l.value}
+                "warps_per_block": l.value}
 
     def stats(self) -> np.ndarray:
         arr = (EpochStatsC * max(self.n_epochs, 1))()

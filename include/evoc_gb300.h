@@ -31,10 +31,10 @@
  *     the edge id, not from rand::SmallRng (embedding.rs:173-175, :231).
  *   - Per-node neighbour order is ascending column, not FxHashMap order
  *     (fuzzy_graph.rs:196-205).
- *   - The per-node gradient is summed in a fixed order (32 virtual lanes, each
- *     summing entries q = lane mod 32 in list order, then a pairwise tree with
- *     strides 16, 8, 4, 2, 1). Results are bit-reproducible and do not depend
- *     on launch configuration.
+ *   - The per-node gradient is summed serially in incidence-list order, each
+ *     fired edge's attraction before its negatives, exactly as the
+ *     reference's loop (embedding.rs:203-248). Results are bit-reproducible
+ *     and do not depend on launch configuration.
  */
 #ifndef EVOC_GB300_H
 #define EVOC_GB300_H
@@ -195,10 +195,11 @@ EVOC_API int evoc_plan_profile_epochs(evoc_plan_t* plan, const float* d_init,
 
 /* Layout facts of a plan (any pointer may be NULL): undirected edges,
  * per-node incidence entries (2 per edge), negative-count bit planes per
- * epoch, and lanes per node used by the epoch kernel (no counterpart). */
+ * epoch, and warps (32-node tiles) per thread block of the epoch kernel
+ * (no counterpart). */
 EVOC_API int evoc_plan_info(const evoc_plan_t* plan, int64_t* n_edges,
                             int64_t* n_incidence, int32_t* neg_planes,
-                            int32_t* lanes);
+                            int32_t* warps_per_block);
 
 /* Per-epoch work counts (stats[params.n_epochs]). */
 EVOC_API int evoc_plan_stats(const evoc_plan_t* plan, evoc_epoch_stats_t* stats);

@@ -34,11 +34,9 @@
 //      k = (u32 * n) >> 32.
 //   4. The squared distance (ann-search-rs 0.5.2 euclidean_simd, called at
 //      embedding.rs:210,237) is the serial left fold sum_d (a_d - b_d)^2.
-//   5. The per-node gradient (embedding.rs:203-248) is summed in a fixed
-//      order: entry q of the node's incidence list goes to partial sum
-//      q mod 32 (entries in list order, each entry's attraction before its
-//      negatives), then partials are combined pairwise with strides
-//      16, 8, 4, 2, 1. The reference's order is the FxHashMap order above.
+//   The per-node gradient is the reference's running sum (embedding.rs:
+//   194-248) in incidence-list order; with deviation 2 that list order is the
+//   canonical one.
 // Floating-point expressions are evaluated exactly as written in the Rust
 // source (no contraction: build with -ffp-contract=off).
 
@@ -571,17 +569,8 @@ int oracle_evoc_embedding(const int64_t* indptr, const uint32_t* indices,
     // :188-253 gradient accumulation, parallel over nodes
 #pragma omp parallel for schedule(dynamic, 1024) reduction(+ : fired_edges, negs, act)
     for (int64_t ni = 0; ni < n; ++ni) {
-      float part[32][16];
-      float* part_dyn = nullptr;
-      std::vector<float> part_heap;
-      if (D > 16) {
-        part_heap.assign(32 * D, 0.0f);
-        part_dyn = part_heap.data();
-      } else {
-        for (int l = 0; l < 32; ++l)
-          for (int64_t d = 0; d < D; ++d) part[l][d] = 0.0f;
-      }
-      auto P = [&](int l) -> float* { return part_dyn ? part_dyn + l * D : part[l]; };
+      float* g = &grads[ni * D];  // :194-196
+      for (int64_t d = 0; d < D; ++d) g[d] = 0.0f;
       const float* ei = &embd[ni * D];
       bool touched = false;
       const int64_t start = offsets[ni], end = offsets[ni + 1];
@@ -589,7 +578,6 @@ int oracle_evoc_embedding(const int64_t* indptr, const uint32_t* indices,
         const Inc& ce = csr_edges[q];
         if (next_sample[ce.eidx] > epoch_t) continue;  // :204
         touched = true;
-        float* g = P((int)((q - start) & 31));
         const float* eo = &embd[(int64_t)ce.other * D];
         float dsq = 0.0f;  // :210 (deviation 4)
         for (int64_t d = 0; d < D; ++d) {
@@ -630,14 +618,6 @@ int oracle_evoc_embedding(const int64_t* indptr, const uint32_t* indices,
           }
         }
       }
-      // pairwise combination of the 32 partial sums (deviation 5)
-      for (int off = 16; off >= 1; off >>= 1)
-        for (int l = 0; l < off; ++l) {
-          float* a = P(l);
-          const float* b = P(l + off);
-          for (int64_t d = 0; d < D; ++d) a[d] = a[d] + b[d];
-        }
-      for (int64_t d = 0; d < D; ++d) grads[ni * D + d] = P(0)[d];
       active[ni] = touched ? 1 : 0;
       act += touched ? 1 : 0;
     }

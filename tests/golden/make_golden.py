@@ -11,7 +11,7 @@ written directly from the Rust source with numpy float32 scalar arithmetic
 
 It shares with the C++ oracle and the CUDA library only the documented
 arithmetic contract (own exp, Philox4x32-10 negatives and initialisation,
-serial squared distance, 32-partial gradient summation). The fixtures pin the
+serial squared distance). The fixtures pin the
 C++ oracle bit for bit. Run from the repository root:
 
     python tests/golden/make_golden.py
@@ -205,14 +205,13 @@ def evoc_embedding(adj, dim, n_epochs=50, noise=0.5, neg_rate=1.0, alpha=0.1, b1
         et = F(ep)
         grads = [None] * n
         for ni in range(n):
-            part = [[F(0)] * dim for _ in range(32)]
+            g = [F(0)] * dim
             touched = False
             ei_ = e[ni * dim:(ni + 1) * dim]
-            for q, (eid, smaller, o) in enumerate(inc[ni]):
+            for eid, smaller, o in inc[ni]:
                 if ns[eid] > et:
                     continue
                 touched = True
-                g = part[q % 32]
                 eo = e[o * dim:(o + 1) * dim]
                 dsq = F(0)
                 for d in range(dim):
@@ -240,12 +239,7 @@ def evoc_embedding(adj, dim, n_epochs=50, noise=0.5, neg_rate=1.0, alpha=0.1, b1
                                 c = gc * (ei_[d] - ek[d])
                                 c = min(max(c, F(-4)), F(4))
                                 g[d] = g[d] + c
-            off = 16
-            while off >= 1:
-                for lane in range(off):
-                    part[lane] = [a + b for a, b in zip(part[lane], part[lane + off])]
-                off //= 2
-            grads[ni] = part[0] if touched else None
+            grads[ni] = g if touched else None
         lr_ad = lr * ads
         for ni in range(n):
             if grads[ni] is None:

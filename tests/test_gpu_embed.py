@@ -111,13 +111,13 @@ def test_stats_vs_oracle(ctx, oracle, blobs_graph):
     assert st[0, 0] == 0 and st[1:, 0].min() > 0
 
 
-def test_lanes_do_not_change_results(ctx, blobs_graph, monkeypatch):
+def test_launch_shape_does_not_change_results(ctx, blobs_graph, monkeypatch):
     g, _, _ = blobs_graph
     outs = []
-    for lanes in ("8", "16", "32"):
-        monkeypatch.setenv("EVOC_LANES", lanes)
+    for wpb in ("1", "2", "4"):
+        monkeypatch.setenv("EVOC_WARPS_PER_BLOCK", wpb)
         outs.append(ctx.embed(g, 8, seed=5))
-    monkeypatch.delenv("EVOC_LANES")
+    monkeypatch.delenv("EVOC_WARPS_PER_BLOCK")
     for o in outs[1:]:
         _assert_bits(o, outs[0])
 
