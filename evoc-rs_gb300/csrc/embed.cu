@@ -77,6 +77,13 @@ struct evoc_plan {
   float one_m_b1 = 0, one_m_b2 = 0;
   std::vector<evoc_epoch_stats_t> stats;
   bool active_counted = false;
+  // per-epoch fired-entry records (the fast path): for epoch t and tile T,
+  // records [tile_off[t * ntiles + T], tile_off[t * ntiles + T + 1])
+  bool use_records = false;
+  int64_t ntiles = 0;
+  int64_t n_records = 0;
+  evoc::DevBuf<int64_t> tile_off;
+  evoc::DevBuf<uint32_t> rec_other, rec_aux, rec_eidx;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
 };
@@ -425,6 +432,10 @@ struct EpochArgs {
   float* grad_out;
   const uint32_t* prob_of_node;
   const ProbInfo* prob;
+  const int64_t* tile_off;  // record offsets of this epoch (records path)
+  const uint32_t* rec_other;
+  const uint32_t* rec_aux;
+  const uint32_t* rec_eidx;
   uint32_t n_total;
   uint32_t epoch;
   uint64_t seed;
@@ -713,6 +724,321 @@ __global__ void __launch_bounds__(128) k_epoch(EpochArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Fast path: per-epoch records of the fired entries.
+//
+// The epochs-per-sample schedule does not depend on the embedding, so the
+// set-up lists, for every epoch and every 32-node tile, the incidence entries
+// that fire, in incidence order, as records (partner id, tile-local node |
+// negative count << 5, edge id). The epoch kernel then streams its tile's
+// records (coalesced, next chunk prefetched) instead of scanning fire bits.
+// ---------------------------------------------------------------------------
+__global__ void k_rec_count(const int64_t* __restrict__ inc_ptr, int64_t n,
+                            int64_t ntiles, const uint32_t* __restrict__ planes,
+                            int32_t ne, int32_t P, int64_t W,
+                            int32_t* __restrict__ counts) {
+  const unsigned FULL = 0xffffffffu;
+  const int64_t tile = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (tile >= ntiles) return;
+  const int64_t v0 = tile * TILE;
+  const int nt = (int)min((int64_t)TILE, n - v0);
+  const int64_t P0 = inc_ptr[v0], P1 = inc_ptr[v0 + nt];
+  const int64_t W0 = P0 >> 5, W1 = (P1 - 1) >> 5;
+  for (int32_t t = 0; t < ne; ++t) {
+    const uint32_t* fire = planes + (size_t)t * (1 + P) * W;
+    int c = 0;
+    if (P1 > P0)
+      for (int64_t w = W0 + lane; w <= W1; w += 32) {
+        uint32_t word = fire[w];
+        if (w == W0) word &= FULL << (P0 & 31);
+        if (w == W1) {
+          const int hi = (int)((P1 - 1) & 31);
+          word &= (hi == 31) ? FULL : ((2u << hi) - 1u);
+        }
+        c += __popc(word);
+      }
+    c = (int)__reduce_add_sync(FULL, (unsigned)c);
+    if (lane == 0) counts[(int64_t)t * ntiles + tile] = c;
+  }
+}
+
+// One warp per tile; entries outer (32-aligned chunks), epochs inner, with a
+// write cursor per epoch in shared memory (held by lane 0).
+__global__ void k_rec_fill(const int64_t* __restrict__ inc_ptr,
+                           const uint32_t* __restrict__ inc_other,
+                           const int64_t* __restrict__ eidx_base, int64_t n,
+                           int64_t ntiles, const uint32_t* __restrict__ planes,
+                           int32_t ne, int32_t P, int64_t W,
+                           const int64_t* __restrict__ tile_off,
+                           uint32_t* __restrict__ rec_other,
+                           uint32_t* __restrict__ rec_aux,
+                           uint32_t* __restrict__ rec_eidx) {
+  extern __shared__ int64_t cursors[];
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  int64_t* cur = cursors + (size_t)wib * ne;
+  const int64_t tile = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
+  if (tile >= ntiles) return;
+  const int64_t v0 = tile * TILE;
+  const int nt = (int)min((int64_t)TILE, n - v0);
+  const int64_t pbl = inc_ptr[v0 + min(lane, nt)];  // lanes >= nt hold the end
+  const int64_t ebl = (lane < nt) ? eidx_base[v0 + lane] : 0;
+  const int64_t P0 = __shfl_sync(FULL, pbl, 0);
+  const int64_t P1 = inc_ptr[v0 + nt];  // nt may be 32: no lane holds the end
+  if (lane == 0)
+    for (int32_t t = 0; t < ne; ++t) cur[t] = tile_off[(int64_t)t * ntiles + tile];
+  const uint32_t lt = (1u << lane) - 1u;
+  for (int64_t base = P0 & ~(int64_t)31; base < P1; base += 32) {
+    const int64_t p = base + lane;
+    const bool valid = p >= P0 && p < P1;
+    int node = 0;
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+      const int64_t st = __shfl_sync(FULL, pbl, node + step);
+      if (node + step < nt && st <= p) node += step;
+    }
+    const int64_t eb = __shfl_sync(FULL, ebl, node);
+    const uint32_t other = valid ? inc_other[p] : 0u;
+    const uint32_t eidx = (uint32_t)(p + eb);
+    for (int32_t t = 0; t < ne; ++t) {
+      const uint32_t* f = planes + (size_t)t * (1 + P) * W + (base >> 5);
+      const uint32_t word = f[0];
+      const bool fired = valid && ((word >> lane) & 1u);
+      const uint32_t bal = __ballot_sync(FULL, fired);
+      if (bal == 0) continue;
+      uint32_t nneg = 0;
+      for (int32_t b = 0; b < P; ++b) nneg |= ((f[(size_t)(1 + b) * W] >> lane) & 1u) << b;
+      int64_t o0 = (lane == 0) ? cur[t] : 0;
+      o0 = __shfl_sync(FULL, o0, 0);
+      if (fired) {
+        const int64_t q = o0 + __popc(bal & lt);
+        rec_other[q] = other;
+        rec_aux[q] = (uint32_t)node | (nneg << 5);
+        rec_eidx[q] = eidx;
+      }
+      if (lane == 0) cur[t] = o0 + __popc(bal);
+    }
+  }
+}
+
+template <int DIMP>
+struct alignas(16) RecSmem {
+  float rows[TILE][DIMP];       // e_cur rows of the tile's nodes
+  float S[TILE][DIMP + 1];      // running gradients
+  float contrib[CAP][DIMP + 1]; // contribution slots of the current chunk
+  uint8_t slot_node[CAP];       // tile-local node of each slot
+};
+
+// Contribution of slot k of an entry: k == 0 attraction (embedding.rs:213-221),
+// k >= 1 negative k-1 (embedding.rs:237-245); +0 for skipped terms.
+template <int DIMP>
+__device__ __forceinline__ void slot_value(float* __restrict__ dst, int k, bool skip,
+                                           const float (&ev)[DIMP],
+                                           const float (&row)[DIMP], float two_noise,
+                                           float gamma4) {
+  if (skip) {
+#pragma unroll
+    for (int d = 0; d < DIMP; ++d) dst[d] = 0.0f;
+    return;
+  }
+  float diff[DIMP];
+  float dsq = 0.0f;
+#pragma unroll
+  for (int d = 0; d < DIMP; ++d) {
+    diff[d] = fsub(ev[d], row[d]);
+    dsq = fadd(dsq, fmul(diff[d], diff[d]));
+  }
+  if (k == 0) {
+    if (dsq >= 1e-8f) {
+      const float dist = fsqrt(dsq);
+      const float coeff = fdiv(fsub(-fmul(two_noise, dist), 2.0f),
+                               fadd(fsub(fmul(2.0f, dsq), fmul(0.5f, dist)), 1.0f));
+#pragma unroll
+      for (int d = 0; d < DIMP; ++d) dst[d] = fmul(coeff, diff[d]);
+      return;
+    }
+  } else if (dsq > 0.01f) {
+    const float gc = fdiv(gamma4, fmul(fadd(1.0f, fmul(0.25f, dsq)), dsq));
+#pragma unroll
+    for (int d = 0; d < DIMP; ++d) {
+      const float c = fmaxf(fmul(gc, diff[d]), -4.0f);
+      dst[d] = fminf(c, 4.0f);
+    }
+    return;
+  }
+#pragma unroll
+  for (int d = 0; d < DIMP; ++d) dst[d] = 0.0f;
+}
+
+template <int DIMP>
+__global__ void __launch_bounds__(128) k_epoch_rec(EpochArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  RecSmem<DIMP>& sm = reinterpret_cast<RecSmem<DIMP>*>(smem_raw)[threadIdx.x >> 5];
+  const int64_t tile = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int64_t v0 = tile * TILE;
+  if (v0 >= (int64_t)a.n_total) return;  // whole warp
+  const int nt = (int)min((int64_t)TILE, (int64_t)a.n_total - v0);
+  const bool has_node = lane < nt;
+  const int64_t r0 = a.tile_off[tile], r1 = a.tile_off[tile + 1];
+  uint32_t o_n = 0, aux_n = 0, ex_n = 0;
+  if (r0 + lane < r1) {
+    o_n = __ldcs(a.rec_other + r0 + lane);
+    aux_n = __ldcs(a.rec_aux + r0 + lane);
+    ex_n = __ldcs(a.rec_eidx + r0 + lane);
+  }
+  {
+    const float4* src = reinterpret_cast<const float4*>(a.e_cur + (size_t)v0 * DIMP);
+    float4* dst = reinterpret_cast<float4*>(&sm.rows[0][0]);
+    for (int i = lane; i < nt * (DIMP / 4); i += 32) dst[i] = __ldg(src + i);
+  }
+  for (int i = lane; i < TILE * (DIMP + 1); i += 32) (&sm.S[0][0])[i] = 0.0f;
+  __syncwarp();
+  const float two_noise = fmul(2.0f, a.noise);
+  const float gamma4 = fmul(a.gamma, 4.0f);
+  uint32_t touched = 0;
+  int64_t r = r0;
+  int so = 0;  // slots of the first record consumed by earlier chunks
+  while (r < r1) {
+    const uint32_t o = o_n, aux = aux_n, exi = ex_n;
+    const bool valid = r + lane < r1;
+    const int node = (int)(aux & 31u);
+    const uint32_t nneg = aux >> 5;
+    const int k_first = (lane == 0) ? so : 0;
+    const int cc = valid ? (int)(1 + nneg) - k_first : 0;
+    int cincl = cc;
+#pragma unroll
+    for (int s2 = 1; s2 < 32; s2 <<= 1) {
+      const int y = __shfl_up_sync(FULL, cincl, s2);
+      if (lane >= s2) cincl += y;
+    }
+    const int cexcl = cincl - cc;
+    const int nslots = max(0, min(cincl, CAP) - cexcl);
+    const int ndone = __popc(__ballot_sync(FULL, valid && cincl <= CAP));
+    const int used = min(__shfl_sync(FULL, cincl, 31), CAP);
+    const int cex_nd = __shfl_sync(FULL, cexcl, ndone & 31);
+    const int kf_nd = __shfl_sync(FULL, k_first, ndone & 31);
+    const int64_t rn = r + ndone;
+    if (rn + lane < r1) {  // prefetch the next chunk's records
+      o_n = __ldcs(a.rec_other + rn + lane);
+      aux_n = __ldcs(a.rec_aux + rn + lane);
+      ex_n = __ldcs(a.rec_eidx + rn + lane);
+    }
+    touched |= __reduce_or_sync(FULL, valid ? (1u << node) : 0u);
+    if (nslots > 0) {
+      const uint32_t vg = (uint32_t)(v0 + node);
+      float ev[DIMP];
+#pragma unroll
+      for (int d = 0; d < DIMP; ++d) ev[d] = sm.rows[node][d];
+      uint32_t nb = 0, np = a.n_total;
+      uint64_t seed = a.seed;
+      if (a.prob_of_node && k_first + nslots > 1) {
+        const ProbInfo pi = a.prob[a.prob_of_node[vg]];
+        nb = pi.node_base;
+        np = pi.n;
+        seed = pi.seed;
+      }
+      // the first two slots: both gathers in flight before either is used
+      const int k0 = k_first;
+      const uint32_t src0 = (k0 == 0) ? o : nb + negative_draw(seed, (uint32_t)(k0 - 1), a.epoch, exi, np);
+      const bool skip0 = (k0 > 0) && (src0 == vg);
+      const bool has1 = nslots >= 2;
+      const uint32_t src1 = has1 ? nb + negative_draw(seed, (uint32_t)k0, a.epoch, exi, np) : 0u;
+      const bool skip1 = has1 && (src1 == vg);
+      float row0[DIMP], row1[DIMP];
+      if (!skip0) load_row<DIMP>(a.e_cur + (size_t)src0 * DIMP, row0);
+      if (has1 && !skip1) load_row<DIMP>(a.e_cur + (size_t)src1 * DIMP, row1);
+      slot_value<DIMP>(sm.contrib[cexcl], k0, skip0, ev, row0, two_noise, gamma4);
+      sm.slot_node[cexcl] = (uint8_t)node;
+      if (has1) {
+        slot_value<DIMP>(sm.contrib[cexcl + 1], k0 + 1, skip1, ev, row1, two_noise, gamma4);
+        sm.slot_node[cexcl + 1] = (uint8_t)node;
+      }
+      for (int t = 2; t < nslots; ++t) {
+        const int k = k0 + t;
+        const uint32_t src = nb + negative_draw(seed, (uint32_t)(k - 1), a.epoch, exi, np);
+        const bool skip = (src == vg);
+        if (!skip) load_row<DIMP>(a.e_cur + (size_t)src * DIMP, row0);
+        slot_value<DIMP>(sm.contrib[cexcl + t], k, skip, ev, row0, two_noise, gamma4);
+        sm.slot_node[cexcl + t] = (uint8_t)node;
+      }
+    }
+    __syncwarp();
+    {  // serial accumulation of slots [0, used), one lane per (node, dim)
+      const int sa = lane, sb = lane + 32;
+      const bool st_a = sa < used && (sa == 0 || sm.slot_node[sa] != sm.slot_node[sa - 1]);
+      const bool st_b = sb < used && sm.slot_node[sb] != sm.slot_node[sb - 1];
+      const uint32_t ma = __ballot_sync(FULL, st_a), mb = __ballot_sync(FULL, st_b);
+      const int na = __popc(ma), nseg = na + __popc(mb);
+      for (int tsk = lane; tsk < nseg * DIMP; tsk += 32) {
+        const int seg = tsk / DIMP, d = tsk - seg * DIMP;
+        const int start = (seg < na) ? (int)__fns(ma, 0u, seg + 1)
+                                     : 32 + (int)__fns(mb, 0u, seg - na + 1);
+        int end = used;
+        if (seg + 1 < nseg)
+          end = (seg + 1 < na) ? (int)__fns(ma, 0u, seg + 2)
+                               : 32 + (int)__fns(mb, 0u, seg + 1 - na + 1);
+        const int nd = sm.slot_node[start];
+        float acc = sm.S[nd][d];
+        for (int s2 = start; s2 < end; ++s2) acc = fadd(acc, sm.contrib[s2][d]);
+        sm.S[nd][d] = acc;
+      }
+    }
+    __syncwarp();
+    int next_so = 0;
+    if (ndone < 32 && rn < r1) next_so = kf_nd + max(0, CAP - cex_nd);
+    r = rn;
+    so = next_so;
+  }
+
+  if (has_node) {  // Adam, embedding.rs:256-272
+    const size_t q = (size_t)(v0 + lane) * DIMP;
+    const bool act = (touched >> lane) & 1u;
+    float e[DIMP], g[DIMP];
+#pragma unroll
+    for (int d = 0; d < DIMP; ++d) {
+      e[d] = sm.rows[lane][d];
+      g[d] = act ? sm.S[lane][d] : 0.0f;
+    }
+    if (act) {
+      const float4* m4 = reinterpret_cast<const float4*>(a.m + q);
+      const float4* v4 = reinterpret_cast<const float4*>(a.v + q);
+      float mm[DIMP], vv[DIMP];
+#pragma unroll
+      for (int i = 0; i < DIMP / 4; ++i) {
+        const float4 x = __ldcs(m4 + i), y = __ldcs(v4 + i);
+        mm[4 * i] = x.x; mm[4 * i + 1] = x.y; mm[4 * i + 2] = x.z; mm[4 * i + 3] = x.w;
+        vv[4 * i] = y.x; vv[4 * i + 1] = y.y; vv[4 * i + 2] = y.z; vv[4 * i + 3] = y.w;
+      }
+#pragma unroll
+      for (int d = 0; d < DIMP; ++d) {
+        mm[d] = fadd(mm[d], fmul(a.one_m_b1, fsub(g[d], mm[d])));
+        vv[d] = fadd(vv[d], fmul(a.one_m_b2, fsub(fmul(g[d], g[d]), vv[d])));
+        e[d] = fadd(e[d], fdiv(fmul(a.lr_ad, mm[d]), fadd(fsqrt(vv[d]), a.epsc)));
+      }
+      float4* mo = reinterpret_cast<float4*>(a.m + q);
+      float4* vo = reinterpret_cast<float4*>(a.v + q);
+#pragma unroll
+      for (int i = 0; i < DIMP / 4; ++i) {
+        __stcs(mo + i, make_float4(mm[4 * i], mm[4 * i + 1], mm[4 * i + 2], mm[4 * i + 3]));
+        __stcs(vo + i, make_float4(vv[4 * i], vv[4 * i + 1], vv[4 * i + 2], vv[4 * i + 3]));
+      }
+    }
+    float4* eo = reinterpret_cast<float4*>(a.e_next + q);
+#pragma unroll
+    for (int i = 0; i < DIMP / 4; ++i)
+      eo[i] = make_float4(e[4 * i], e[4 * i + 1], e[4 * i + 2], e[4 * i + 3]);
+    if (a.grad_out) {
+      float4* go = reinterpret_cast<float4*>(a.grad_out + q);
+#pragma unroll
+      for (int i = 0; i < DIMP / 4; ++i)
+        go[i] = make_float4(g[4 * i], g[4 * i + 1], g[4 * i + 2], g[4 * i + 3]);
+    }
+  }
+}
+
 using EpochKernel = void (*)(EpochArgs);
 
 EpochKernel pick_kernel(int dimp) {
@@ -726,6 +1052,19 @@ size_t tile_smem(int dimp) {
   if (dimp == 4) return sizeof(TileSmem<4>);
   if (dimp == 8) return sizeof(TileSmem<8>);
   return sizeof(TileSmem<16>);
+}
+
+EpochKernel pick_rec_kernel(int dimp) {
+  if (dimp == 4) return k_epoch_rec<4>;
+  if (dimp == 8) return k_epoch_rec<8>;
+  if (dimp == 16) return k_epoch_rec<16>;
+  return nullptr;
+}
+
+size_t rec_smem(int dimp) {
+  if (dimp == 4) return sizeof(RecSmem<4>);
+  if (dimp == 8) return sizeof(RecSmem<8>);
+  return sizeof(RecSmem<16>);
 }
 
 // Warps (node tiles) per thread block of k_epoch; EVOC_WARPS_PER_BLOCK
@@ -745,7 +1084,7 @@ void launch_epoch(evoc_plan* pl, int32_t t, const float* e_cur, float* e_next,
   a.inc_ptr = pl->inc_ptr.get();
   a.inc_other = pl->inc_other.get();
   a.eidx_base = pl->eidx_base.get();
-  a.fire = pl->planes.get() + (size_t)t * (1 + pl->P) * pl->W;
+  a.fire = pl->use_records ? nullptr : pl->planes.get() + (size_t)t * (1 + pl->P) * pl->W;
   a.W = pl->W;
   a.P = pl->P;
   a.e_cur = e_cur;
@@ -764,10 +1103,20 @@ void launch_epoch(evoc_plan* pl, int32_t t, const float* e_cur, float* e_next,
   a.epsc = pl->epsc[t];
   a.one_m_b1 = pl->one_m_b1;
   a.one_m_b2 = pl->one_m_b2;
+  a.tile_off = nullptr;
+  a.rec_other = a.rec_aux = a.rec_eidx = nullptr;
   const int wpb = pl->lanes;
   const int64_t tiles = (pl->n + TILE - 1) / TILE;
-  pick_kernel(pl->dimp)<<<(unsigned)((tiles + wpb - 1) / wpb), 32 * wpb,
-                          wpb * tile_smem(pl->dimp), s>>>(a);
+  const unsigned grid = (unsigned)((tiles + wpb - 1) / wpb);
+  if (pl->use_records) {
+    a.tile_off = pl->tile_off.get() + (size_t)t * pl->ntiles;
+    a.rec_other = pl->rec_other.get();
+    a.rec_aux = pl->rec_aux.get();
+    a.rec_eidx = pl->rec_eidx.get();
+    pick_rec_kernel(pl->dimp)<<<grid, 32 * wpb, wpb * rec_smem(pl->dimp), s>>>(a);
+  } else {
+    pick_kernel(pl->dimp)<<<grid, 32 * wpb, wpb * tile_smem(pl->dimp), s>>>(a);
+  }
   EVOC_CHECK_LAUNCH();
 }
 
@@ -782,6 +1131,56 @@ void concat_graph(const evoc_graph* g, int64_t node_off, int64_t entry_off,
 void fill_eidx_src(uint2* out, const uint32_t* e_src, int64_t U, cudaStream_t s);
 void add_counts(const int32_t* a, const int32_t* b, int32_t* out, int64_t n,
                 cudaStream_t s);
+
+// Chooses the epoch path and, for the records path, builds the per-epoch
+// fired-entry records (12 bytes per fired directed entry and epoch) and frees
+// the bit planes. EVOC_EPOCH_PATH=scan forces the bit-plane path;
+// EVOC_EPOCH_PATH=records forces the records path.
+static void build_records(evoc_plan* pl) {
+  cudaStream_t s = pl->ctx->stream;
+  const int32_t ne = pl->params.n_epochs;
+  const int64_t n = pl->n;
+  pl->ntiles = (n + TILE - 1) / TILE;
+  const char* env = std::getenv("EVOC_EPOCH_PATH");
+  const bool force_scan = env && std::strcmp(env, "scan") == 0;
+  const bool force_rec = env && std::strcmp(env, "records") == 0;
+  // one int64 write cursor per epoch per warp in shared memory
+  if (force_scan || (size_t)ne * sizeof(int64_t) > 200 * 1024) return;
+  const int64_t cells = (int64_t)ne * pl->ntiles;
+  DevBuf<int32_t> counts(cells, s);
+  k_rec_count<<<blocks_for(pl->ntiles * 32), 256, 0, s>>>(
+      pl->inc_ptr.get(), n, pl->ntiles, pl->planes.get(), ne, pl->P, pl->W, counts.get());
+  EVOC_CHECK_LAUNCH();
+  DevBuf<int64_t> off(cells + 1, s);
+  exclusive_scan_i32_to_i64(counts.get(), off.get(), cells, s);
+  int64_t total = 0;
+  EVOC_CUDA(cudaMemcpyAsync(&total, off.get() + cells, sizeof(int64_t),
+                            cudaMemcpyDeviceToHost, s));
+  EVOC_CUDA(cudaStreamSynchronize(s));
+  size_t free_b = 0, total_b = 0;
+  EVOC_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  const double need = 12.0 * (double)total;
+  if (!force_rec && need > 0.5 * (double)free_b) return;  // keep the bit-plane path
+  pl->rec_other.alloc(total, s);
+  pl->rec_aux.alloc(total, s);
+  pl->rec_eidx.alloc(total, s);
+  const int wpb = (int)std::max<size_t>(1, std::min<size_t>(4, (200 * 1024) / ((size_t)ne * sizeof(int64_t))));
+  const size_t smem = (size_t)wpb * ne * sizeof(int64_t);
+  if (smem > 48 * 1024)
+    EVOC_CUDA(cudaFuncSetAttribute((const void*)k_rec_fill,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_rec_fill<<<(unsigned)((pl->ntiles + wpb - 1) / wpb), 32 * wpb, smem, s>>>(
+      pl->inc_ptr.get(), pl->inc_other.get(), pl->eidx_base.get(), n, pl->ntiles,
+      pl->planes.get(), ne, pl->P, pl->W, off.get(), pl->rec_other.get(),
+      pl->rec_aux.get(), pl->rec_eidx.get());
+  EVOC_CHECK_LAUNCH();
+  pl->tile_off = std::move(off);
+  pl->n_records = total;
+  pl->use_records = true;
+  pl->planes.release();
+  pl->inc_other.release();
+  EVOC_CUDA(cudaStreamSynchronize(s));
+}
 
 evoc_ctx* plan_ctx(const evoc_plan* p) { return p->ctx; }
 void plan_info(const evoc_plan* p, int64_t* n_edges, int64_t* n_inc,
@@ -1015,6 +1414,22 @@ evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
         inc_ps.get(), inc_up.get(), n_inc, ne, neg_factor, pl->P, pl->W,
         pl->planes.get());
     EVOC_CHECK_LAUNCH();
+  }
+
+  if (ne > 0) {
+    // active nodes per epoch, from the fire planes
+    DevBuf<unsigned long long> act(ne, s);
+    EVOC_CUDA(cudaMemsetAsync(act.get(), 0, act.bytes(), s));
+    k_active_count<<<blocks_for(n * 32), 256, 0, s>>>(pl->inc_ptr.get(), n, pl->planes.get(),
+                                                      ne, pl->P, pl->W, act.get());
+    EVOC_CHECK_LAUNCH();
+    std::vector<unsigned long long> h(ne);
+    EVOC_CUDA(cudaMemcpyAsync(h.data(), act.get(), ne * sizeof(unsigned long long),
+                              cudaMemcpyDeviceToHost, s));
+    EVOC_CUDA(cudaStreamSynchronize(s));
+    for (int32_t t = 0; t < ne; ++t) pl->stats[t].active_nodes = (int64_t)h[t];
+    pl->active_counted = true;
+    build_records(pl.get());
   }
 
   pl->m.alloc(n * pl->dimp, s);
