@@ -76,14 +76,15 @@ struct evoc_plan {
   std::vector<float> lr_ad, epsc, gamma;
   float one_m_b1 = 0, one_m_b2 = 0;
   std::vector<evoc_epoch_stats_t> stats;
-  bool active_counted = false;
   // per-epoch fired-entry records (the fast path): for epoch t and tile T,
   // records [tile_off[t * ntiles + T], tile_off[t * ntiles + T + 1])
   bool use_records = false;
   int64_t ntiles = 0;
   int64_t n_records = 0;
   evoc::DevBuf<int64_t> tile_off;
-  evoc::DevBuf<uint32_t> rec_other, rec_aux, rec_eidx;
+  evoc::DevBuf<uint32_t> rec_other, rec_aux, rec_neg0;
+  evoc::DevBuf<uint32_t> rec_eidx;  // only when an edge draws > 1 negative
+  bool stats_done = false;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
 };
@@ -435,6 +436,7 @@ struct EpochArgs {
   const int64_t* tile_off;  // record offsets of this epoch (records path)
   const uint32_t* rec_other;
   const uint32_t* rec_aux;
+  const uint32_t* rec_neg0;
   const uint32_t* rec_eidx;
   uint32_t n_total;
   uint32_t epoch;
@@ -733,47 +735,67 @@ __global__ void __launch_bounds__(128) k_epoch(EpochArgs a) {
 // negative count << 5, edge id). The epoch kernel then streams its tile's
 // records (coalesced, next chunk prefetched) instead of scanning fire bits.
 // ---------------------------------------------------------------------------
-__global__ void k_rec_count(const int64_t* __restrict__ inc_ptr, int64_t n,
-                            int64_t ntiles, const uint32_t* __restrict__ planes,
-                            int32_t ne, int32_t P, int64_t W,
-                            int32_t* __restrict__ counts) {
+// Count pass: warp per tile; each lane runs the epochs-per-sample recurrence
+// of one incidence entry over all epochs; per-epoch fired counts of the tile
+// accumulate in shared memory (lane 0), and the largest negative count is
+// reduced into *max_neg.
+__global__ void k_sched_count(const int64_t* __restrict__ inc_ptr,
+                              const float* __restrict__ inc_ps,
+                              const uint8_t* __restrict__ inc_up, int64_t n,
+                              int64_t ntiles, int32_t ne, float neg_factor,
+                              int32_t* __restrict__ counts,
+                              unsigned long long* __restrict__ max_neg) {
+  extern __shared__ int32_t cnt_all[];
   const unsigned FULL = 0xffffffffu;
-  const int64_t tile = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  int32_t* cnt = cnt_all + (size_t)wib * ne;
+  const int64_t tile = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
   if (tile >= ntiles) return;
+  for (int32_t t = lane; t < ne; t += 32) cnt[t] = 0;
+  __syncwarp();
   const int64_t v0 = tile * TILE;
   const int nt = (int)min((int64_t)TILE, n - v0);
   const int64_t P0 = inc_ptr[v0], P1 = inc_ptr[v0 + nt];
-  const int64_t W0 = P0 >> 5, W1 = (P1 - 1) >> 5;
-  for (int32_t t = 0; t < ne; ++t) {
-    const uint32_t* fire = planes + (size_t)t * (1 + P) * W;
-    int c = 0;
-    if (P1 > P0)
-      for (int64_t w = W0 + lane; w <= W1; w += 32) {
-        uint32_t word = fire[w];
-        if (w == W0) word &= FULL << (P0 & 31);
-        if (w == W1) {
-          const int hi = (int)((P1 - 1) & 31);
-          word &= (hi == 31) ? FULL : ((2u << hi) - 1u);
-        }
-        c += __popc(word);
-      }
-    c = (int)__reduce_add_sync(FULL, (unsigned)c);
-    if (lane == 0) counts[(int64_t)t * ntiles + tile] = c;
+  unsigned long long mx = 0;
+  for (int64_t base = P0 & ~(int64_t)31; base < P1; base += 32) {
+    const int64_t p = base + lane;
+    const bool valid = p >= P0 && p < P1;
+    Sched sc;
+    sc.init(valid ? inc_ps[p] : 3.0e38f, neg_factor, valid && inc_up[p]);
+    for (int32_t t = 0; t < ne; ++t) {
+      uint64_t nn = 0;
+      const bool f = valid && sc.step((float)t, &nn);
+      if (nn > mx) mx = nn;
+      const uint32_t bal = __ballot_sync(FULL, f);
+      if (lane == 0) cnt[t] += __popc(bal);
+    }
   }
+  __syncwarp();
+  for (int32_t t = lane; t < ne; t += 32) counts[(int64_t)t * ntiles + tile] = cnt[t];
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long y = __shfl_xor_sync(FULL, mx, o);
+    mx = y > mx ? y : mx;
+  }
+  if (lane == 0 && mx) atomicMax(max_neg, mx);
 }
 
-// One warp per tile; entries outer (32-aligned chunks), epochs inner, with a
-// write cursor per epoch in shared memory (held by lane 0).
-__global__ void k_rec_fill(const int64_t* __restrict__ inc_ptr,
-                           const uint32_t* __restrict__ inc_other,
-                           const int64_t* __restrict__ eidx_base, int64_t n,
-                           int64_t ntiles, const uint32_t* __restrict__ planes,
-                           int32_t ne, int32_t P, int64_t W,
-                           const int64_t* __restrict__ tile_off,
-                           uint32_t* __restrict__ rec_other,
-                           uint32_t* __restrict__ rec_aux,
-                           uint32_t* __restrict__ rec_eidx) {
+// Fill pass: the same recurrence; fired entries are written as records at
+// per-epoch cursors (shared memory, owned by lane 0). The first negative
+// sample of each record is drawn here (Philox, counter j = 0), so the epoch
+// loop only draws the rare further negatives.
+__global__ void k_sched_fill(const int64_t* __restrict__ inc_ptr,
+                             const uint32_t* __restrict__ inc_other,
+                             const float* __restrict__ inc_ps,
+                             const uint8_t* __restrict__ inc_up,
+                             const int64_t* __restrict__ eidx_base, int64_t n,
+                             int64_t ntiles, int32_t ne, float neg_factor,
+                             const int64_t* __restrict__ tile_off,
+                             const uint32_t* __restrict__ prob_of_node,
+                             const ProbInfo* __restrict__ prob, uint64_t seed,
+                             uint32_t* __restrict__ rec_other,
+                             uint32_t* __restrict__ rec_aux,
+                             uint32_t* __restrict__ rec_neg0,
+                             uint32_t* __restrict__ rec_eidx) {
   extern __shared__ int64_t cursors[];
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -789,6 +811,7 @@ __global__ void k_rec_fill(const int64_t* __restrict__ inc_ptr,
   if (lane == 0)
     for (int32_t t = 0; t < ne; ++t) cur[t] = tile_off[(int64_t)t * ntiles + tile];
   const uint32_t lt = (1u << lane) - 1u;
+  const uint32_t n_total = (uint32_t)n;
   for (int64_t base = P0 & ~(int64_t)31; base < P1; base += 32) {
     const int64_t p = base + lane;
     const bool valid = p >= P0 && p < P1;
@@ -801,23 +824,59 @@ __global__ void k_rec_fill(const int64_t* __restrict__ inc_ptr,
     const int64_t eb = __shfl_sync(FULL, ebl, node);
     const uint32_t other = valid ? inc_other[p] : 0u;
     const uint32_t eidx = (uint32_t)(p + eb);
+    uint32_t nb = 0, np = n_total;
+    uint64_t sd = seed;
+    if (prob_of_node && valid) {
+      const ProbInfo pi = prob[prob_of_node[v0 + node]];
+      nb = pi.node_base;
+      np = pi.n;
+      sd = pi.seed;
+    }
+    Sched sc;
+    sc.init(valid ? inc_ps[p] : 3.0e38f, neg_factor, valid && inc_up[p]);
     for (int32_t t = 0; t < ne; ++t) {
-      const uint32_t* f = planes + (size_t)t * (1 + P) * W + (base >> 5);
-      const uint32_t word = f[0];
-      const bool fired = valid && ((word >> lane) & 1u);
-      const uint32_t bal = __ballot_sync(FULL, fired);
+      uint64_t nn = 0;
+      const bool f = valid && sc.step((float)t, &nn);
+      const uint32_t bal = __ballot_sync(FULL, f);
       if (bal == 0) continue;
-      uint32_t nneg = 0;
-      for (int32_t b = 0; b < P; ++b) nneg |= ((f[(size_t)(1 + b) * W] >> lane) & 1u) << b;
       int64_t o0 = (lane == 0) ? cur[t] : 0;
       o0 = __shfl_sync(FULL, o0, 0);
-      if (fired) {
+      if (f) {
         const int64_t q = o0 + __popc(bal & lt);
         rec_other[q] = other;
-        rec_aux[q] = (uint32_t)node | (nneg << 5);
-        rec_eidx[q] = eidx;
+        rec_aux[q] = (uint32_t)node | ((uint32_t)nn << 5);
+        rec_neg0[q] = nn ? nb + negative_draw(sd, 0u, (uint32_t)t, eidx, np) : 0u;
+        if (rec_eidx) rec_eidx[q] = eidx;
       }
       if (lane == 0) cur[t] = o0 + __popc(bal);
+    }
+  }
+}
+
+// Per-epoch negatives and active nodes from the records (on request).
+__global__ void k_rec_stats(const int64_t* __restrict__ tile_off,
+                            const uint32_t* __restrict__ rec_aux, int64_t ntiles,
+                            int32_t ne, unsigned long long* __restrict__ negs,
+                            unsigned long long* __restrict__ active) {
+  const unsigned FULL = 0xffffffffu;
+  const int64_t tile = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (tile >= ntiles) return;
+  for (int32_t t = 0; t < ne; ++t) {
+    const int64_t r0 = tile_off[(int64_t)t * ntiles + tile];
+    const int64_t r1 = tile_off[(int64_t)t * ntiles + tile + 1];
+    uint32_t mask = 0;
+    unsigned long long ng = 0;
+    for (int64_t r = r0 + lane; r < r1; r += 32) {
+      const uint32_t x = rec_aux[r];
+      mask |= 1u << (x & 31u);
+      ng += x >> 5;
+    }
+    mask = __reduce_or_sync(FULL, mask);
+    for (int o = 16; o > 0; o >>= 1) ng += __shfl_xor_sync(FULL, ng, o);
+    if (lane == 0) {
+      if (ng) atomicAdd(&negs[t], ng);
+      if (mask) atomicAdd(&active[t], (unsigned long long)__popc(mask));
     }
   }
 }
@@ -883,11 +942,12 @@ __global__ void __launch_bounds__(128) k_epoch_rec(EpochArgs a) {
   const int nt = (int)min((int64_t)TILE, (int64_t)a.n_total - v0);
   const bool has_node = lane < nt;
   const int64_t r0 = a.tile_off[tile], r1 = a.tile_off[tile + 1];
-  uint32_t o_n = 0, aux_n = 0, ex_n = 0;
+  uint32_t o_n = 0, aux_n = 0, ng_n = 0, ex_n = 0;
   if (r0 + lane < r1) {
     o_n = __ldcs(a.rec_other + r0 + lane);
     aux_n = __ldcs(a.rec_aux + r0 + lane);
-    ex_n = __ldcs(a.rec_eidx + r0 + lane);
+    ng_n = __ldcs(a.rec_neg0 + r0 + lane);
+    if (a.rec_eidx) ex_n = __ldcs(a.rec_eidx + r0 + lane);
   }
   {
     const float4* src = reinterpret_cast<const float4*>(a.e_cur + (size_t)v0 * DIMP);
@@ -902,7 +962,7 @@ __global__ void __launch_bounds__(128) k_epoch_rec(EpochArgs a) {
   int64_t r = r0;
   int so = 0;  // slots of the first record consumed by earlier chunks
   while (r < r1) {
-    const uint32_t o = o_n, aux = aux_n, exi = ex_n;
+    const uint32_t o = o_n, aux = aux_n, neg0 = ng_n, exi = ex_n;
     const bool valid = r + lane < r1;
     const int node = (int)(aux & 31u);
     const uint32_t nneg = aux >> 5;
@@ -924,7 +984,8 @@ __global__ void __launch_bounds__(128) k_epoch_rec(EpochArgs a) {
     if (rn + lane < r1) {  // prefetch the next chunk's records
       o_n = __ldcs(a.rec_other + rn + lane);
       aux_n = __ldcs(a.rec_aux + rn + lane);
-      ex_n = __ldcs(a.rec_eidx + rn + lane);
+      ng_n = __ldcs(a.rec_neg0 + rn + lane);
+      if (a.rec_eidx) ex_n = __ldcs(a.rec_eidx + rn + lane);
     }
     touched |= __reduce_or_sync(FULL, valid ? (1u << node) : 0u);
     if (nslots > 0) {
@@ -934,18 +995,22 @@ __global__ void __launch_bounds__(128) k_epoch_rec(EpochArgs a) {
       for (int d = 0; d < DIMP; ++d) ev[d] = sm.rows[node][d];
       uint32_t nb = 0, np = a.n_total;
       uint64_t seed = a.seed;
-      if (a.prob_of_node && k_first + nslots > 1) {
+      if (a.prob_of_node && k_first + nslots > 2) {
         const ProbInfo pi = a.prob[a.prob_of_node[vg]];
         nb = pi.node_base;
         np = pi.n;
         seed = pi.seed;
       }
+      // negative j: j == 0 was drawn at set-up, later ones draw here
+      auto neg_src = [&](int j) -> uint32_t {
+        return (j == 0) ? neg0 : nb + negative_draw(seed, (uint32_t)j, a.epoch, exi, np);
+      };
       // the first two slots: both gathers in flight before either is used
       const int k0 = k_first;
-      const uint32_t src0 = (k0 == 0) ? o : nb + negative_draw(seed, (uint32_t)(k0 - 1), a.epoch, exi, np);
+      const uint32_t src0 = (k0 == 0) ? o : neg_src(k0 - 1);
       const bool skip0 = (k0 > 0) && (src0 == vg);
       const bool has1 = nslots >= 2;
-      const uint32_t src1 = has1 ? nb + negative_draw(seed, (uint32_t)k0, a.epoch, exi, np) : 0u;
+      const uint32_t src1 = has1 ? neg_src(k0) : 0u;
       const bool skip1 = has1 && (src1 == vg);
       float row0[DIMP], row1[DIMP];
       if (!skip0) load_row<DIMP>(a.e_cur + (size_t)src0 * DIMP, row0);
@@ -958,7 +1023,7 @@ __global__ void __launch_bounds__(128) k_epoch_rec(EpochArgs a) {
       }
       for (int t = 2; t < nslots; ++t) {
         const int k = k0 + t;
-        const uint32_t src = nb + negative_draw(seed, (uint32_t)(k - 1), a.epoch, exi, np);
+        const uint32_t src = neg_src(k - 1);
         const bool skip = (src == vg);
         if (!skip) load_row<DIMP>(a.e_cur + (size_t)src * DIMP, row0);
         slot_value<DIMP>(sm.contrib[cexcl + t], k, skip, ev, row0, two_noise, gamma4);
@@ -1104,7 +1169,7 @@ void launch_epoch(evoc_plan* pl, int32_t t, const float* e_cur, float* e_next,
   a.one_m_b1 = pl->one_m_b1;
   a.one_m_b2 = pl->one_m_b2;
   a.tile_off = nullptr;
-  a.rec_other = a.rec_aux = a.rec_eidx = nullptr;
+  a.rec_other = a.rec_aux = a.rec_neg0 = a.rec_eidx = nullptr;
   const int wpb = pl->lanes;
   const int64_t tiles = (pl->n + TILE - 1) / TILE;
   const unsigned grid = (unsigned)((tiles + wpb - 1) / wpb);
@@ -1112,6 +1177,7 @@ void launch_epoch(evoc_plan* pl, int32_t t, const float* e_cur, float* e_next,
     a.tile_off = pl->tile_off.get() + (size_t)t * pl->ntiles;
     a.rec_other = pl->rec_other.get();
     a.rec_aux = pl->rec_aux.get();
+    a.rec_neg0 = pl->rec_neg0.get();
     a.rec_eidx = pl->rec_eidx.get();
     pick_rec_kernel(pl->dimp)<<<grid, 32 * wpb, wpb * rec_smem(pl->dimp), s>>>(a);
   } else {
@@ -1132,11 +1198,12 @@ void fill_eidx_src(uint2* out, const uint32_t* e_src, int64_t U, cudaStream_t s)
 void add_counts(const int32_t* a, const int32_t* b, int32_t* out, int64_t n,
                 cudaStream_t s);
 
-// Chooses the epoch path and, for the records path, builds the per-epoch
-// fired-entry records (12 bytes per fired directed entry and epoch) and frees
-// the bit planes. EVOC_EPOCH_PATH=scan forces the bit-plane path;
-// EVOC_EPOCH_PATH=records forces the records path.
-static void build_records(evoc_plan* pl) {
+// Records path of the schedule set-up: count pass, scan, fill pass. Returns
+// false (nothing built) when EVOC_EPOCH_PATH=scan, when the epoch count
+// exceeds the shared-memory cursors, or when the records would take more than
+// half of the free device memory (unless EVOC_EPOCH_PATH=records).
+static bool build_records(evoc_plan* pl, const float* inc_ps, const uint8_t* inc_up,
+                          float neg_factor) {
   cudaStream_t s = pl->ctx->stream;
   const int32_t ne = pl->params.n_epochs;
   const int64_t n = pl->n;
@@ -1144,51 +1211,78 @@ static void build_records(evoc_plan* pl) {
   const char* env = std::getenv("EVOC_EPOCH_PATH");
   const bool force_scan = env && std::strcmp(env, "scan") == 0;
   const bool force_rec = env && std::strcmp(env, "records") == 0;
-  // one int64 write cursor per epoch per warp in shared memory
-  if (force_scan || (size_t)ne * sizeof(int64_t) > 200 * 1024) return;
+  if (force_scan || (size_t)ne * sizeof(int64_t) > 200 * 1024) return false;
+  const int wpb = (int)std::max<size_t>(
+      1, std::min<size_t>(4, (200 * 1024) / ((size_t)ne * sizeof(int64_t))));
+  const unsigned grid = (unsigned)((pl->ntiles + wpb - 1) / wpb);
   const int64_t cells = (int64_t)ne * pl->ntiles;
   DevBuf<int32_t> counts(cells, s);
-  k_rec_count<<<blocks_for(pl->ntiles * 32), 256, 0, s>>>(
-      pl->inc_ptr.get(), n, pl->ntiles, pl->planes.get(), ne, pl->P, pl->W, counts.get());
+  DevBuf<unsigned long long> mx(1, s);
+  EVOC_CUDA(cudaMemsetAsync(mx.get(), 0, sizeof(unsigned long long), s));
+  const size_t csmem = (size_t)wpb * ne * sizeof(int32_t);
+  if (csmem > 48 * 1024)
+    EVOC_CUDA(cudaFuncSetAttribute((const void*)k_sched_count,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem));
+  k_sched_count<<<grid, 32 * wpb, csmem, s>>>(pl->inc_ptr.get(), inc_ps, inc_up, n,
+                                              pl->ntiles, ne, neg_factor, counts.get(),
+                                              mx.get());
   EVOC_CHECK_LAUNCH();
   DevBuf<int64_t> off(cells + 1, s);
   exclusive_scan_i32_to_i64(counts.get(), off.get(), cells, s);
   int64_t total = 0;
+  unsigned long long maxneg = 0;
   EVOC_CUDA(cudaMemcpyAsync(&total, off.get() + cells, sizeof(int64_t),
                             cudaMemcpyDeviceToHost, s));
+  EVOC_CUDA(cudaMemcpyAsync(&maxneg, mx.get(), sizeof(maxneg), cudaMemcpyDeviceToHost, s));
   EVOC_CUDA(cudaStreamSynchronize(s));
+  if (maxneg > (unsigned long long)NEG_LIMIT)
+    throw Error(EVOC_ERR_UNSUPPORTED,
+                "more than 2^20 negative samples per edge and epoch "
+                "(negative_sample_rate too large)");
+  const bool need_eidx = maxneg > 1;
   size_t free_b = 0, total_b = 0;
   EVOC_CUDA(cudaMemGetInfo(&free_b, &total_b));
-  const double need = 12.0 * (double)total;
-  if (!force_rec && need > 0.5 * (double)free_b) return;  // keep the bit-plane path
+  const double need = (need_eidx ? 16.0 : 12.0) * (double)total;
+  if (!force_rec && need > 0.5 * (double)free_b) return false;
+  pl->max_neg = maxneg;
   pl->rec_other.alloc(total, s);
   pl->rec_aux.alloc(total, s);
-  pl->rec_eidx.alloc(total, s);
-  const int wpb = (int)std::max<size_t>(1, std::min<size_t>(4, (200 * 1024) / ((size_t)ne * sizeof(int64_t))));
-  const size_t smem = (size_t)wpb * ne * sizeof(int64_t);
-  if (smem > 48 * 1024)
-    EVOC_CUDA(cudaFuncSetAttribute((const void*)k_rec_fill,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_rec_fill<<<(unsigned)((pl->ntiles + wpb - 1) / wpb), 32 * wpb, smem, s>>>(
-      pl->inc_ptr.get(), pl->inc_other.get(), pl->eidx_base.get(), n, pl->ntiles,
-      pl->planes.get(), ne, pl->P, pl->W, off.get(), pl->rec_other.get(),
-      pl->rec_aux.get(), pl->rec_eidx.get());
+  pl->rec_neg0.alloc(total, s);
+  if (need_eidx) pl->rec_eidx.alloc(total, s);
+  const size_t fsmem = (size_t)wpb * ne * sizeof(int64_t);
+  if (fsmem > 48 * 1024)
+    EVOC_CUDA(cudaFuncSetAttribute((const void*)k_sched_fill,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
+  k_sched_fill<<<grid, 32 * wpb, fsmem, s>>>(
+      pl->inc_ptr.get(), pl->inc_other.get(), inc_ps, inc_up, pl->eidx_base.get(), n,
+      pl->ntiles, ne, neg_factor, off.get(),
+      pl->n_problems > 1 ? pl->prob_of_node.get() : nullptr,
+      pl->n_problems > 1 ? pl->prob.get() : nullptr, pl->seeds.empty() ? 0 : pl->seeds[0],
+      pl->rec_other.get(), pl->rec_aux.get(), pl->rec_neg0.get(),
+      need_eidx ? pl->rec_eidx.get() : nullptr);
   EVOC_CHECK_LAUNCH();
+  // fired edges per epoch = records of the epoch / 2 (both copies fire)
+  std::vector<int64_t> h(ne + 1);
+  for (int32_t t = 0; t <= ne; ++t)
+    EVOC_CUDA(cudaMemcpyAsync(&h[t], off.get() + (int64_t)t * pl->ntiles, sizeof(int64_t),
+                              cudaMemcpyDeviceToHost, s));
+  EVOC_CUDA(cudaStreamSynchronize(s));
+  for (int32_t t = 0; t < ne; ++t) pl->stats[t].fired_edges = (h[t + 1] - h[t]) / 2;
   pl->tile_off = std::move(off);
   pl->n_records = total;
   pl->use_records = true;
-  pl->planes.release();
   pl->inc_other.release();
-  EVOC_CUDA(cudaStreamSynchronize(s));
+  return true;
 }
 
 evoc_ctx* plan_ctx(const evoc_plan* p) { return p->ctx; }
 void plan_info(const evoc_plan* p, int64_t* n_edges, int64_t* n_inc,
-               int32_t* planes, int32_t* lanes) {
+               int32_t* planes, int32_t* wpb, int64_t* n_records) {
   if (n_edges) *n_edges = p->n_edges;
   if (n_inc) *n_inc = p->n_inc;
   if (planes) *planes = p->P;
-  if (lanes) *lanes = p->lanes;
+  if (wpb) *wpb = p->lanes;
+  if (n_records) *n_records = p->use_records ? p->n_records : 0;
 }
 int64_t plan_n(const evoc_plan* p) { return p->n; }
 int32_t plan_n_epochs(const evoc_plan* p) { return p->params.n_epochs; }
@@ -1375,13 +1469,13 @@ evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
   lptr.release();
   e_ps.release();
 
-  // schedule planes
+  // schedule: per-epoch records (fast path) or bit planes (fallback)
   const float neg_factor = 1.5f / params.negative_sample_rate;  // embedding.rs:116
   pl->W = (n_inc + 31) / 32;
-  DevBuf<unsigned long long> mx(1, s), st(2 * std::max(ne, 1), s);
-  EVOC_CUDA(cudaMemsetAsync(mx.get(), 0, sizeof(unsigned long long), s));
-  EVOC_CUDA(cudaMemsetAsync(st.get(), 0, st.bytes(), s));
-  if (ne > 0) {
+  if (ne > 0 && !build_records(pl.get(), inc_ps.get(), inc_up.get(), neg_factor)) {
+    DevBuf<unsigned long long> mx(1, s), st(2 * ne, s);
+    EVOC_CUDA(cudaMemsetAsync(mx.get(), 0, sizeof(unsigned long long), s));
+    EVOC_CUDA(cudaMemsetAsync(st.get(), 0, st.bytes(), s));
     const bool want_stats = ne <= 4096;
     const size_t smem = want_stats ? 2 * ne * sizeof(unsigned long long) : 0;
     if (smem > 48 * 1024)
@@ -1416,22 +1510,6 @@ evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
     EVOC_CHECK_LAUNCH();
   }
 
-  if (ne > 0) {
-    // active nodes per epoch, from the fire planes
-    DevBuf<unsigned long long> act(ne, s);
-    EVOC_CUDA(cudaMemsetAsync(act.get(), 0, act.bytes(), s));
-    k_active_count<<<blocks_for(n * 32), 256, 0, s>>>(pl->inc_ptr.get(), n, pl->planes.get(),
-                                                      ne, pl->P, pl->W, act.get());
-    EVOC_CHECK_LAUNCH();
-    std::vector<unsigned long long> h(ne);
-    EVOC_CUDA(cudaMemcpyAsync(h.data(), act.get(), ne * sizeof(unsigned long long),
-                              cudaMemcpyDeviceToHost, s));
-    EVOC_CUDA(cudaStreamSynchronize(s));
-    for (int32_t t = 0; t < ne; ++t) pl->stats[t].active_nodes = (int64_t)h[t];
-    pl->active_counted = true;
-    build_records(pl.get());
-  }
-
   pl->m.alloc(n * pl->dimp, s);
   pl->v.alloc(n * pl->dimp, s);
   pl->lanes = default_wpb();
@@ -1442,19 +1520,30 @@ evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
 void plan_stats(const evoc_plan* cpl, evoc_epoch_stats_t* out) {
   evoc_plan* pl = const_cast<evoc_plan*>(cpl);
   const int32_t ne = pl->params.n_epochs;
-  if (pl->has_edges && !pl->active_counted && ne > 0) {
+  if (pl->has_edges && !pl->stats_done && ne > 0) {
     cudaStream_t s = pl->ctx->stream;
-    DevBuf<unsigned long long> act(ne, s);
+    DevBuf<unsigned long long> act(ne, s), ng(ne, s);
     EVOC_CUDA(cudaMemsetAsync(act.get(), 0, act.bytes(), s));
-    k_active_count<<<blocks_for(pl->n * 32), 256, 0, s>>>(
-        pl->inc_ptr.get(), pl->n, pl->planes.get(), ne, pl->P, pl->W, act.get());
+    EVOC_CUDA(cudaMemsetAsync(ng.get(), 0, ng.bytes(), s));
+    if (pl->use_records) {
+      k_rec_stats<<<blocks_for(pl->ntiles * 32), 256, 0, s>>>(
+          pl->tile_off.get(), pl->rec_aux.get(), pl->ntiles, ne, ng.get(), act.get());
+    } else {
+      k_active_count<<<blocks_for(pl->n * 32), 256, 0, s>>>(
+          pl->inc_ptr.get(), pl->n, pl->planes.get(), ne, pl->P, pl->W, act.get());
+    }
     EVOC_CHECK_LAUNCH();
-    std::vector<unsigned long long> h(ne);
-    EVOC_CUDA(cudaMemcpyAsync(h.data(), act.get(), ne * sizeof(unsigned long long),
+    std::vector<unsigned long long> ha(ne), hn(ne);
+    EVOC_CUDA(cudaMemcpyAsync(ha.data(), act.get(), ne * sizeof(unsigned long long),
+                              cudaMemcpyDeviceToHost, s));
+    EVOC_CUDA(cudaMemcpyAsync(hn.data(), ng.get(), ne * sizeof(unsigned long long),
                               cudaMemcpyDeviceToHost, s));
     EVOC_CUDA(cudaStreamSynchronize(s));
-    for (int32_t t = 0; t < ne; ++t) pl->stats[t].active_nodes = (int64_t)h[t];
-    pl->active_counted = true;
+    for (int32_t t = 0; t < ne; ++t) {
+      pl->stats[t].active_nodes = (int64_t)ha[t];
+      if (pl->use_records) pl->stats[t].negatives = (int64_t)hn[t];
+    }
+    pl->stats_done = true;
   }
   for (int32_t t = 0; t < ne; ++t) out[t] = pl->stats[t];
 }

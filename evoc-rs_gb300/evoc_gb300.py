@@ -121,7 +121,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "evoc_plan_enqueue_device": ([vp, vp, vp], C.c_int),
         "evoc_plan_profile_epochs": ([vp, vp, vp, vp], C.c_int),
         "evoc_plan_info": ([vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i32),
-                            C.POINTER(i32)], C.c_int),
+                            C.POINTER(i32), C.POINTER(i64)], C.c_int),
         "evoc_plan_stats": ([vp, C.POINTER(EpochStatsC)], C.c_int),
         "evoc_plan_debug_run": ([vp, vp, i32, i32, vp, vp], C.c_int),
         "evoc_plan_free": ([vp], None),
@@ -218,11 +218,11 @@ class Plan:
         return ms[: self.n_epochs]
 
     def info(self) -> dict:
-        e, i, p, l = C.c_int64(), C.c_int64(), C.c_int32(), C.c_int32()
+        e, i, p, l, r = C.c_int64(), C.c_int64(), C.c_int32(), C.c_int32(), C.c_int64()
         self._ctx._check(self._ctx.lib.evoc_plan_info(self.handle, C.byref(e), C.byref(i),
-                                                      C.byref(p), C.byref(l)))
+                                                      C.byref(p), C.byref(l), C.byref(r)))
         return {"n_edges": e.value, "n_incidence": i.value, "neg_planes": p.value,
-                "warps_per_block": l.value}
+                "warps_per_block": l.value, "n_records": r.value}
 
     def stats(self) -> np.ndarray:
         arr = (EpochStatsC * max(self.n_epochs, 1))()
