@@ -135,6 +135,19 @@ def make_workload(name: str, n_override: int | None):
     return cfg, idx32, dist
 
 
+def profiled_traffic() -> tuple[float | None, str | None]:
+    """DRAM bytes per k_epoch_rec launch at 2M points, from the committed ncu
+    summary (dram__bytes_read.sum + dram__bytes_write.sum, scaled from the
+    captured size by the fired entries); None when no summary exists."""
+    f = ROOT / "profiles" / "k_epoch_rec_hierarchical.md"
+    if not f.exists():
+        return None, None
+    for line in f.read_text().splitlines():
+        if line.startswith("TRAFFIC_PER_LAUNCH_2M_BYTES="):
+            return float(line.split("=", 1)[1]), f"profiles/{f.name}"
+    return None, None
+
+
 def algorithmic_hbm_bytes(n: int, info: dict, dimp: int, stats: np.ndarray) -> np.ndarray:
     """Per-epoch bytes the epoch kernel must move to/from HBM (the partner and
     negative row gathers are served by L2 and counted separately).
@@ -249,9 +262,14 @@ def run_ours(args) -> dict:
     bytes_launch = float(hbm[act].mean())
     pk = peaks()
     achieved = bytes_launch / t_launch / 1e9
+    traffic, traffic_src = profiled_traffic()
+    if args.workload != "hierarchical_2m" or n != 2_000_000 or not info["n_records"]:
+        traffic, traffic_src = None, None
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"],
-                "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4), "traffic": None,
-                "peak_src": pk["src"], "kernel": "k_epoch",
+                "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4),
+                "traffic": traffic, "traffic_src": traffic_src,
+                "algorithmic_bytes_per_launch": round(bytes_launch),
+                "peak_src": pk["src"], "kernel": "k_epoch_rec",
                 "launch_ms": round(t_launch * 1e3, 4), "warps_per_block": info["warps_per_block"],
                 "epoch_path": "records" if info["n_records"] else "bit-planes",
                 "l2_gather_gbs": round(float(l2b[act].mean()) / t_launch / 1e9, 1)}
