@@ -33,6 +33,8 @@ void use_device(evoc_ctx* ctx) { EVOC_CUDA(cudaSetDevice(ctx->device)); }
 
 }  // namespace
 
+void evoc::set_thread_error(const std::string& message) { g_thread_error = message; }
+
 #define EVOC_API_BEGIN try {
 #define EVOC_API_END(ctx)                                        \
   }                                                              \

@@ -129,6 +129,8 @@ void radix_sort_pairs(uint32_t* keys, uint2* vals, int64_t n, int key_bits,
 int bits_for(uint64_t max_value);
 // Read the context's status word and reset it; throw on any set bit.
 void check_status(evoc_ctx* ctx, const char* where);
+// Message returned by evoc_last_error(NULL) on this thread.
+void set_thread_error(const std::string& message);
 
 // ---- fuzzy_set.cu ----------------------------------------------------------
 void smooth_knn_device(evoc_ctx* ctx, const float* d_dist,

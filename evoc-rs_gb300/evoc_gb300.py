@@ -33,6 +33,7 @@ EVOC_ERR_OUT_OF_MEMORY = -5
 EVOC_ERR_NO_DEVICE = -6
 EVOC_ERR_INTERNAL = -7
 KNN_PAD = 0xFFFFFFFF
+NOALLOC_SCRATCH_BYTES = 16 << 20  # EVOC_NOALLOC_SCRATCH_BYTES
 
 # Every symbol declared in include/evoc_gb300.h.
 EXPORTED = [
@@ -43,6 +44,7 @@ EXPORTED = [
     "evoc_plan_create", "evoc_plan_run_device", "evoc_plan_enqueue_device",
     "evoc_plan_profile_epochs", "evoc_plan_info", "evoc_plan_stats",
     "evoc_plan_debug_run", "evoc_plan_free", "evoc_embed_batched",
+    "evoc_knn_to_csr_noalloc",
 ]
 
 
@@ -126,6 +128,8 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "evoc_plan_debug_run": ([vp, vp, i32, i32, vp, vp], C.c_int),
         "evoc_plan_free": ([vp], None),
         "evoc_embed_batched": ([vp, i32, vp, i32, C.POINTER(EmbedParamsC), vp, vp, vp], C.c_int),
+        "evoc_knn_to_csr_noalloc": ([vp, vp, i64, i32, f32, vp, vp, vp, i64, C.POINTER(i64), vp],
+                                    C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)

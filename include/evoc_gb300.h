@@ -149,6 +149,43 @@ EVOC_API int evoc_graph_from_csr(evoc_ctx_t* ctx, const int64_t* indptr,
                         const uint32_t* indices, const float* weights,
                         int64_t n, evoc_graph_t** out_graph);
 
+/* Scratch of evoc_knn_to_csr_noalloc: one device array of this many bytes,
+ * held by every GPU that loads the library until the process exits. */
+#define EVOC_NOALLOC_SCRATCH_BYTES (16u << 20)
+
+/* Weighted directed kNN graph without allocating anything (no counterpart in
+ * the reference). For callers that must not allocate device memory while
+ * they run, such as services that reserve their whole device-memory budget
+ * up front, or host frameworks that own the device heap and forbid operators
+ * to call cudaMalloc. evoc_fuzzy_set_device allocates its scratch and its
+ * result, so those callers cannot use it.
+ *
+ * Computes exactly what evoc_fuzzy_set_device computes with symmetrise = 0
+ * (smooth_knn_dist + knn_to_coo + coo_to_adjacency_list): rows in kNN order,
+ * self loops dropped. Inputs d_knn_idx/d_knn_dist (n*k, rows padded with
+ * EVOC_KNN_PAD) and outputs d_indptr[n+1], d_indices[capacity] and
+ * d_weights[capacity] are caller-owned device memory on the current device;
+ * *nnz_out receives the entry count. The work runs on `stream` (a
+ * cudaStream_t, NULL for the default stream); the call returns when it is
+ * done.
+ *
+ * Limits and sharing:
+ * - Per-row scratch comes from a fixed file-scope device array, so
+ *   n <= (EVOC_NOALLOC_SCRATCH_BYTES - 256) / 16 = 1,048,560 rows. Larger n is
+ *   rejected with EVOC_ERR_UNSUPPORTED, and a capacity below the entry count
+ *   with EVOC_ERR_INVALID_ARGUMENT.
+ * - All calls on a device share that array. Calls whose GPU work overlaps
+ *   race on it.
+ * - The first call on a device looks up the array's device address. Make
+ *   that first call before any stream capture.
+ * - Errors are reported through evoc_last_error(NULL). */
+EVOC_API int evoc_knn_to_csr_noalloc(const uint32_t* d_knn_idx,
+                                     const float* d_knn_dist, int64_t n,
+                                     int32_t k, float effective_n_neighbours,
+                                     int64_t* d_indptr, uint32_t* d_indices,
+                                     float* d_weights, int64_t capacity,
+                                     int64_t* nnz_out, void* stream);
+
 /* Number of nodes and of directed entries of a graph. */
 EVOC_API int evoc_graph_info(const evoc_graph_t* g, int64_t* n, int64_t* nnz);
 
