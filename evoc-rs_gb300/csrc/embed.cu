@@ -38,7 +38,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <chrono>
 #include <memory>
+#include <string>
+#include <utility>
 
 namespace evoc {
 
@@ -203,7 +206,8 @@ __global__ void k_inc_fill(const int64_t* __restrict__ indptr,
                            uint32_t* __restrict__ inc_other,
                            float* __restrict__ inc_ps,
                            uint8_t* __restrict__ inc_up,
-                           int64_t* __restrict__ eidx_base) {
+                           int64_t* __restrict__ eidx_base,
+                           uint32_t* __restrict__ inc_eidx) {
   const int64_t v = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (v >= n) return;
@@ -222,9 +226,17 @@ __global__ void k_inc_fill(const int64_t* __restrict__ indptr,
       const uint32_t bal = __ballot_sync(0xffffffffu, lo);
       if (lo) {
         const int64_t q = o + __popc(bal & lt);
-        inc_other[q] = indices[p];
+        const uint32_t c = indices[p];
+        inc_other[q] = c;
         inc_ps[q] = ps_from_w(weights[p], mw);
         inc_up[q] = 0;
+        // the twin entry (c -> v) is an upper entry of the sorted row c
+        int64_t lo_i = indptr[c], hi_i = indptr[c + 1] - 1;
+        while (lo_i < hi_i) {
+          const int64_t mid = (lo_i + hi_i) >> 1;
+          if ((int64_t)indices[mid] < v) lo_i = mid + 1; else hi_i = mid;
+        }
+        inc_eidx[q] = (uint32_t)(uptr[c] + (lo_i - indptr[c]) - lcnt[c]);
       }
       o += __popc(bal);
     }
@@ -235,6 +247,7 @@ __global__ void k_inc_fill(const int64_t* __restrict__ indptr,
       inc_other[p0 + j] = pe.y;
       inc_ps[p0 + j] = e_ps[pe.x];
       inc_up[p0 + j] = 0;
+      inc_eidx[p0 + j] = pe.x;
     }
   }
   int64_t o = p0 + nl;
@@ -247,6 +260,7 @@ __global__ void k_inc_fill(const int64_t* __restrict__ indptr,
       inc_other[q] = indices[p];
       inc_ps[q] = ps_from_w(weights[p], mw);
       inc_up[q] = 1;
+      inc_eidx[q] = (uint32_t)(uptr[v] + (q - (p0 + nl)));
     }
     o += __popc(bal);
   }
@@ -266,17 +280,26 @@ struct Sched {
     up = up_;
   }
   // Returns fired; *nneg gets the negative count (upper entries only).
+  // The count stays a float: for x = floor(q), to_usize(x).unwrap_or(0) as
+  // f32 equals x when 0 < x < 2^64 and +0 otherwise (x is integer-valued).
   __device__ __forceinline__ bool step(float tf, uint64_t* nneg) {
+    float cntf;
+    const bool fire = stepf(tf, &cntf);
+    *nneg = (uint64_t)cntf;
+    return fire;
+  }
+  __device__ __forceinline__ bool stepf(float tf, float* cnt_out) {
     const bool fire = !(ns > tf);
-    uint64_t cnt = 0;
+    float cntf = 0.0f;
     if (ns <= tf) {
       ns = fadd(ns, ps);
       if (up) {
-        cnt = to_usize_or0(floorf(fdiv(fsub(tf, nn), pn)));
-        nn = fadd(nn, fmul((float)cnt, pn));
+        const float x = floorf(fdiv(fsub(tf, nn), pn));
+        cntf = (x > 0.0f && x < 18446744073709551616.0f) ? x : 0.0f;
+        nn = fadd(nn, fmul(cntf, pn));
       }
     }
-    *nneg = (fire && up) ? cnt : 0;
+    *cnt_out = (fire && up) ? cntf : 0.0f;
     return fire;
   }
 };
@@ -735,16 +758,287 @@ __global__ void __launch_bounds__(128) k_epoch(EpochArgs a) {
 // negative count << 5, edge id). The epoch kernel then streams its tile's
 // records (coalesced, next chunk prefetched) instead of scanning fire bits.
 // ---------------------------------------------------------------------------
+// Per-edge schedule (n_epochs <= 64): thread per undirected edge runs the
+// recurrence once (embedding.rs:274-286) and stores the epochs in which the
+// edge fires as a bit mask, and its negative count per epoch as two bit
+// planes (bit 0 and bit 1 of the count; counts above 3 are caught through
+// max_neg, and the per-entry path is used then). Both incidence copies of the
+// edge take their fire pattern from here.
+__global__ void k_edge_sched(const float* __restrict__ e_ps, int64_t U, int32_t ne,
+                             float neg_factor, unsigned long long* __restrict__ fire_mask,
+                             unsigned long long* __restrict__ neg_lo,
+                             unsigned long long* __restrict__ neg_hi,
+                             unsigned long long* __restrict__ max_neg) {
+  const unsigned FULL = 0xffffffffu;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = e < U;
+  Sched sc;
+  sc.init(valid ? e_ps[e] : 3.0e38f, neg_factor, valid);
+  unsigned long long fm = 0, n0 = 0, n1 = 0;
+  float mx = 0.0f;
+  for (int32_t t = 0; t < ne; ++t) {
+    float c = 0.0f;
+    const bool f = valid && sc.stepf((float)t, &c);
+    if (f) fm |= 1ull << t;
+    const uint32_t c3 = c >= 3.0f ? 3u : (uint32_t)c;
+    n0 |= (unsigned long long)(c3 & 1u) << t;
+    n1 |= (unsigned long long)(c3 >> 1) << t;
+    mx = fmaxf(mx, c);
+  }
+  if (valid) {
+    fire_mask[e] = fm;
+    neg_lo[e] = n0;
+    neg_hi[e] = n1;
+  }
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, o));
+  if ((threadIdx.x & 31) == 0 && mx > 0.0f)
+    atomicMax(max_neg, mx >= 1.8446744e19f ? ~0ull : (unsigned long long)mx);
+}
+
+// 32 x 32 bit transpose across a warp: lane l passes row word x (bit c =
+// element (l, c)); lane c receives column c (bit l = element (l, c)), which
+// is __ballot_sync of bit c. Five butterfly stages swap off-diagonal blocks.
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x, int lane) {
+#pragma unroll
+  for (int j = 16; j >= 1; j >>= 1) {
+    const uint32_t m = j == 16 ? 0x0000FFFFu
+                     : j == 8  ? 0x00FF00FFu
+                     : j == 4  ? 0x0F0F0F0Fu
+                     : j == 2  ? 0x33333333u
+                               : 0x55555555u;
+    const uint32_t y = __shfl_xor_sync(0xffffffffu, x, j);
+    x = (lane & j) ? ((x & ~m) | ((y >> j) & m)) : ((x & m) | ((y << j) & ~m));
+  }
+  return x;
+}
+
+// Fire and negative-count bit planes in incidence order (n_epochs <= 64).
+// F[t * W + w] bit l = entry 32 w + l fires in epoch t; N0 / N1 hold bits 0 /
+// 1 of its negative count (upper entries only). Block of 8 warps per 32 words:
+// each warp gathers the edge masks of 4 words and transposes them (lane t
+// receives epoch t and t + 32); the words are staged in shared memory and
+// every plane row leaves as one 128-byte line.
+constexpr int PLANE_BLOCK_WORDS = 32;
+__global__ void __launch_bounds__(256) k_inc_planes(
+    const uint32_t* __restrict__ inc_eidx, const uint8_t* __restrict__ inc_up, int64_t n_inc,
+    int64_t W, int32_t ne, const unsigned long long* __restrict__ edge_fire,
+    const unsigned long long* __restrict__ edge_neg_lo,
+    const unsigned long long* __restrict__ edge_neg_hi, uint32_t* __restrict__ fplane,
+    uint32_t* __restrict__ nplane0, uint32_t* __restrict__ nplane1) {
+  __shared__ uint32_t sbuf[3][64][PLANE_BLOCK_WORDS + 1];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t w0 = (int64_t)blockIdx.x * PLANE_BLOCK_WORDS;
+  constexpr int J = PLANE_BLOCK_WORDS / 8;
+  uint32_t e[J];
+  bool up[J];
+#pragma unroll
+  for (int j = 0; j < J; ++j) {
+    const int64_t p = ((w0 + wid * J + j) << 5) + lane;
+    const bool ok = p < n_inc;
+    e[j] = ok ? inc_eidx[p] : 0xffffffffu;
+    up[j] = ok && inc_up[p];
+  }
+  unsigned long long fm[J], g0[J], g1[J];
+#pragma unroll
+  for (int j = 0; j < J; ++j) {
+    fm[j] = e[j] != 0xffffffffu ? edge_fire[e[j]] : 0ull;
+    g0[j] = up[j] ? edge_neg_lo[e[j]] : 0ull;
+    g1[j] = up[j] ? edge_neg_hi[e[j]] : 0ull;
+  }
+#pragma unroll
+  for (int j = 0; j < J; ++j) {
+    const int col = wid * J + j;
+    sbuf[0][lane][col] = warp_transpose32((uint32_t)fm[j], lane);
+    sbuf[0][lane + 32][col] = warp_transpose32((uint32_t)(fm[j] >> 32), lane);
+    sbuf[1][lane][col] = warp_transpose32((uint32_t)g0[j], lane);
+    sbuf[1][lane + 32][col] = warp_transpose32((uint32_t)(g0[j] >> 32), lane);
+    sbuf[2][lane][col] = warp_transpose32((uint32_t)g1[j], lane);
+    sbuf[2][lane + 32][col] = warp_transpose32((uint32_t)(g1[j] >> 32), lane);
+  }
+  __syncthreads();
+  const int64_t w = w0 + lane;
+  if (w >= W) return;
+  for (int r = wid; r < 3 * ne; r += 8) {
+    const int kind = r / ne, t = r - kind * ne;
+    uint32_t* dst = kind == 0 ? fplane : kind == 1 ? nplane0 : nplane1;
+    dst[(int64_t)t * W + w] = sbuf[kind][t][lane];
+  }
+}
+
+// Words [wb, we) of a tile's entries [P0, P1) with the bits outside masked.
+__device__ __forceinline__ uint32_t tile_word(const uint32_t* __restrict__ plane, int64_t w,
+                                              int64_t wb, int64_t we, uint32_t lo_mask,
+                                              uint32_t hi_mask) {
+  if (w >= we) return 0u;
+  uint32_t x = plane[w];
+  if (w == wb) x &= lo_mask;
+  if (w == we - 1) x &= hi_mask;
+  return x;
+}
+
+// Count pass from the fire planes: warp per tile, fired entries per epoch.
+__global__ void k_plane_count(const int64_t* __restrict__ inc_ptr, int64_t n, int64_t ntiles,
+                              int64_t W, int32_t ne, const uint32_t* __restrict__ fplane,
+                              int32_t* __restrict__ counts) {
+  const int lane = threadIdx.x & 31;
+  const int64_t tile = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (tile >= ntiles) return;
+  const int64_t v0 = tile * TILE;
+  const int nt = (int)min((int64_t)TILE, n - v0);
+  const int64_t P0 = inc_ptr[v0], P1 = inc_ptr[v0 + nt];
+  const int64_t wb = P0 >> 5, we = P1 > P0 ? ((P1 - 1) >> 5) + 1 : wb;
+  const uint32_t lo_mask = ~0u << (P0 & 31);
+  const uint32_t hi_mask = ~0u >> (31 - (int)((P1 - 1) & 31));
+  for (int32_t t = 0; t < ne; ++t) {
+    const uint32_t* pl = fplane + (int64_t)t * W;
+    int c = 0;
+    for (int64_t w = wb + lane; w < we; w += 32) c += __popc(tile_word(pl, w, wb, we, lo_mask, hi_mask));
+    c = __reduce_add_sync(0xffffffffu, c);
+    if (lane == 0) counts[(int64_t)t * ntiles + tile] = c;
+  }
+}
+
+// Position of the r-th (from 0) set bit of m; some lane index for r >= popc(m).
+__device__ __forceinline__ int nth_set_bit(uint32_t m, int r) {
+  int pos = 0;
+#pragma unroll
+  for (int w = 16; w >= 1; w >>= 1) {
+    const int c = __popc(m & ((1u << w) - 1u));
+    if (c <= r) {
+      r -= c;
+      m >>= w;
+      pos += w;
+    }
+  }
+  return pos;
+}
+
+// Fill pass from the planes (n_epochs <= 64, at most 3 negatives per edge and
+// epoch): warp per tile, epochs in order. For each epoch the tile's plane
+// words are taken 64 at a time; their fire events are spread over the lanes
+// in incidence order, so consecutive lanes write consecutive records of the
+// (epoch, tile) segment and each segment is written front to back. A lane
+// whose event draws negatives also draws the first one (counter j = 0).
+struct PlaneFillSmem {
+  uint32_t f[64], n0[64], n1[64];
+  int32_t ex[65];  // exclusive prefix of the words' event counts
+};
+
+__global__ void __launch_bounds__(128) k_plane_fill(
+    const int64_t* __restrict__ inc_ptr, const uint32_t* __restrict__ inc_other,
+    const int64_t* __restrict__ eidx_base, int64_t n, int64_t ntiles, int64_t W, int32_t ne,
+    const uint32_t* __restrict__ fplane, const uint32_t* __restrict__ nplane0,
+    const uint32_t* __restrict__ nplane1, const int64_t* __restrict__ tile_off,
+    const uint32_t* __restrict__ prob_of_node, const ProbInfo* __restrict__ prob,
+    uint64_t seed, uint32_t* __restrict__ rec_other, uint32_t* __restrict__ rec_aux,
+    uint32_t* __restrict__ rec_neg0, uint32_t* __restrict__ rec_eidx) {
+  __shared__ PlaneFillSmem sm_all[4];
+  PlaneFillSmem& sm = sm_all[threadIdx.x >> 5];
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int64_t tile = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (tile >= ntiles) return;
+  const int64_t v0 = tile * TILE;
+  const int nt = (int)min((int64_t)TILE, n - v0);
+  const int64_t pbl = inc_ptr[v0 + min(lane, nt)];  // lanes >= nt hold the end
+  const int64_t ebl = (lane < nt) ? eidx_base[v0 + lane] : 0;
+  const int64_t P0 = __shfl_sync(FULL, pbl, 0);
+  const int64_t P1 = inc_ptr[v0 + nt];
+  if (P1 <= P0) return;
+  const int64_t wb = P0 >> 5, we = ((P1 - 1) >> 5) + 1;
+  const uint32_t lo_mask = ~0u << (P0 & 31);
+  const uint32_t hi_mask = ~0u >> (31 - (int)((P1 - 1) & 31));
+  const uint32_t n_total = (uint32_t)n;
+  for (int32_t t = 0; t < ne; ++t) {
+    const int64_t po = (int64_t)t * W;
+    int64_t cur = tile_off[(int64_t)t * ntiles + tile];
+    for (int64_t ws = wb; ws < we; ws += 64) {
+      const uint32_t xa = tile_word(fplane + po, ws + lane, wb, we, lo_mask, hi_mask);
+      const uint32_t xb = tile_word(fplane + po, ws + 32 + lane, wb, we, lo_mask, hi_mask);
+      const uint32_t na0 = xa ? nplane0[po + ws + lane] : 0u;
+      const uint32_t na1 = xa ? nplane1[po + ws + lane] : 0u;
+      const uint32_t nb0 = xb ? nplane0[po + ws + 32 + lane] : 0u;
+      const uint32_t nb1 = xb ? nplane1[po + ws + 32 + lane] : 0u;
+      const int ca = __popc(xa), cb = __popc(xb);
+      int ia = ca, ib = cb;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int ya = __shfl_up_sync(FULL, ia, o), yb = __shfl_up_sync(FULL, ib, o);
+        if (lane >= o) {
+          ia += ya;
+          ib += yb;
+        }
+      }
+      const int tot_a = __shfl_sync(FULL, ia, 31);
+      const int total = tot_a + __shfl_sync(FULL, ib, 31);
+      if (total == 0) continue;
+      __syncwarp();  // readers of the previous window are done
+      sm.f[lane] = xa;
+      sm.f[lane + 32] = xb;
+      sm.n0[lane] = na0;
+      sm.n0[lane + 32] = nb0;
+      sm.n1[lane] = na1;
+      sm.n1[lane + 32] = nb1;
+      sm.ex[lane] = ia - ca;
+      sm.ex[lane + 32] = tot_a + ib - cb;
+      __syncwarp();
+      for (int kb = 0; kb < total; kb += 32) {
+        const int k = kb + lane;
+        int wi = 0;  // word of event k: last wi with ex[wi] <= k
+#pragma unroll
+        for (int step = 32; step >= 1; step >>= 1)
+          if (wi + step < 64 && sm.ex[wi + step] <= k) wi += step;
+        const int r = k - sm.ex[wi];
+        const uint32_t fw = sm.f[wi];
+        const int u = nth_set_bit(fw, r);  // in range for any r
+        const int64_t p = ((ws + wi) << 5) + u;
+        int node = 0;
+#pragma unroll
+        for (int step = 16; step >= 1; step >>= 1) {
+          const int64_t st = __shfl_sync(FULL, pbl, node + step);
+          if (node + step < nt && st <= p) node += step;
+        }
+        const int64_t eb = __shfl_sync(FULL, ebl, node);
+        if (k < total) {
+          const uint32_t eidx = (uint32_t)(p + eb);
+          const uint32_t nn = ((sm.n0[wi] >> u) & 1u) | (((sm.n1[wi] >> u) & 1u) << 1);
+          uint32_t neg0 = 0;
+          if (nn) {
+            uint32_t nb = 0, np = n_total;
+            uint64_t sd = seed;
+            if (prob_of_node) {
+              const ProbInfo pi = prob[prob_of_node[v0 + node]];
+              nb = pi.node_base;
+              np = pi.n;
+              sd = pi.seed;
+            }
+            neg0 = nb + negative_draw(sd, 0u, (uint32_t)t, eidx, np);
+          }
+          const int64_t q = cur + k;
+          rec_other[q] = inc_other[p];
+          rec_aux[q] = (uint32_t)node | (nn << 5);
+          rec_neg0[q] = neg0;
+          if (rec_eidx) rec_eidx[q] = eidx;
+        }
+      }
+      cur += total;
+    }
+  }
+}
+
 // Count pass: warp per tile; each lane runs the epochs-per-sample recurrence
 // of one incidence entry over all epochs; per-epoch fired counts of the tile
 // accumulate in shared memory (lane 0), and the largest negative count is
-// reduced into *max_neg.
+// reduced into *max_neg. With fire_mask != NULL (n_epochs <= 64) each entry's
+// fired epochs (bit t) and epochs with a negative (bit t) are stored too.
 __global__ void k_sched_count(const int64_t* __restrict__ inc_ptr,
                               const float* __restrict__ inc_ps,
                               const uint8_t* __restrict__ inc_up, int64_t n,
                               int64_t ntiles, int32_t ne, float neg_factor,
                               int32_t* __restrict__ counts,
-                              unsigned long long* __restrict__ max_neg) {
+                              unsigned long long* __restrict__ max_neg,
+                              unsigned long long* __restrict__ fire_mask,
+                              unsigned long long* __restrict__ neg_mask) {
   extern __shared__ int32_t cnt_all[];
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -756,27 +1050,32 @@ __global__ void k_sched_count(const int64_t* __restrict__ inc_ptr,
   const int64_t v0 = tile * TILE;
   const int nt = (int)min((int64_t)TILE, n - v0);
   const int64_t P0 = inc_ptr[v0], P1 = inc_ptr[v0 + nt];
-  unsigned long long mx = 0;
+  float mx = 0.0f;
   for (int64_t base = P0 & ~(int64_t)31; base < P1; base += 32) {
     const int64_t p = base + lane;
     const bool valid = p >= P0 && p < P1;
     Sched sc;
     sc.init(valid ? inc_ps[p] : 3.0e38f, neg_factor, valid && inc_up[p]);
+    unsigned long long fm = 0, nm = 0;
     for (int32_t t = 0; t < ne; ++t) {
-      uint64_t nn = 0;
-      const bool f = valid && sc.step((float)t, &nn);
-      if (nn > mx) mx = nn;
+      float c = 0.0f;
+      const bool f = valid && sc.stepf((float)t, &c);
+      mx = fmaxf(mx, c);
+      if (f) fm |= 1ull << (t & 63);
+      if (c > 0.0f) nm |= 1ull << (t & 63);
       const uint32_t bal = __ballot_sync(FULL, f);
       if (lane == 0) cnt[t] += __popc(bal);
+    }
+    if (fire_mask && valid) {
+      fire_mask[p] = fm;
+      neg_mask[p] = nm;
     }
   }
   __syncwarp();
   for (int32_t t = lane; t < ne; t += 32) counts[(int64_t)t * ntiles + tile] = cnt[t];
-  for (int o = 16; o > 0; o >>= 1) {
-    const unsigned long long y = __shfl_xor_sync(FULL, mx, o);
-    mx = y > mx ? y : mx;
-  }
-  if (lane == 0 && mx) atomicMax(max_neg, mx);
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, o));
+  if (lane == 0 && mx > 0.0f)
+    atomicMax(max_neg, mx >= 1.8446744e19f ? ~0ull : (unsigned long long)mx);
 }
 
 // Fill pass: the same recurrence; fired entries are written as records at
@@ -1203,6 +1502,7 @@ void add_counts(const int32_t* a, const int32_t* b, int32_t* out, int64_t n,
 // exceeds the shared-memory cursors, or when the records would take more than
 // half of the free device memory (unless EVOC_EPOCH_PATH=records).
 static bool build_records(evoc_plan* pl, const float* inc_ps, const uint8_t* inc_up,
+                          const uint32_t* inc_eidx, const float* e_ps, int64_t U,
                           float neg_factor) {
   cudaStream_t s = pl->ctx->stream;
   const int32_t ne = pl->params.n_epochs;
@@ -1216,6 +1516,7 @@ static bool build_records(evoc_plan* pl, const float* inc_ps, const uint8_t* inc
       1, std::min<size_t>(4, (200 * 1024) / ((size_t)ne * sizeof(int64_t))));
   const unsigned grid = (unsigned)((pl->ntiles + wpb - 1) / wpb);
   const int64_t cells = (int64_t)ne * pl->ntiles;
+  StageTrace trace(s);
   DevBuf<int32_t> counts(cells, s);
   DevBuf<unsigned long long> mx(1, s);
   EVOC_CUDA(cudaMemsetAsync(mx.get(), 0, sizeof(unsigned long long), s));
@@ -1223,12 +1524,47 @@ static bool build_records(evoc_plan* pl, const float* inc_ps, const uint8_t* inc
   if (csmem > 48 * 1024)
     EVOC_CUDA(cudaFuncSetAttribute((const void*)k_sched_count,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem));
-  k_sched_count<<<grid, 32 * wpb, csmem, s>>>(pl->inc_ptr.get(), inc_ps, inc_up, n,
-                                              pl->ntiles, ne, neg_factor, counts.get(),
-                                              mx.get());
+  // n_epochs <= 64: the recurrence runs once per edge into bit masks, and
+  // the count and fill passes read masks; otherwise both passes run it.
+  const bool use_masks = ne <= 64;
+  DevBuf<unsigned long long> efire, eneg_lo, eneg_hi;
+  DevBuf<uint32_t> fpl, npl0, npl1;
+  int64_t planes_w = 0;
+  if (use_masks) {
+    efire.alloc(U, s);
+    eneg_lo.alloc(U, s);
+    eneg_hi.alloc(U, s);
+    trace.mark("alloc masks");
+    k_edge_sched<<<blocks_for(U), 256, 0, s>>>(e_ps, U, ne, neg_factor, efire.get(),
+                                               eneg_lo.get(), eneg_hi.get(), mx.get());
+    EVOC_CHECK_LAUNCH();
+    trace.mark("edge schedule");
+    planes_w = (pl->n_inc + 31) / 32;
+    const int64_t pw = planes_w * ne;
+    fpl.alloc(pw, s);
+    npl0.alloc(pw, s);
+    npl1.alloc(pw, s);
+    k_inc_planes<<<(unsigned)((planes_w + PLANE_BLOCK_WORDS - 1) / PLANE_BLOCK_WORDS), 256, 0,
+                   s>>>(
+        inc_eidx, inc_up, pl->n_inc, planes_w, ne, efire.get(), eneg_lo.get(),
+        eneg_hi.get(), fpl.get(), npl0.get(), npl1.get());
+    EVOC_CHECK_LAUNCH();
+    efire.release();
+    eneg_lo.release();
+    eneg_hi.release();
+    trace.mark("incidence planes");
+    k_plane_count<<<blocks_for(pl->ntiles * 32), 256, 0, s>>>(
+        pl->inc_ptr.get(), n, pl->ntiles, planes_w, ne, fpl.get(), counts.get());
+  } else {
+    k_sched_count<<<grid, 32 * wpb, csmem, s>>>(pl->inc_ptr.get(), inc_ps, inc_up, n,
+                                                pl->ntiles, ne, neg_factor, counts.get(),
+                                                mx.get(), nullptr, nullptr);
+  }
   EVOC_CHECK_LAUNCH();
+  trace.mark("count pass");
   DevBuf<int64_t> off(cells + 1, s);
   exclusive_scan_i32_to_i64(counts.get(), off.get(), cells, s);
+  trace.mark("offset scan");
   int64_t total = 0;
   unsigned long long maxneg = 0;
   EVOC_CUDA(cudaMemcpyAsync(&total, off.get() + cells, sizeof(int64_t),
@@ -1245,10 +1581,21 @@ static bool build_records(evoc_plan* pl, const float* inc_ps, const uint8_t* inc
   const double need = (need_eidx ? 16.0 : 12.0) * (double)total;
   if (!force_rec && need > 0.5 * (double)free_b) return false;
   pl->max_neg = maxneg;
+  trace.mark("sync + memgetinfo");
   pl->rec_other.alloc(total, s);
   pl->rec_aux.alloc(total, s);
   pl->rec_neg0.alloc(total, s);
   if (need_eidx) pl->rec_eidx.alloc(total, s);
+  trace.mark("alloc records");
+  if (use_masks && maxneg <= 3) {
+    k_plane_fill<<<(unsigned)((pl->ntiles + 3) / 4), 128, 0, s>>>(
+        pl->inc_ptr.get(), pl->inc_other.get(), pl->eidx_base.get(), n, pl->ntiles, planes_w,
+        ne, fpl.get(), npl0.get(), npl1.get(), off.get(),
+        pl->n_problems > 1 ? pl->prob_of_node.get() : nullptr,
+        pl->n_problems > 1 ? pl->prob.get() : nullptr, pl->seeds.empty() ? 0 : pl->seeds[0],
+        pl->rec_other.get(), pl->rec_aux.get(), pl->rec_neg0.get(),
+        need_eidx ? pl->rec_eidx.get() : nullptr);
+  } else {
   const size_t fsmem = (size_t)wpb * ne * sizeof(int64_t);
   if (fsmem > 48 * 1024)
     EVOC_CUDA(cudaFuncSetAttribute((const void*)k_sched_fill,
@@ -1260,7 +1607,9 @@ static bool build_records(evoc_plan* pl, const float* inc_ps, const uint8_t* inc
       pl->n_problems > 1 ? pl->prob.get() : nullptr, pl->seeds.empty() ? 0 : pl->seeds[0],
       pl->rec_other.get(), pl->rec_aux.get(), pl->rec_neg0.get(),
       need_eidx ? pl->rec_eidx.get() : nullptr);
+  }
   EVOC_CHECK_LAUNCH();
+  trace.mark("fill pass");
   // fired edges per epoch = records of the epoch / 2 (both copies fire)
   std::vector<int64_t> h(ne + 1);
   for (int32_t t = 0; t <= ne; ++t)
@@ -1387,6 +1736,8 @@ evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
   }
   const uint32_t* pon = pl->n_problems > 1 ? pl->prob_of_node.get() : nullptr;
 
+  StageTrace trace(s);
+  trace.mark("graph concat");
   // upper / lower counts and the edge list
   DevBuf<int32_t> ucnt(n, s), lcnt(n, s);
   k_row_counts<<<blocks_for(n * 32), 256, 0, s>>>(indptr, indices, n, ucnt.get(),
@@ -1409,6 +1760,7 @@ evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
     throw Error(EVOC_ERR_UNSUPPORTED, "more than 2^32-2 edges");
   pl->has_edges = true;
 
+  trace.mark("row counts + scan");
   DevBuf<float> e_w(U, s), e_ps(U, s);
   DevBuf<uint32_t> e_dst(U, s), e_src(U, s);
   DevBuf<int32_t> max_w(pl->n_problems, s);
@@ -1438,6 +1790,7 @@ evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
   e_dst.release();
   e_src.release();
 
+  trace.mark("edges + transpose");
   // incidence lists
   DevBuf<int32_t> deg(n, s);
   add_counts(ucnt.get(), lcnt.get(), deg.get(), n, s);
@@ -1460,19 +1813,22 @@ evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
   pl->eidx_base.alloc(n, s);
   DevBuf<float> inc_ps(n_inc, s);
   DevBuf<uint8_t> inc_up(n_inc, s);
+  DevBuf<uint32_t> inc_eidx(n_inc, s);
   k_inc_fill<<<blocks_for(n * 32), 256, 0, s>>>(
       indptr, indices, weights, n, uptr.get(), lcnt.get(), lptr.get(),
       lower.get(), e_ps.get(), pl->inc_ptr.get(), pon, max_w.get(), ebase.get(),
-      pl->inc_other.get(), inc_ps.get(), inc_up.get(), pl->eidx_base.get());
+      pl->inc_other.get(), inc_ps.get(), inc_up.get(), pl->eidx_base.get(),
+      inc_eidx.get());
   EVOC_CHECK_LAUNCH();
   lower.release();
   lptr.release();
-  e_ps.release();
 
+  trace.mark("incidence lists");
   // schedule: per-epoch records (fast path) or bit planes (fallback)
   const float neg_factor = 1.5f / params.negative_sample_rate;  // embedding.rs:116
   pl->W = (n_inc + 31) / 32;
-  if (ne > 0 && !build_records(pl.get(), inc_ps.get(), inc_up.get(), neg_factor)) {
+  if (ne > 0 && !build_records(pl.get(), inc_ps.get(), inc_up.get(), inc_eidx.get(),
+                               e_ps.get(), U, neg_factor)) {
     DevBuf<unsigned long long> mx(1, s), st(2 * ne, s);
     EVOC_CUDA(cudaMemsetAsync(mx.get(), 0, sizeof(unsigned long long), s));
     EVOC_CUDA(cudaMemsetAsync(st.get(), 0, st.bytes(), s));
@@ -1510,9 +1866,11 @@ evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
     EVOC_CHECK_LAUNCH();
   }
 
+  trace.mark("schedule");
   pl->m.alloc(n * pl->dimp, s);
   pl->v.alloc(n * pl->dimp, s);
   pl->lanes = default_wpb();
+  trace.mark("moments");
   EVOC_CUDA(cudaStreamSynchronize(s));
   return pl.release();
 }

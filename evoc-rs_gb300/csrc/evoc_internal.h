@@ -4,9 +4,12 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/evoc_gb300.h"
@@ -86,6 +89,43 @@ struct DevBuf {
   }
   size_t bytes() const { return count * sizeof(T); }
   T* get() const { return ptr; }
+};
+
+// Optional stage timing (EVOC_TRACE=1 prints to stderr):
+// CUDA events between stages (device time) and the host clock.
+struct StageTrace {
+  bool on = false;
+  cudaStream_t s = nullptr;
+  std::vector<std::pair<std::string, cudaEvent_t>> ev;
+  std::vector<double> host;
+  explicit StageTrace(cudaStream_t st) : s(st) {
+    const char* e = std::getenv("EVOC_TRACE");
+    on = e && e[0] == '1';
+    mark("start");
+  }
+  static double now_ms() {
+    return std::chrono::duration<double, std::milli>(
+               std::chrono::steady_clock::now().time_since_epoch()).count();
+  }
+  void mark(const char* name) {
+    if (!on) return;
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) { on = false; return; }
+    cudaEventRecord(e, s);
+    ev.emplace_back(name, e);
+    host.push_back(now_ms());
+  }
+  ~StageTrace() {
+    if (!on) return;
+    cudaEventSynchronize(ev.back().second);
+    for (size_t i = 1; i < ev.size(); ++i) {
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, ev[i - 1].second, ev[i].second);
+      std::fprintf(stderr, "[evoc trace] %-22s device %8.3f ms  host %8.3f ms\n",
+                   ev[i].first.c_str(), ms, host[i] - host[i - 1]);
+    }
+    for (auto& x : ev) cudaEventDestroy(x.second);
+  }
 };
 
 }  // namespace evoc

@@ -374,6 +374,7 @@ void fuzzy_set_device(evoc_ctx* ctx, const uint32_t* d_idx,
   if (k <= 0) throw Error(EVOC_ERR_INVALID_ARGUMENT, "k must be positive");
   if (n >= (int64_t)PAD) throw Error(EVOC_ERR_UNSUPPORTED, "n must be < 2^32-1");
 
+  StageTrace trace(s);
   DevBuf<int32_t> row_len(n, s);
   {
     const int64_t threads = n * 32;
@@ -382,6 +383,7 @@ void fuzzy_set_device(evoc_ctx* ctx, const uint32_t* d_idx,
     EVOC_CHECK_LAUNCH();
   }
   check_status(ctx, "fuzzy set");
+  trace.mark("row lengths");
 
   // k = effective_n_neighbors.to_usize().unwrap_or(knn_dists[0].len())
   // (fuzzy_graph.rs:284-286)
@@ -406,6 +408,7 @@ void fuzzy_set_device(evoc_ctx* ctx, const uint32_t* d_idx,
   smooth_knn_device(ctx, d_dist, row_len.get(), n, k, kk, 1.0f, 64, d_sig,
                     d_rho, wts.get(), nullptr);
   check_status(ctx, "fuzzy set");
+  trace.mark("smooth knn + weights");
 
   out->ctx = ctx;
   out->n = n;
@@ -451,6 +454,7 @@ void fuzzy_set_device(evoc_ctx* ctx, const uint32_t* d_idx,
       fcnt.get(), indeg.get());
   EVOC_CHECK_LAUNCH();
   wts.release();
+  trace.mark("forward rows");
 
   DevBuf<int64_t> fptr(n + 1, s), bptr(n + 1, s);
   exclusive_scan_i32_to_i64(fcnt.get(), fptr.get(), n, s);
@@ -472,6 +476,7 @@ void fuzzy_set_device(evoc_ctx* ctx, const uint32_t* d_idx,
   }
   keys.release();
   fptr.release();
+  trace.mark("transpose");
 
   DevBuf<int32_t> ucnt(n, s);
   k_union<false><<<row_blocks, 256, 0, s>>>(fcol.get(), fw.get(), fcnt.get(),
@@ -487,6 +492,7 @@ void fuzzy_set_device(evoc_ctx* ctx, const uint32_t* d_idx,
   out->nnz = nnz;
   out->indices.alloc(nnz, s);
   out->weights.alloc(nnz, s);
+  trace.mark("union count");
   k_union<true><<<row_blocks, 256, 0, s>>>(fcol.get(), fw.get(), fcnt.get(),
                                            bptr.get(), vals.get(), n, k,
                                            nullptr, out->indptr.get(),
@@ -494,6 +500,7 @@ void fuzzy_set_device(evoc_ctx* ctx, const uint32_t* d_idx,
                                            out->weights.get());
   EVOC_CHECK_LAUNCH();
   out->canonical = true;
+  trace.mark("union write");
   EVOC_CUDA(cudaStreamSynchronize(s));
 }
 

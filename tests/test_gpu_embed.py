@@ -73,7 +73,7 @@ def test_blobs_full_run_vs_oracle(ctx, oracle, blobs_graph):
 
 
 @pytest.mark.parametrize("dim,neg_rate,n_epochs", [(2, 1.0, 20), (8, 3.7, 15), (16, 0.0, 10),
-                                                  (5, 1.0, 12), (12, 0.5, 8)])
+                                                  (5, 1.0, 12), (12, 0.5, 8), (4, 1.0, 80)])
 def test_blobs_dims_and_rates(ctx, oracle, blobs_graph, dim, neg_rate, n_epochs):
     import evoc_gb300 as E
     g, (ip, ix, w), _ = blobs_graph
