@@ -85,6 +85,7 @@ struct evoc_plan {
   int64_t ntiles = 0;
   int64_t n_records = 0;
   evoc::DevBuf<int64_t> tile_off;
+  evoc::DevBuf<uint32_t> tile_order;  // tiles by descending record count (launch order)
   evoc::DevBuf<uint32_t> rec_other, rec_aux, rec_neg0;
   evoc::DevBuf<uint32_t> rec_eidx;  // only when an edge draws > 1 negative
   bool stats_done = false;
@@ -457,6 +458,7 @@ struct EpochArgs {
   const uint32_t* prob_of_node;
   const ProbInfo* prob;
   const int64_t* tile_off;  // record offsets of this epoch (records path)
+  const uint32_t* tile_order;  // records path: tiles in launch order, heaviest first
   const uint32_t* rec_other;
   const uint32_t* rec_aux;
   const uint32_t* rec_neg0;
@@ -1235,9 +1237,10 @@ __global__ void __launch_bounds__(128) k_epoch_rec(EpochArgs a) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   RecSmem<DIMP>& sm = reinterpret_cast<RecSmem<DIMP>*>(smem_raw)[threadIdx.x >> 5];
-  const int64_t tile = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int64_t slot = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (slot * TILE >= (int64_t)a.n_total) return;  // whole warp
+  const int64_t tile = a.tile_order[slot];
   const int64_t v0 = tile * TILE;
-  if (v0 >= (int64_t)a.n_total) return;  // whole warp
   const int nt = (int)min((int64_t)TILE, (int64_t)a.n_total - v0);
   const bool has_node = lane < nt;
   const int64_t r0 = a.tile_off[tile], r1 = a.tile_off[tile + 1];
@@ -1468,12 +1471,14 @@ void launch_epoch(evoc_plan* pl, int32_t t, const float* e_cur, float* e_next,
   a.one_m_b1 = pl->one_m_b1;
   a.one_m_b2 = pl->one_m_b2;
   a.tile_off = nullptr;
+  a.tile_order = nullptr;
   a.rec_other = a.rec_aux = a.rec_neg0 = a.rec_eidx = nullptr;
   const int wpb = pl->lanes;
   const int64_t tiles = (pl->n + TILE - 1) / TILE;
   const unsigned grid = (unsigned)((tiles + wpb - 1) / wpb);
   if (pl->use_records) {
     a.tile_off = pl->tile_off.get() + (size_t)t * pl->ntiles;
+    a.tile_order = pl->tile_order.get();
     a.rec_other = pl->rec_other.get();
     a.rec_aux = pl->rec_aux.get();
     a.rec_neg0 = pl->rec_neg0.get();
@@ -1496,6 +1501,25 @@ void concat_graph(const evoc_graph* g, int64_t node_off, int64_t entry_off,
 void fill_eidx_src(uint2* out, const uint32_t* e_src, int64_t U, cudaStream_t s);
 void add_counts(const int32_t* a, const int32_t* b, int32_t* out, int64_t n,
                 cudaStream_t s);
+
+// Launch order of the records kernels: sort key per tile = ~(its records over
+// all epochs), so that an ascending sort puts the heaviest tiles (hub nodes)
+// first and their long serial sums overlap the many light tiles.
+__global__ void k_tile_weight(const int32_t* __restrict__ counts, int64_t ntiles, int32_t ne,
+                              uint32_t* __restrict__ keys, uint2* __restrict__ vals) {
+  const int64_t tile = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (tile >= ntiles) return;
+  uint64_t tot = 0;
+  for (int32_t t = 0; t < ne; ++t) tot += (uint32_t)counts[(int64_t)t * ntiles + tile];
+  keys[tile] = ~(uint32_t)min(tot, (uint64_t)0xffffffffu);
+  vals[tile] = make_uint2((uint32_t)tile, 0u);
+}
+
+__global__ void k_tile_order(const uint2* __restrict__ vals, int64_t ntiles,
+                             uint32_t* __restrict__ order) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < ntiles) order[i] = vals[i].x;
+}
 
 // Records path of the schedule set-up: count pass, scan, fill pass. Returns
 // false (nothing built) when EVOC_EPOCH_PATH=scan, when the epoch count
@@ -1564,7 +1588,19 @@ static bool build_records(evoc_plan* pl, const float* inc_ps, const uint8_t* inc
   trace.mark("count pass");
   DevBuf<int64_t> off(cells + 1, s);
   exclusive_scan_i32_to_i64(counts.get(), off.get(), cells, s);
-  trace.mark("offset scan");
+  {
+    DevBuf<uint32_t> keys(pl->ntiles, s);
+    DevBuf<uint2> vals(pl->ntiles, s);
+    k_tile_weight<<<blocks_for(pl->ntiles), 256, 0, s>>>(counts.get(), pl->ntiles, ne,
+                                                          keys.get(), vals.get());
+    EVOC_CHECK_LAUNCH();
+    radix_sort_pairs(keys.get(), vals.get(), pl->ntiles, 32, s);
+    pl->tile_order.alloc(pl->ntiles, s);
+    k_tile_order<<<blocks_for(pl->ntiles), 256, 0, s>>>(vals.get(), pl->ntiles,
+                                                         pl->tile_order.get());
+    EVOC_CHECK_LAUNCH();
+  }
+  trace.mark("offset scan + tile order");
   int64_t total = 0;
   unsigned long long maxneg = 0;
   EVOC_CUDA(cudaMemcpyAsync(&total, off.get() + cells, sizeof(int64_t),
