@@ -136,10 +136,10 @@ def make_workload(name: str, n_override: int | None):
 
 
 def profiled_traffic() -> tuple[float | None, str | None]:
-    """DRAM bytes per k_epoch_rec launch at 2M points, from the committed ncu
+    """DRAM bytes per k_epoch_slot launch at 2M points, from the committed ncu
     summary (dram__bytes_read.sum + dram__bytes_write.sum, scaled from the
-    captured size by the fired entries); None when no summary exists."""
-    f = ROOT / "profiles" / "k_epoch_rec_hierarchical.md"
+    captured size by the slots); None when no summary exists."""
+    f = ROOT / "profiles" / "k_epoch_slot_hierarchical.md"
     if not f.exists():
         return None, None
     for line in f.read_text().splitlines():
@@ -151,16 +151,16 @@ def profiled_traffic() -> tuple[float | None, str | None]:
 def algorithmic_hbm_bytes(n: int, info: dict, dimp: int, stats: np.ndarray) -> np.ndarray:
     """Per-epoch bytes the epoch kernel must move to/from HBM (the partner and
     negative row gathers are served by L2 and counted separately).
-    Records path: tile offsets 8 (n/32 + 1), fired-entry records 12 per fired
-    directed entry (2 F_t), own rows read + next rows written 2 * 4 dimp n,
-    Adam moments read + written 4 * 4 dimp A_t.
+    Slots path: tile offsets 8 (n/32 + 1), tile order 4 n/32, slots 8 per
+    fired directed entry (2 F_t) and per negative sample (N_t), own rows read +
+    next rows written 2 * 4 dimp n, Adam moments read + written 4 * 4 dimp A_t.
     Bit-plane path: incidence offsets 8 (n + 1), fire + negative-count planes
     (1 + P) n_inc / 8, partner ids 4 * 2 F_t, and the same row and moment terms."""
-    F, _, A = stats[:, 0], stats[:, 1], stats[:, 2]
+    F, N, A = stats[:, 0], stats[:, 1], stats[:, 2]
     row = 4 * dimp
     common = 2 * row * n + 4 * row * A
-    if info["n_records"]:
-        return (8 * (n // 32 + 1) + 12 * 2 * F + common).astype(np.float64)
+    if info["n_slots"]:
+        return (8 * (n // 32 + 1) + 4 * (n // 32) + 8 * (2 * F + N) + common).astype(np.float64)
     return (8 * (n + 1) + (1 + info["neg_planes"]) * info["n_incidence"] / 8 + 4 * 2 * F
             + common).astype(np.float64)
 
@@ -263,15 +263,15 @@ def run_ours(args) -> dict:
     pk = peaks()
     achieved = bytes_launch / t_launch / 1e9
     traffic, traffic_src = profiled_traffic()
-    if args.workload != "hierarchical_2m" or n != 2_000_000 or not info["n_records"]:
+    if args.workload != "hierarchical_2m" or n != 2_000_000 or not info["n_slots"]:
         traffic, traffic_src = None, None
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": pk["hbm_gbs"],
                 "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4),
                 "traffic": traffic, "traffic_src": traffic_src,
                 "algorithmic_bytes_per_launch": round(bytes_launch),
-                "peak_src": pk["src"], "kernel": "k_epoch_rec",
+                "peak_src": pk["src"], "kernel": "k_epoch_slot" if info["n_slots"] else "k_epoch",
                 "launch_ms": round(t_launch * 1e3, 4), "warps_per_block": info["warps_per_block"],
-                "epoch_path": "records" if info["n_records"] else "bit-planes",
+                "epoch_path": "slots" if info["n_slots"] else "bit-planes",
                 "l2_gather_gbs": round(float(l2b[act].mean()) / t_launch / 1e9, 1)}
 
     res = {

@@ -337,9 +337,9 @@ int evoc_plan_profile_epochs(evoc_plan_t* plan, const float* d_init,
 
 int evoc_plan_info(const evoc_plan_t* plan, int64_t* n_edges,
                    int64_t* n_incidence, int32_t* neg_planes,
-                   int32_t* warps_per_block, int64_t* n_records) {
+                   int32_t* warps_per_block, int64_t* n_slots) {
   if (!plan) return EVOC_ERR_INVALID_ARGUMENT;
-  evoc::plan_info(plan, n_edges, n_incidence, neg_planes, warps_per_block, n_records);
+  evoc::plan_info(plan, n_edges, n_incidence, neg_planes, warps_per_block, n_slots);
   return EVOC_OK;
 }
 

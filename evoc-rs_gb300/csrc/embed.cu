@@ -79,15 +79,17 @@ struct evoc_plan {
   std::vector<float> lr_ad, epsc, gamma;
   float one_m_b1 = 0, one_m_b2 = 0;
   std::vector<evoc_epoch_stats_t> stats;
-  // per-epoch fired-entry records (the fast path): for epoch t and tile T,
-  // records [tile_off[t * ntiles + T], tile_off[t * ntiles + T + 1])
-  bool use_records = false;
+  // per-epoch gradient slots (the fast path): for epoch t and tile T, slots
+  // [tile_off[t * ntiles + T], tile_off[t * ntiles + T + 1]); a slot is
+  // (source row, tile-local node | 32 for a negative sample)
+  bool use_slots = false;
   int64_t ntiles = 0;
-  int64_t n_records = 0;
+  int64_t n_slots = 0;
   evoc::DevBuf<int64_t> tile_off;
-  evoc::DevBuf<uint32_t> tile_order;  // tiles by descending record count (launch order)
-  evoc::DevBuf<uint32_t> rec_other, rec_aux, rec_neg0;
-  evoc::DevBuf<uint32_t> rec_eidx;  // only when an edge draws > 1 negative
+  evoc::DevBuf<uint32_t> tile_order;  // tiles by descending slot count (launch order)
+  evoc::DevBuf<uint2> slots;
+  evoc::DevBuf<unsigned long long> work_ctr;  // per epoch
+  unsigned slot_grid = 0;                     // persistent grid of the slots kernel
   bool stats_done = false;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -457,12 +459,10 @@ struct EpochArgs {
   float* grad_out;
   const uint32_t* prob_of_node;
   const ProbInfo* prob;
-  const int64_t* tile_off;  // record offsets of this epoch (records path)
-  const uint32_t* tile_order;  // records path: tiles in launch order, heaviest first
-  const uint32_t* rec_other;
-  const uint32_t* rec_aux;
-  const uint32_t* rec_neg0;
-  const uint32_t* rec_eidx;
+  const int64_t* tile_off;     // slot offsets of this epoch (slots path)
+  const uint32_t* tile_order;  // slots path: tiles in launch order, heaviest first
+  const uint2* slots;
+  unsigned long long* work_ctr;  // slots path: next tile of this epoch (zeroed per launch)
   uint32_t n_total;
   uint32_t epoch;
   uint64_t seed;
@@ -878,10 +878,17 @@ __device__ __forceinline__ uint32_t tile_word(const uint32_t* __restrict__ plane
   return x;
 }
 
-// Count pass from the fire planes: warp per tile, fired entries per epoch.
+// Count pass from the planes: warp per tile; slots per epoch = fired entries
+// + their negatives (N0 + 2 N1). Per-epoch totals of fired entries and
+// negatives go to fired[t] / negs[t].
 __global__ void k_plane_count(const int64_t* __restrict__ inc_ptr, int64_t n, int64_t ntiles,
                               int64_t W, int32_t ne, const uint32_t* __restrict__ fplane,
-                              int32_t* __restrict__ counts) {
+                              const uint32_t* __restrict__ nplane0,
+                              const uint32_t* __restrict__ nplane1,
+                              int32_t* __restrict__ counts,
+                              unsigned long long* __restrict__ fired,
+                              unsigned long long* __restrict__ negs) {
+  const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int64_t tile = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (tile >= ntiles) return;
@@ -892,11 +899,20 @@ __global__ void k_plane_count(const int64_t* __restrict__ inc_ptr, int64_t n, in
   const uint32_t lo_mask = ~0u << (P0 & 31);
   const uint32_t hi_mask = ~0u >> (31 - (int)((P1 - 1) & 31));
   for (int32_t t = 0; t < ne; ++t) {
-    const uint32_t* pl = fplane + (int64_t)t * W;
-    int c = 0;
-    for (int64_t w = wb + lane; w < we; w += 32) c += __popc(tile_word(pl, w, wb, we, lo_mask, hi_mask));
-    c = __reduce_add_sync(0xffffffffu, c);
-    if (lane == 0) counts[(int64_t)t * ntiles + tile] = c;
+    const int64_t po = (int64_t)t * W;
+    int cf = 0, cn = 0;
+    for (int64_t w = wb + lane; w < we; w += 32) {
+      cf += __popc(tile_word(fplane + po, w, wb, we, lo_mask, hi_mask));
+      cn += __popc(tile_word(nplane0 + po, w, wb, we, lo_mask, hi_mask)) +
+            2 * __popc(tile_word(nplane1 + po, w, wb, we, lo_mask, hi_mask));
+    }
+    cf = __reduce_add_sync(FULL, cf);
+    cn = __reduce_add_sync(FULL, cn);
+    if (lane == 0) {
+      counts[(int64_t)t * ntiles + tile] = cf + cn;
+      if (cf) atomicAdd(&fired[t], (unsigned long long)cf);
+      if (cn) atomicAdd(&negs[t], (unsigned long long)cn);
+    }
   }
 }
 
@@ -918,9 +934,10 @@ __device__ __forceinline__ int nth_set_bit(uint32_t m, int r) {
 // Fill pass from the planes (n_epochs <= 64, at most 3 negatives per edge and
 // epoch): warp per tile, epochs in order. For each epoch the tile's plane
 // words are taken 64 at a time; their fire events are spread over the lanes
-// in incidence order, so consecutive lanes write consecutive records of the
-// (epoch, tile) segment and each segment is written front to back. A lane
-// whose event draws negatives also draws the first one (counter j = 0).
+// in incidence order and each writes its slots (the attraction, then its
+// negatives j = 0.., drawn here with Philox counter (j, epoch, edge)) after
+// those of the lower lanes, so every (epoch, tile) segment is written front
+// to back in the order of the reference's serial sum.
 struct PlaneFillSmem {
   uint32_t f[64], n0[64], n1[64];
   int32_t ex[65];  // exclusive prefix of the words' event counts
@@ -932,8 +949,7 @@ __global__ void __launch_bounds__(128) k_plane_fill(
     const uint32_t* __restrict__ fplane, const uint32_t* __restrict__ nplane0,
     const uint32_t* __restrict__ nplane1, const int64_t* __restrict__ tile_off,
     const uint32_t* __restrict__ prob_of_node, const ProbInfo* __restrict__ prob,
-    uint64_t seed, uint32_t* __restrict__ rec_other, uint32_t* __restrict__ rec_aux,
-    uint32_t* __restrict__ rec_neg0, uint32_t* __restrict__ rec_eidx) {
+    uint64_t seed, uint2* __restrict__ slots) {
   __shared__ PlaneFillSmem sm_all[4];
   PlaneFillSmem& sm = sm_all[threadIdx.x >> 5];
   const unsigned FULL = 0xffffffffu;
@@ -1001,11 +1017,21 @@ __global__ void __launch_bounds__(128) k_plane_fill(
           if (node + step < nt && st <= p) node += step;
         }
         const int64_t eb = __shfl_sync(FULL, ebl, node);
-        if (k < total) {
-          const uint32_t eidx = (uint32_t)(p + eb);
-          const uint32_t nn = ((sm.n0[wi] >> u) & 1u) | (((sm.n1[wi] >> u) & 1u) << 1);
-          uint32_t neg0 = 0;
+        const bool ev = k < total;
+        const uint32_t nn =
+            ev ? ((sm.n0[wi] >> u) & 1u) | (((sm.n1[wi] >> u) & 1u) << 1) : 0u;
+        const int cnt = ev ? 1 + (int)nn : 0;
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const int y = __shfl_up_sync(FULL, incl, o);
+          if (lane >= o) incl += y;
+        }
+        if (ev) {
+          int64_t q = cur + incl - cnt;
+          slots[q] = make_uint2(inc_other[p], (uint32_t)node);
           if (nn) {
+            const uint32_t eidx = (uint32_t)(p + eb);
             uint32_t nb = 0, np = n_total;
             uint64_t sd = seed;
             if (prob_of_node) {
@@ -1014,33 +1040,31 @@ __global__ void __launch_bounds__(128) k_plane_fill(
               np = pi.n;
               sd = pi.seed;
             }
-            neg0 = nb + negative_draw(sd, 0u, (uint32_t)t, eidx, np);
+            for (uint32_t j = 0; j < nn; ++j)
+              slots[++q] = make_uint2(nb + negative_draw(sd, j, (uint32_t)t, eidx, np),
+                                      (uint32_t)node | 32u);
           }
-          const int64_t q = cur + k;
-          rec_other[q] = inc_other[p];
-          rec_aux[q] = (uint32_t)node | (nn << 5);
-          rec_neg0[q] = neg0;
-          if (rec_eidx) rec_eidx[q] = eidx;
         }
+        cur += __shfl_sync(FULL, incl, 31);
       }
-      cur += total;
     }
   }
 }
 
-// Count pass: warp per tile; each lane runs the epochs-per-sample recurrence
-// of one incidence entry over all epochs; per-epoch fired counts of the tile
-// accumulate in shared memory (lane 0), and the largest negative count is
-// reduced into *max_neg. With fire_mask != NULL (n_epochs <= 64) each entry's
-// fired epochs (bit t) and epochs with a negative (bit t) are stored too.
+// Count pass (general path): warp per tile; each lane runs the
+// epochs-per-sample recurrence of one incidence entry over all epochs. Slots
+// per epoch of the tile (fired entries + their negatives, saturating at 2^30)
+// accumulate in shared memory (lane 0); per-epoch totals of fired entries
+// and negatives go to fired[t] / negs[t], and the largest negative count per
+// entry and epoch to *max_neg.
 __global__ void k_sched_count(const int64_t* __restrict__ inc_ptr,
                               const float* __restrict__ inc_ps,
                               const uint8_t* __restrict__ inc_up, int64_t n,
                               int64_t ntiles, int32_t ne, float neg_factor,
                               int32_t* __restrict__ counts,
                               unsigned long long* __restrict__ max_neg,
-                              unsigned long long* __restrict__ fire_mask,
-                              unsigned long long* __restrict__ neg_mask) {
+                              unsigned long long* __restrict__ fired,
+                              unsigned long long* __restrict__ negs) {
   extern __shared__ int32_t cnt_all[];
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -1058,19 +1082,19 @@ __global__ void k_sched_count(const int64_t* __restrict__ inc_ptr,
     const bool valid = p >= P0 && p < P1;
     Sched sc;
     sc.init(valid ? inc_ps[p] : 3.0e38f, neg_factor, valid && inc_up[p]);
-    unsigned long long fm = 0, nm = 0;
     for (int32_t t = 0; t < ne; ++t) {
       float c = 0.0f;
       const bool f = valid && sc.stepf((float)t, &c);
       mx = fmaxf(mx, c);
-      if (f) fm |= 1ull << (t & 63);
-      if (c > 0.0f) nm |= 1ull << (t & 63);
-      const uint32_t bal = __ballot_sync(FULL, f);
-      if (lane == 0) cnt[t] += __popc(bal);
-    }
-    if (fire_mask && valid) {
-      fire_mask[p] = fm;
-      neg_mask[p] = nm;
+      const uint32_t nn = c >= (float)NEG_LIMIT ? (uint32_t)NEG_LIMIT : (uint32_t)c;
+      const uint32_t nf = __popc(__ballot_sync(FULL, f));
+      if (nf == 0) continue;
+      const uint32_t ng = __reduce_add_sync(FULL, f ? nn : 0u);
+      if (lane == 0) {
+        cnt[t] = (int32_t)min((int64_t)cnt[t] + nf + ng, (int64_t)1 << 30);
+        atomicAdd(&fired[t], (unsigned long long)nf);
+        if (ng) atomicAdd(&negs[t], (unsigned long long)ng);
+      }
     }
   }
   __syncwarp();
@@ -1080,10 +1104,10 @@ __global__ void k_sched_count(const int64_t* __restrict__ inc_ptr,
     atomicMax(max_neg, mx >= 1.8446744e19f ? ~0ull : (unsigned long long)mx);
 }
 
-// Fill pass: the same recurrence; fired entries are written as records at
-// per-epoch cursors (shared memory, owned by lane 0). The first negative
-// sample of each record is drawn here (Philox, counter j = 0), so the epoch
-// loop only draws the rare further negatives.
+// Fill pass (general path): the same recurrence; each fired entry writes its
+// slots (attraction, then negatives j = 0.. drawn with Philox counter
+// (j, epoch, edge)) at the per-epoch cursor of the tile (shared memory,
+// lane 0), after the slots of the lower lanes.
 __global__ void k_sched_fill(const int64_t* __restrict__ inc_ptr,
                              const uint32_t* __restrict__ inc_other,
                              const float* __restrict__ inc_ps,
@@ -1093,10 +1117,7 @@ __global__ void k_sched_fill(const int64_t* __restrict__ inc_ptr,
                              const int64_t* __restrict__ tile_off,
                              const uint32_t* __restrict__ prob_of_node,
                              const ProbInfo* __restrict__ prob, uint64_t seed,
-                             uint32_t* __restrict__ rec_other,
-                             uint32_t* __restrict__ rec_aux,
-                             uint32_t* __restrict__ rec_neg0,
-                             uint32_t* __restrict__ rec_eidx) {
+                             uint2* __restrict__ slots) {
   extern __shared__ int64_t cursors[];
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -1111,7 +1132,6 @@ __global__ void k_sched_fill(const int64_t* __restrict__ inc_ptr,
   const int64_t P1 = inc_ptr[v0 + nt];  // nt may be 32: no lane holds the end
   if (lane == 0)
     for (int32_t t = 0; t < ne; ++t) cur[t] = tile_off[(int64_t)t * ntiles + tile];
-  const uint32_t lt = (1u << lane) - 1u;
   const uint32_t n_total = (uint32_t)n;
   for (int64_t base = P0 & ~(int64_t)31; base < P1; base += 32) {
     const int64_t p = base + lane;
@@ -1138,27 +1158,34 @@ __global__ void k_sched_fill(const int64_t* __restrict__ inc_ptr,
     for (int32_t t = 0; t < ne; ++t) {
       uint64_t nn = 0;
       const bool f = valid && sc.step((float)t, &nn);
-      const uint32_t bal = __ballot_sync(FULL, f);
-      if (bal == 0) continue;
+      if (__ballot_sync(FULL, f) == 0) continue;
+      const int64_t c = f ? 1 + (int64_t)nn : 0;
+      int64_t incl = c;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int64_t y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
+      }
       int64_t o0 = (lane == 0) ? cur[t] : 0;
       o0 = __shfl_sync(FULL, o0, 0);
       if (f) {
-        const int64_t q = o0 + __popc(bal & lt);
-        rec_other[q] = other;
-        rec_aux[q] = (uint32_t)node | ((uint32_t)nn << 5);
-        rec_neg0[q] = nn ? nb + negative_draw(sd, 0u, (uint32_t)t, eidx, np) : 0u;
-        if (rec_eidx) rec_eidx[q] = eidx;
+        int64_t q = o0 + incl - c;
+        slots[q] = make_uint2(other, (uint32_t)node);
+        for (uint64_t j = 0; j < nn; ++j)
+          slots[++q] = make_uint2(nb + negative_draw(sd, (uint32_t)j, (uint32_t)t, eidx, np),
+                                  (uint32_t)node | 32u);
       }
-      if (lane == 0) cur[t] = o0 + __popc(bal);
+      const int64_t tot = __shfl_sync(FULL, incl, 31);
+      if (lane == 0) cur[t] = o0 + tot;
     }
   }
 }
 
-// Per-epoch negatives and active nodes from the records (on request).
-__global__ void k_rec_stats(const int64_t* __restrict__ tile_off,
-                            const uint32_t* __restrict__ rec_aux, int64_t ntiles,
-                            int32_t ne, unsigned long long* __restrict__ negs,
-                            unsigned long long* __restrict__ active) {
+// Per-epoch active nodes (a fired entry, i.e. an attraction slot) from the
+// slots (on request).
+__global__ void k_slot_stats(const int64_t* __restrict__ tile_off,
+                             const uint2* __restrict__ slots, int64_t ntiles, int32_t ne,
+                             unsigned long long* __restrict__ active) {
   const unsigned FULL = 0xffffffffu;
   const int64_t tile = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
@@ -1167,41 +1194,44 @@ __global__ void k_rec_stats(const int64_t* __restrict__ tile_off,
     const int64_t r0 = tile_off[(int64_t)t * ntiles + tile];
     const int64_t r1 = tile_off[(int64_t)t * ntiles + tile + 1];
     uint32_t mask = 0;
-    unsigned long long ng = 0;
     for (int64_t r = r0 + lane; r < r1; r += 32) {
-      const uint32_t x = rec_aux[r];
-      mask |= 1u << (x & 31u);
-      ng += x >> 5;
+      const uint32_t y = slots[r].y;
+      if (!(y & 32u)) mask |= 1u << (y & 31u);
     }
     mask = __reduce_or_sync(FULL, mask);
-    for (int o = 16; o > 0; o >>= 1) ng += __shfl_xor_sync(FULL, ng, o);
-    if (lane == 0) {
-      if (ng) atomicAdd(&negs[t], ng);
-      if (mask) atomicAdd(&active[t], (unsigned long long)__popc(mask));
-    }
+    if (lane == 0 && mask) atomicAdd(&active[t], (unsigned long long)__popc(mask));
   }
 }
 
+// One epoch, slots path: persistent warps; each takes the next 32-node tile
+// in tile_order (heaviest first) from the epoch's work counter. The tile's
+// slots of the epoch come in windows of SLOT_WIN. Phase 1: each lane computes
+// the contributions of SLOT_U slots (attraction, embedding.rs:213-221, or
+// repulsion, embedding.rs:237-245, from the slot's source row and the node's
+// own row) into shared memory, all loads and gathers issued first; the first
+// slot of each node run records its position. Phase 2: the slots are
+// node-major in the order of the reference's serial sum (embedding.rs:
+// 194-253), so lane l adds the run of node v0 + l onto its running gradient
+// in registers. Then Adam (embedding.rs:256-272).
+constexpr int SLOT_WIN = 256;
+constexpr int SLOT_U = 4;
+
 template <int DIMP>
-struct alignas(16) RecSmem {
-  float rows[TILE][DIMP];       // e_cur rows of the tile's nodes
-  float S[TILE][DIMP + 1];      // running gradients
-  float contrib[CAP][DIMP + 1]; // contribution slots of the current chunk
-  uint8_t slot_node[CAP];       // tile-local node of each slot
+struct alignas(16) SlotSmem {
+  float rows[TILE][DIMP];      // e_cur rows of the tile's nodes
+  float c[SLOT_WIN][DIMP];     // contributions of the window's slots
+  int32_t start[TILE];         // first window slot of each node's run (or none)
 };
 
-// Contribution of slot k of an entry: k == 0 attraction (embedding.rs:213-221),
-// k >= 1 negative k-1 (embedding.rs:237-245); +0 for skipped terms.
+// Contribution of one slot; +0 where the reference adds nothing (adding +0
+// leaves the running sum unchanged: it starts at +0 and never becomes -0).
+// One division serves both kinds; a negative sample equal to the node itself
+// has dsq = 0 and contributes nothing, like the reference's skip.
 template <int DIMP>
-__device__ __forceinline__ void slot_value(float* __restrict__ dst, int k, bool skip,
-                                           const float (&ev)[DIMP],
-                                           const float (&row)[DIMP], float two_noise,
-                                           float gamma4) {
-  if (skip) {
-#pragma unroll
-    for (int d = 0; d < DIMP; ++d) dst[d] = 0.0f;
-    return;
-  }
+__device__ __forceinline__ void slot_contrib(float (&c)[DIMP], bool neg,
+                                             const float (&ev)[DIMP],
+                                             const float (&row)[DIMP], float two_noise,
+                                             float gamma4) {
   float diff[DIMP];
   float dsq = 0.0f;
 #pragma unroll
@@ -1209,165 +1239,116 @@ __device__ __forceinline__ void slot_value(float* __restrict__ dst, int k, bool 
     diff[d] = fsub(ev[d], row[d]);
     dsq = fadd(dsq, fmul(diff[d], diff[d]));
   }
-  if (k == 0) {
-    if (dsq >= 1e-8f) {
-      const float dist = fsqrt(dsq);
-      const float coeff = fdiv(fsub(-fmul(two_noise, dist), 2.0f),
-                               fadd(fsub(fmul(2.0f, dsq), fmul(0.5f, dist)), 1.0f));
+  const float dist = fsqrt(dsq);
+  const float num = neg ? gamma4 : fsub(-fmul(two_noise, dist), 2.0f);
+  const float den = neg ? fmul(fadd(1.0f, fmul(0.25f, dsq)), dsq)
+                        : fadd(fsub(fmul(2.0f, dsq), fmul(0.5f, dist)), 1.0f);
+  const float k = fdiv(num, den);
+  const bool on = neg ? (dsq > 0.01f) : (dsq >= 1e-8f);
 #pragma unroll
-      for (int d = 0; d < DIMP; ++d) dst[d] = fmul(coeff, diff[d]);
-      return;
-    }
-  } else if (dsq > 0.01f) {
-    const float gc = fdiv(gamma4, fmul(fadd(1.0f, fmul(0.25f, dsq)), dsq));
-#pragma unroll
-    for (int d = 0; d < DIMP; ++d) {
-      const float c = fmaxf(fmul(gc, diff[d]), -4.0f);
-      dst[d] = fminf(c, 4.0f);
-    }
-    return;
+  for (int d = 0; d < DIMP; ++d) {
+    const float x = fmul(k, diff[d]);
+    const float y = neg ? fminf(fmaxf(x, -4.0f), 4.0f) : x;
+    c[d] = on ? y : 0.0f;
   }
-#pragma unroll
-  for (int d = 0; d < DIMP; ++d) dst[d] = 0.0f;
 }
 
 template <int DIMP>
-__global__ void __launch_bounds__(128) k_epoch_rec(EpochArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP>& sm, int64_t tile,
+                                          int lane) {
   const unsigned FULL = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
-  RecSmem<DIMP>& sm = reinterpret_cast<RecSmem<DIMP>*>(smem_raw)[threadIdx.x >> 5];
-  const int64_t slot = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (slot * TILE >= (int64_t)a.n_total) return;  // whole warp
-  const int64_t tile = a.tile_order[slot];
   const int64_t v0 = tile * TILE;
   const int nt = (int)min((int64_t)TILE, (int64_t)a.n_total - v0);
-  const bool has_node = lane < nt;
-  const int64_t r0 = a.tile_off[tile], r1 = a.tile_off[tile + 1];
-  uint32_t o_n = 0, aux_n = 0, ng_n = 0, ex_n = 0;
-  if (r0 + lane < r1) {
-    o_n = __ldcs(a.rec_other + r0 + lane);
-    aux_n = __ldcs(a.rec_aux + r0 + lane);
-    ng_n = __ldcs(a.rec_neg0 + r0 + lane);
-    if (a.rec_eidx) ex_n = __ldcs(a.rec_eidx + r0 + lane);
-  }
+  const int64_t s0 = a.tile_off[tile], s1 = a.tile_off[tile + 1];
+  __syncwarp();  // the previous tile's readers of the shared rows are done
   {
     const float4* src = reinterpret_cast<const float4*>(a.e_cur + (size_t)v0 * DIMP);
     float4* dst = reinterpret_cast<float4*>(&sm.rows[0][0]);
     for (int i = lane; i < nt * (DIMP / 4); i += 32) dst[i] = __ldg(src + i);
   }
-  for (int i = lane; i < TILE * (DIMP + 1); i += 32) (&sm.S[0][0])[i] = 0.0f;
-  __syncwarp();
   const float two_noise = fmul(2.0f, a.noise);
   const float gamma4 = fmul(a.gamma, 4.0f);
-  uint32_t touched = 0;
-  int64_t r = r0;
-  int so = 0;  // slots of the first record consumed by earlier chunks
-  while (r < r1) {
-    const uint32_t o = o_n, aux = aux_n, neg0 = ng_n, exi = ex_n;
-    const bool valid = r + lane < r1;
-    const int node = (int)(aux & 31u);
-    const uint32_t nneg = aux >> 5;
-    const int k_first = (lane == 0) ? so : 0;
-    const int cc = valid ? (int)(1 + nneg) - k_first : 0;
-    int cincl = cc;
+  float g[DIMP];
 #pragma unroll
-    for (int s2 = 1; s2 < 32; s2 <<= 1) {
-      const int y = __shfl_up_sync(FULL, cincl, s2);
-      if (lane >= s2) cincl += y;
-    }
-    const int cexcl = cincl - cc;
-    const int nslots = max(0, min(cincl, CAP) - cexcl);
-    const int ndone = __popc(__ballot_sync(FULL, valid && cincl <= CAP));
-    const int used = min(__shfl_sync(FULL, cincl, 31), CAP);
-    const int cex_nd = __shfl_sync(FULL, cexcl, ndone & 31);
-    const int kf_nd = __shfl_sync(FULL, k_first, ndone & 31);
-    const int64_t rn = r + ndone;
-    if (rn + lane < r1) {  // prefetch the next chunk's records
-      o_n = __ldcs(a.rec_other + rn + lane);
-      aux_n = __ldcs(a.rec_aux + rn + lane);
-      ng_n = __ldcs(a.rec_neg0 + rn + lane);
-      if (a.rec_eidx) ex_n = __ldcs(a.rec_eidx + rn + lane);
-    }
-    touched |= __reduce_or_sync(FULL, valid ? (1u << node) : 0u);
-    if (nslots > 0) {
-      const uint32_t vg = (uint32_t)(v0 + node);
-      float ev[DIMP];
+  for (int d = 0; d < DIMP; ++d) g[d] = 0.0f;
+  uint32_t act_mask = 0;
+  for (int64_t w0 = s0; w0 < s1; w0 += SLOT_WIN) {
+    const int wn = (int)min((int64_t)SLOT_WIN, s1 - w0);
+    sm.start[lane] = SLOT_WIN;  // none
+    __syncwarp();
+    int carry = -1;  // node of the previous slot of the window
+    for (int ib = 0; ib < wn; ib += 32 * SLOT_U) {
+      uint2 sl[SLOT_U];
+      float row[SLOT_U][DIMP];
 #pragma unroll
-      for (int d = 0; d < DIMP; ++d) ev[d] = sm.rows[node][d];
-      uint32_t nb = 0, np = a.n_total;
-      uint64_t seed = a.seed;
-      if (a.prob_of_node && k_first + nslots > 2) {
-        const ProbInfo pi = a.prob[a.prob_of_node[vg]];
-        nb = pi.node_base;
-        np = pi.n;
-        seed = pi.seed;
+      for (int u = 0; u < SLOT_U; ++u) {  // past the end: the window's last slot again
+        const int i = ib + 32 * u + lane;
+        sl[u] = __ldcs(a.slots + w0 + (i < wn ? i : wn - 1));
       }
-      // negative j: j == 0 was drawn at set-up, later ones draw here
-      auto neg_src = [&](int j) -> uint32_t {
-        return (j == 0) ? neg0 : nb + negative_draw(seed, (uint32_t)j, a.epoch, exi, np);
-      };
-      // the first two slots: both gathers in flight before either is used
-      const int k0 = k_first;
-      const uint32_t src0 = (k0 == 0) ? o : neg_src(k0 - 1);
-      const bool skip0 = (k0 > 0) && (src0 == vg);
-      const bool has1 = nslots >= 2;
-      const uint32_t src1 = has1 ? neg_src(k0) : 0u;
-      const bool skip1 = has1 && (src1 == vg);
-      float row0[DIMP], row1[DIMP];
-      if (!skip0) load_row<DIMP>(a.e_cur + (size_t)src0 * DIMP, row0);
-      if (has1 && !skip1) load_row<DIMP>(a.e_cur + (size_t)src1 * DIMP, row1);
-      slot_value<DIMP>(sm.contrib[cexcl], k0, skip0, ev, row0, two_noise, gamma4);
-      sm.slot_node[cexcl] = (uint8_t)node;
-      if (has1) {
-        slot_value<DIMP>(sm.contrib[cexcl + 1], k0 + 1, skip1, ev, row1, two_noise, gamma4);
-        sm.slot_node[cexcl + 1] = (uint8_t)node;
+#pragma unroll
+      for (int u = 0; u < SLOT_U; ++u) load_row<DIMP>(a.e_cur + (size_t)sl[u].x * DIMP, row[u]);
+#pragma unroll
+      for (int u = 0; u < SLOT_U; ++u) {  // run starts (a repeated last slot starts nothing)
+        const int i = ib + 32 * u + lane;
+        const int node = (int)(sl[u].y & 31u);
+        int prev = __shfl_up_sync(FULL, node, 1);
+        if (lane == 0) prev = carry;
+        carry = __shfl_sync(FULL, node, 31);
+        if (i < wn && node != prev) sm.start[node] = i;
+        act_mask |= __reduce_or_sync(FULL, (i < wn && !(sl[u].y & 32u)) ? (1u << node) : 0u);
       }
-      for (int t = 2; t < nslots; ++t) {
-        const int k = k0 + t;
-        const uint32_t src = neg_src(k - 1);
-        const bool skip = (src == vg);
-        if (!skip) load_row<DIMP>(a.e_cur + (size_t)src * DIMP, row0);
-        slot_value<DIMP>(sm.contrib[cexcl + t], k, skip, ev, row0, two_noise, gamma4);
-        sm.slot_node[cexcl + t] = (uint8_t)node;
+#pragma unroll
+      for (int u = 0; u < SLOT_U; ++u) {
+        const int i = ib + 32 * u + lane;
+        if (i < wn) {
+          const int node = (int)(sl[u].y & 31u);
+          float ev[DIMP], c[DIMP];
+#pragma unroll
+          for (int d = 0; d < DIMP; ++d) ev[d] = sm.rows[node][d];
+          slot_contrib<DIMP>(c, (sl[u].y & 32u) != 0, ev, row[u], two_noise, gamma4);
+          float4* cd = reinterpret_cast<float4*>(&sm.c[i][0]);
+#pragma unroll
+          for (int q = 0; q < DIMP / 4; ++q)
+            cd[q] = make_float4(c[4 * q], c[4 * q + 1], c[4 * q + 2], c[4 * q + 3]);
+        }
       }
     }
     __syncwarp();
-    {  // serial accumulation of slots [0, used), one lane per (node, dim)
-      const int sa = lane, sb = lane + 32;
-      const bool st_a = sa < used && (sa == 0 || sm.slot_node[sa] != sm.slot_node[sa - 1]);
-      const bool st_b = sb < used && sm.slot_node[sb] != sm.slot_node[sb - 1];
-      const uint32_t ma = __ballot_sync(FULL, st_a), mb = __ballot_sync(FULL, st_b);
-      const int na = __popc(ma), nseg = na + __popc(mb);
-      for (int tsk = lane; tsk < nseg * DIMP; tsk += 32) {
-        const int seg = tsk / DIMP, d = tsk - seg * DIMP;
-        const int start = (seg < na) ? (int)__fns(ma, 0u, seg + 1)
-                                     : 32 + (int)__fns(mb, 0u, seg - na + 1);
-        int end = used;
-        if (seg + 1 < nseg)
-          end = (seg + 1 < na) ? (int)__fns(ma, 0u, seg + 2)
-                               : 32 + (int)__fns(mb, 0u, seg + 1 - na + 1);
-        const int nd = sm.slot_node[start];
-        float acc = sm.S[nd][d];
-        for (int s2 = start; s2 < end; ++s2) acc = fadd(acc, sm.contrib[s2][d]);
-        sm.S[nd][d] = acc;
+    // run of node l: [start[l], first start of a later node or wn)
+    const int st = sm.start[lane];
+    int sfx = (st == SLOT_WIN) ? wn : st;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_down_sync(FULL, sfx, o);
+      if (lane + o < 32) sfx = min(sfx, y);
+    }
+    int en = __shfl_down_sync(FULL, sfx, 1);
+    if (lane == 31) en = wn;
+    if (st != SLOT_WIN) {
+      for (int s2 = st; s2 < en; ++s2) {
+        const float4* cd = reinterpret_cast<const float4*>(&sm.c[s2][0]);
+#pragma unroll
+        for (int q = 0; q < DIMP / 4; ++q) {
+          const float4 x = cd[q];
+          g[4 * q] = fadd(g[4 * q], x.x);
+          g[4 * q + 1] = fadd(g[4 * q + 1], x.y);
+          g[4 * q + 2] = fadd(g[4 * q + 2], x.z);
+          g[4 * q + 3] = fadd(g[4 * q + 3], x.w);
+        }
       }
     }
-    __syncwarp();
-    int next_so = 0;
-    if (ndone < 32 && rn < r1) next_so = kf_nd + max(0, CAP - cex_nd);
-    r = rn;
-    so = next_so;
+    __syncwarp();  // contributions and run starts are read before the next window
   }
+  __syncwarp();  // the shared rows are complete for Adam (also with no slots)
 
-  if (has_node) {  // Adam, embedding.rs:256-272
+  if (lane < nt) {  // Adam, embedding.rs:256-272
     const size_t q = (size_t)(v0 + lane) * DIMP;
-    const bool act = (touched >> lane) & 1u;
-    float e[DIMP], g[DIMP];
+    const bool act = (act_mask >> lane) & 1u;
+    float e[DIMP];
 #pragma unroll
     for (int d = 0; d < DIMP; ++d) {
       e[d] = sm.rows[lane][d];
-      g[d] = act ? sm.S[lane][d] : 0.0f;
+      if (!act) g[d] = 0.0f;
     }
     if (act) {
       const float4* m4 = reinterpret_cast<const float4*>(a.m + q);
@@ -1408,6 +1389,21 @@ __global__ void __launch_bounds__(128) k_epoch_rec(EpochArgs a) {
 
 using EpochKernel = void (*)(EpochArgs);
 
+template <int DIMP>
+__global__ void __launch_bounds__(128) k_epoch_slot(EpochArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31;
+  SlotSmem<DIMP>& sm = reinterpret_cast<SlotSmem<DIMP>*>(smem_raw)[threadIdx.x >> 5];
+  const int64_t ntiles = ((int64_t)a.n_total + TILE - 1) / TILE;
+  for (;;) {
+    unsigned long long w = 0;
+    if (lane == 0) w = atomicAdd(a.work_ctr, 1ull);
+    w = __shfl_sync(0xffffffffu, w, 0);
+    if ((int64_t)w >= ntiles) break;
+    slot_tile<DIMP>(a, sm, (int64_t)a.tile_order[w], lane);
+  }
+}
+
 EpochKernel pick_kernel(int dimp) {
   if (dimp == 4) return k_epoch<4>;
   if (dimp == 8) return k_epoch<8>;
@@ -1421,17 +1417,17 @@ size_t tile_smem(int dimp) {
   return sizeof(TileSmem<16>);
 }
 
-EpochKernel pick_rec_kernel(int dimp) {
-  if (dimp == 4) return k_epoch_rec<4>;
-  if (dimp == 8) return k_epoch_rec<8>;
-  if (dimp == 16) return k_epoch_rec<16>;
+EpochKernel pick_slot_kernel(int dimp) {
+  if (dimp == 4) return k_epoch_slot<4>;
+  if (dimp == 8) return k_epoch_slot<8>;
+  if (dimp == 16) return k_epoch_slot<16>;
   return nullptr;
 }
 
-size_t rec_smem(int dimp) {
-  if (dimp == 4) return sizeof(RecSmem<4>);
-  if (dimp == 8) return sizeof(RecSmem<8>);
-  return sizeof(RecSmem<16>);
+size_t slot_smem(int dimp) {
+  if (dimp == 4) return sizeof(SlotSmem<4>);
+  if (dimp == 8) return sizeof(SlotSmem<8>);
+  return sizeof(SlotSmem<16>);
 }
 
 // Warps (node tiles) per thread block of k_epoch; EVOC_WARPS_PER_BLOCK
@@ -1451,7 +1447,7 @@ void launch_epoch(evoc_plan* pl, int32_t t, const float* e_cur, float* e_next,
   a.inc_ptr = pl->inc_ptr.get();
   a.inc_other = pl->inc_other.get();
   a.eidx_base = pl->eidx_base.get();
-  a.fire = pl->use_records ? nullptr : pl->planes.get() + (size_t)t * (1 + pl->P) * pl->W;
+  a.fire = pl->use_slots ? nullptr : pl->planes.get() + (size_t)t * (1 + pl->P) * pl->W;
   a.W = pl->W;
   a.P = pl->P;
   a.e_cur = e_cur;
@@ -1472,18 +1468,17 @@ void launch_epoch(evoc_plan* pl, int32_t t, const float* e_cur, float* e_next,
   a.one_m_b2 = pl->one_m_b2;
   a.tile_off = nullptr;
   a.tile_order = nullptr;
-  a.rec_other = a.rec_aux = a.rec_neg0 = a.rec_eidx = nullptr;
+  a.slots = nullptr;
+  a.work_ctr = nullptr;
   const int wpb = pl->lanes;
   const int64_t tiles = (pl->n + TILE - 1) / TILE;
   const unsigned grid = (unsigned)((tiles + wpb - 1) / wpb);
-  if (pl->use_records) {
+  if (pl->use_slots) {
     a.tile_off = pl->tile_off.get() + (size_t)t * pl->ntiles;
     a.tile_order = pl->tile_order.get();
-    a.rec_other = pl->rec_other.get();
-    a.rec_aux = pl->rec_aux.get();
-    a.rec_neg0 = pl->rec_neg0.get();
-    a.rec_eidx = pl->rec_eidx.get();
-    pick_rec_kernel(pl->dimp)<<<grid, 32 * wpb, wpb * rec_smem(pl->dimp), s>>>(a);
+    a.slots = pl->slots.get();
+    a.work_ctr = pl->work_ctr.get() + t;  // zeroed before the epoch loop
+    pick_slot_kernel(pl->dimp)<<<pl->slot_grid, 32 * wpb, wpb * slot_smem(pl->dimp), s>>>(a);
   } else {
     pick_kernel(pl->dimp)<<<grid, 32 * wpb, wpb * tile_smem(pl->dimp), s>>>(a);
   }
@@ -1521,20 +1516,23 @@ __global__ void k_tile_order(const uint2* __restrict__ vals, int64_t ntiles,
   if (i < ntiles) order[i] = vals[i].x;
 }
 
-// Records path of the schedule set-up: count pass, scan, fill pass. Returns
-// false (nothing built) when EVOC_EPOCH_PATH=scan, when the epoch count
-// exceeds the shared-memory cursors, or when the records would take more than
-// half of the free device memory (unless EVOC_EPOCH_PATH=records).
-static bool build_records(evoc_plan* pl, const float* inc_ps, const uint8_t* inc_up,
-                          const uint32_t* inc_eidx, const float* e_ps, int64_t U,
-                          float neg_factor) {
+// Slots path of the schedule set-up: per-edge schedule and incidence planes
+// (n_epochs <= 64 and at most 3 negatives per edge and epoch) or the
+// per-entry recurrence (otherwise), then count pass, offset scan, tile order
+// and fill pass. Returns false (nothing built) when EVOC_EPOCH_PATH=scan,
+// when the epoch count exceeds the shared-memory cursors, or when the slots
+// would take more than half of the free device memory (unless
+// EVOC_EPOCH_PATH=slots).
+static bool build_slots(evoc_plan* pl, const float* inc_ps, const uint8_t* inc_up,
+                        const uint32_t* inc_eidx, const float* e_ps, int64_t U,
+                        float neg_factor) {
   cudaStream_t s = pl->ctx->stream;
   const int32_t ne = pl->params.n_epochs;
   const int64_t n = pl->n;
   pl->ntiles = (n + TILE - 1) / TILE;
   const char* env = std::getenv("EVOC_EPOCH_PATH");
   const bool force_scan = env && std::strcmp(env, "scan") == 0;
-  const bool force_rec = env && std::strcmp(env, "records") == 0;
+  const bool force_slots = env && std::strcmp(env, "slots") == 0;
   if (force_scan || (size_t)ne * sizeof(int64_t) > 200 * 1024) return false;
   const int wpb = (int)std::max<size_t>(
       1, std::min<size_t>(4, (200 * 1024) / ((size_t)ne * sizeof(int64_t))));
@@ -1542,52 +1540,72 @@ static bool build_records(evoc_plan* pl, const float* inc_ps, const uint8_t* inc
   const int64_t cells = (int64_t)ne * pl->ntiles;
   StageTrace trace(s);
   DevBuf<int32_t> counts(cells, s);
-  DevBuf<unsigned long long> mx(1, s);
+  DevBuf<unsigned long long> mx(1, s), tot(2 * ne, s);  // tot: fired[ne], negs[ne]
   EVOC_CUDA(cudaMemsetAsync(mx.get(), 0, sizeof(unsigned long long), s));
-  const size_t csmem = (size_t)wpb * ne * sizeof(int32_t);
-  if (csmem > 48 * 1024)
-    EVOC_CUDA(cudaFuncSetAttribute((const void*)k_sched_count,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem));
-  // n_epochs <= 64: the recurrence runs once per edge into bit masks, and
-  // the count and fill passes read masks; otherwise both passes run it.
-  const bool use_masks = ne <= 64;
-  DevBuf<unsigned long long> efire, eneg_lo, eneg_hi;
+  EVOC_CUDA(cudaMemsetAsync(tot.get(), 0, tot.bytes(), s));
+  unsigned long long maxneg = 0;
+  // n_epochs <= 64: the recurrence runs once per edge into bit masks, turned
+  // into incidence-order bit planes that the count and fill passes read.
+  bool use_planes = ne <= 64;
   DevBuf<uint32_t> fpl, npl0, npl1;
   int64_t planes_w = 0;
-  if (use_masks) {
-    efire.alloc(U, s);
-    eneg_lo.alloc(U, s);
-    eneg_hi.alloc(U, s);
+  if (use_planes) {
+    DevBuf<unsigned long long> efire(U, s), eneg_lo(U, s), eneg_hi(U, s);
     trace.mark("alloc masks");
     k_edge_sched<<<blocks_for(U), 256, 0, s>>>(e_ps, U, ne, neg_factor, efire.get(),
                                                eneg_lo.get(), eneg_hi.get(), mx.get());
     EVOC_CHECK_LAUNCH();
+    EVOC_CUDA(cudaMemcpyAsync(&maxneg, mx.get(), sizeof(maxneg), cudaMemcpyDeviceToHost, s));
+    EVOC_CUDA(cudaStreamSynchronize(s));
     trace.mark("edge schedule");
-    planes_w = (pl->n_inc + 31) / 32;
-    const int64_t pw = planes_w * ne;
-    fpl.alloc(pw, s);
-    npl0.alloc(pw, s);
-    npl1.alloc(pw, s);
-    k_inc_planes<<<(unsigned)((planes_w + PLANE_BLOCK_WORDS - 1) / PLANE_BLOCK_WORDS), 256, 0,
-                   s>>>(
-        inc_eidx, inc_up, pl->n_inc, planes_w, ne, efire.get(), eneg_lo.get(),
-        eneg_hi.get(), fpl.get(), npl0.get(), npl1.get());
-    EVOC_CHECK_LAUNCH();
-    efire.release();
-    eneg_lo.release();
-    eneg_hi.release();
-    trace.mark("incidence planes");
-    k_plane_count<<<blocks_for(pl->ntiles * 32), 256, 0, s>>>(
-        pl->inc_ptr.get(), n, pl->ntiles, planes_w, ne, fpl.get(), counts.get());
-  } else {
+    use_planes = maxneg <= 3;  // the planes hold negative counts 0..3
+    if (use_planes) {
+      planes_w = (pl->n_inc + 31) / 32;
+      const int64_t pw = planes_w * ne;
+      fpl.alloc(pw, s);
+      npl0.alloc(pw, s);
+      npl1.alloc(pw, s);
+      k_inc_planes<<<(unsigned)((planes_w + PLANE_BLOCK_WORDS - 1) / PLANE_BLOCK_WORDS), 256,
+                     0, s>>>(inc_eidx, inc_up, pl->n_inc, planes_w, ne, efire.get(),
+                             eneg_lo.get(), eneg_hi.get(), fpl.get(), npl0.get(), npl1.get());
+      EVOC_CHECK_LAUNCH();
+      trace.mark("incidence planes");
+      k_plane_count<<<blocks_for(pl->ntiles * 32), 256, 0, s>>>(
+          pl->inc_ptr.get(), n, pl->ntiles, planes_w, ne, fpl.get(), npl0.get(), npl1.get(),
+          counts.get(), tot.get(), tot.get() + ne);
+      EVOC_CHECK_LAUNCH();
+    }
+  }
+  if (!use_planes) {
+    const size_t csmem = (size_t)wpb * ne * sizeof(int32_t);
+    if (csmem > 48 * 1024)
+      EVOC_CUDA(cudaFuncSetAttribute((const void*)k_sched_count,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)csmem));
     k_sched_count<<<grid, 32 * wpb, csmem, s>>>(pl->inc_ptr.get(), inc_ps, inc_up, n,
                                                 pl->ntiles, ne, neg_factor, counts.get(),
-                                                mx.get(), nullptr, nullptr);
+                                                mx.get(), tot.get(), tot.get() + ne);
+    EVOC_CHECK_LAUNCH();
   }
-  EVOC_CHECK_LAUNCH();
   trace.mark("count pass");
   DevBuf<int64_t> off(cells + 1, s);
   exclusive_scan_i32_to_i64(counts.get(), off.get(), cells, s);
+  int64_t total = 0;
+  std::vector<unsigned long long> htot(2 * ne);
+  EVOC_CUDA(cudaMemcpyAsync(&total, off.get() + cells, sizeof(int64_t),
+                            cudaMemcpyDeviceToHost, s));
+  EVOC_CUDA(cudaMemcpyAsync(&maxneg, mx.get(), sizeof(maxneg), cudaMemcpyDeviceToHost, s));
+  EVOC_CUDA(cudaMemcpyAsync(htot.data(), tot.get(), tot.bytes(), cudaMemcpyDeviceToHost, s));
+  EVOC_CUDA(cudaStreamSynchronize(s));
+  if (maxneg > (unsigned long long)NEG_LIMIT)
+    throw Error(EVOC_ERR_UNSUPPORTED,
+                "more than 2^20 negative samples per edge and epoch "
+                "(negative_sample_rate too large)");
+  size_t free_b = 0, total_b = 0;
+  EVOC_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  const double need = (double)sizeof(uint2) * (double)total;
+  if (!force_slots && need > 0.5 * (double)free_b) return false;
+  pl->max_neg = maxneg;
+  trace.mark("offset scan + sync");
   {
     DevBuf<uint32_t> keys(pl->ntiles, s);
     DevBuf<uint2> vals(pl->ntiles, s);
@@ -1600,74 +1618,47 @@ static bool build_records(evoc_plan* pl, const float* inc_ps, const uint8_t* inc
                                                          pl->tile_order.get());
     EVOC_CHECK_LAUNCH();
   }
-  trace.mark("offset scan + tile order");
-  int64_t total = 0;
-  unsigned long long maxneg = 0;
-  EVOC_CUDA(cudaMemcpyAsync(&total, off.get() + cells, sizeof(int64_t),
-                            cudaMemcpyDeviceToHost, s));
-  EVOC_CUDA(cudaMemcpyAsync(&maxneg, mx.get(), sizeof(maxneg), cudaMemcpyDeviceToHost, s));
-  EVOC_CUDA(cudaStreamSynchronize(s));
-  if (maxneg > (unsigned long long)NEG_LIMIT)
-    throw Error(EVOC_ERR_UNSUPPORTED,
-                "more than 2^20 negative samples per edge and epoch "
-                "(negative_sample_rate too large)");
-  const bool need_eidx = maxneg > 1;
-  size_t free_b = 0, total_b = 0;
-  EVOC_CUDA(cudaMemGetInfo(&free_b, &total_b));
-  const double need = (need_eidx ? 16.0 : 12.0) * (double)total;
-  if (!force_rec && need > 0.5 * (double)free_b) return false;
-  pl->max_neg = maxneg;
-  trace.mark("sync + memgetinfo");
-  pl->rec_other.alloc(total, s);
-  pl->rec_aux.alloc(total, s);
-  pl->rec_neg0.alloc(total, s);
-  if (need_eidx) pl->rec_eidx.alloc(total, s);
-  trace.mark("alloc records");
-  if (use_masks && maxneg <= 3) {
+  trace.mark("tile order");
+  pl->slots.alloc(total, s);
+  trace.mark("alloc slots");
+  const uint32_t* pon = pl->n_problems > 1 ? pl->prob_of_node.get() : nullptr;
+  const ProbInfo* pinfo = pl->n_problems > 1 ? pl->prob.get() : nullptr;
+  const uint64_t seed0 = pl->seeds.empty() ? 0 : pl->seeds[0];
+  if (use_planes) {
     k_plane_fill<<<(unsigned)((pl->ntiles + 3) / 4), 128, 0, s>>>(
         pl->inc_ptr.get(), pl->inc_other.get(), pl->eidx_base.get(), n, pl->ntiles, planes_w,
-        ne, fpl.get(), npl0.get(), npl1.get(), off.get(),
-        pl->n_problems > 1 ? pl->prob_of_node.get() : nullptr,
-        pl->n_problems > 1 ? pl->prob.get() : nullptr, pl->seeds.empty() ? 0 : pl->seeds[0],
-        pl->rec_other.get(), pl->rec_aux.get(), pl->rec_neg0.get(),
-        need_eidx ? pl->rec_eidx.get() : nullptr);
+        ne, fpl.get(), npl0.get(), npl1.get(), off.get(), pon, pinfo, seed0, pl->slots.get());
   } else {
-  const size_t fsmem = (size_t)wpb * ne * sizeof(int64_t);
-  if (fsmem > 48 * 1024)
-    EVOC_CUDA(cudaFuncSetAttribute((const void*)k_sched_fill,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
-  k_sched_fill<<<grid, 32 * wpb, fsmem, s>>>(
-      pl->inc_ptr.get(), pl->inc_other.get(), inc_ps, inc_up, pl->eidx_base.get(), n,
-      pl->ntiles, ne, neg_factor, off.get(),
-      pl->n_problems > 1 ? pl->prob_of_node.get() : nullptr,
-      pl->n_problems > 1 ? pl->prob.get() : nullptr, pl->seeds.empty() ? 0 : pl->seeds[0],
-      pl->rec_other.get(), pl->rec_aux.get(), pl->rec_neg0.get(),
-      need_eidx ? pl->rec_eidx.get() : nullptr);
+    const size_t fsmem = (size_t)wpb * ne * sizeof(int64_t);
+    if (fsmem > 48 * 1024)
+      EVOC_CUDA(cudaFuncSetAttribute((const void*)k_sched_fill,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fsmem));
+    k_sched_fill<<<grid, 32 * wpb, fsmem, s>>>(
+        pl->inc_ptr.get(), pl->inc_other.get(), inc_ps, inc_up, pl->eidx_base.get(), n,
+        pl->ntiles, ne, neg_factor, off.get(), pon, pinfo, seed0, pl->slots.get());
   }
   EVOC_CHECK_LAUNCH();
   trace.mark("fill pass");
-  // fired edges per epoch = records of the epoch / 2 (both copies fire)
-  std::vector<int64_t> h(ne + 1);
-  for (int32_t t = 0; t <= ne; ++t)
-    EVOC_CUDA(cudaMemcpyAsync(&h[t], off.get() + (int64_t)t * pl->ntiles, sizeof(int64_t),
-                              cudaMemcpyDeviceToHost, s));
-  EVOC_CUDA(cudaStreamSynchronize(s));
-  for (int32_t t = 0; t < ne; ++t) pl->stats[t].fired_edges = (h[t + 1] - h[t]) / 2;
+  // fired edges per epoch = fired incidence entries / 2 (both copies fire)
+  for (int32_t t = 0; t < ne; ++t) {
+    pl->stats[t].fired_edges = (int64_t)(htot[t] / 2);
+    pl->stats[t].negatives = (int64_t)htot[ne + t];
+  }
   pl->tile_off = std::move(off);
-  pl->n_records = total;
-  pl->use_records = true;
+  pl->n_slots = total;
+  pl->use_slots = true;
   pl->inc_other.release();
   return true;
 }
 
 evoc_ctx* plan_ctx(const evoc_plan* p) { return p->ctx; }
 void plan_info(const evoc_plan* p, int64_t* n_edges, int64_t* n_inc,
-               int32_t* planes, int32_t* wpb, int64_t* n_records) {
+               int32_t* planes, int32_t* wpb, int64_t* n_slots) {
   if (n_edges) *n_edges = p->n_edges;
   if (n_inc) *n_inc = p->n_inc;
   if (planes) *planes = p->P;
   if (wpb) *wpb = p->lanes;
-  if (n_records) *n_records = p->use_records ? p->n_records : 0;
+  if (n_slots) *n_slots = p->use_slots ? p->n_slots : 0;
 }
 int64_t plan_n(const evoc_plan* p) { return p->n; }
 int32_t plan_n_epochs(const evoc_plan* p) { return p->params.n_epochs; }
@@ -1863,7 +1854,7 @@ evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
   // schedule: per-epoch records (fast path) or bit planes (fallback)
   const float neg_factor = 1.5f / params.negative_sample_rate;  // embedding.rs:116
   pl->W = (n_inc + 31) / 32;
-  if (ne > 0 && !build_records(pl.get(), inc_ps.get(), inc_up.get(), inc_eidx.get(),
+  if (ne > 0 && !build_slots(pl.get(), inc_ps.get(), inc_up.get(), inc_eidx.get(),
                                e_ps.get(), U, neg_factor)) {
     DevBuf<unsigned long long> mx(1, s), st(2 * ne, s);
     EVOC_CUDA(cudaMemsetAsync(mx.get(), 0, sizeof(unsigned long long), s));
@@ -1906,6 +1897,18 @@ evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
   pl->m.alloc(n * pl->dimp, s);
   pl->v.alloc(n * pl->dimp, s);
   pl->lanes = default_wpb();
+  if (pl->use_slots) {  // persistent grid: as many warps as fit on the device
+    int nb = 0, dev = 0, sms = 0;
+    const size_t smem = (size_t)pl->lanes * slot_smem(pl->dimp);
+    EVOC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &nb, (const void*)pick_slot_kernel(pl->dimp), 32 * pl->lanes, smem));
+    EVOC_CUDA(cudaGetDevice(&dev));
+    EVOC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const int64_t want = (int64_t)std::max(nb, 1) * sms;
+    const int64_t need = (pl->ntiles + pl->lanes - 1) / pl->lanes;
+    pl->slot_grid = (unsigned)std::max<int64_t>(1, std::min(want, need));
+    pl->work_ctr.alloc(std::max<int32_t>(ne, 1), s);
+  }
   trace.mark("moments");
   EVOC_CUDA(cudaStreamSynchronize(s));
   return pl.release();
@@ -1914,29 +1917,23 @@ evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
 void plan_stats(const evoc_plan* cpl, evoc_epoch_stats_t* out) {
   evoc_plan* pl = const_cast<evoc_plan*>(cpl);
   const int32_t ne = pl->params.n_epochs;
-  if (pl->has_edges && !pl->stats_done && ne > 0) {
+  if (pl->has_edges && !pl->stats_done && ne > 0) {  // active nodes, on request
     cudaStream_t s = pl->ctx->stream;
-    DevBuf<unsigned long long> act(ne, s), ng(ne, s);
+    DevBuf<unsigned long long> act(ne, s);
     EVOC_CUDA(cudaMemsetAsync(act.get(), 0, act.bytes(), s));
-    EVOC_CUDA(cudaMemsetAsync(ng.get(), 0, ng.bytes(), s));
-    if (pl->use_records) {
-      k_rec_stats<<<blocks_for(pl->ntiles * 32), 256, 0, s>>>(
-          pl->tile_off.get(), pl->rec_aux.get(), pl->ntiles, ne, ng.get(), act.get());
+    if (pl->use_slots) {
+      k_slot_stats<<<blocks_for(pl->ntiles * 32), 256, 0, s>>>(
+          pl->tile_off.get(), pl->slots.get(), pl->ntiles, ne, act.get());
     } else {
       k_active_count<<<blocks_for(pl->n * 32), 256, 0, s>>>(
           pl->inc_ptr.get(), pl->n, pl->planes.get(), ne, pl->P, pl->W, act.get());
     }
     EVOC_CHECK_LAUNCH();
-    std::vector<unsigned long long> ha(ne), hn(ne);
+    std::vector<unsigned long long> ha(ne);
     EVOC_CUDA(cudaMemcpyAsync(ha.data(), act.get(), ne * sizeof(unsigned long long),
                               cudaMemcpyDeviceToHost, s));
-    EVOC_CUDA(cudaMemcpyAsync(hn.data(), ng.get(), ne * sizeof(unsigned long long),
-                              cudaMemcpyDeviceToHost, s));
     EVOC_CUDA(cudaStreamSynchronize(s));
-    for (int32_t t = 0; t < ne; ++t) {
-      pl->stats[t].active_nodes = (int64_t)ha[t];
-      if (pl->use_records) pl->stats[t].negatives = (int64_t)hn[t];
-    }
+    for (int32_t t = 0; t < ne; ++t) pl->stats[t].active_nodes = (int64_t)ha[t];
     pl->stats_done = true;
   }
   for (int32_t t = 0; t < ne; ++t) out[t] = pl->stats[t];
@@ -1967,6 +1964,8 @@ void plan_run_device(evoc_plan* pl, const float* d_init, float* d_out) {
   if (pl->has_edges && ne > 0) {
     EVOC_CUDA(cudaMemsetAsync(pl->m.get(), 0, pl->m.bytes(), s));
     EVOC_CUDA(cudaMemsetAsync(pl->v.get(), 0, pl->v.bytes(), s));
+    if (pl->use_slots)  // tile counters of the slots kernel, one per epoch
+      EVOC_CUDA(cudaMemsetAsync(pl->work_ctr.get(), 0, pl->work_ctr.bytes(), s));
     if (!pl->graph_exec) {
       EVOC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
       try {
@@ -2003,6 +2002,8 @@ void plan_profile_epochs(evoc_plan* pl, const float* d_init, float* d_out,
   if (pl->has_edges && ne > 0) {
     EVOC_CUDA(cudaMemsetAsync(pl->m.get(), 0, pl->m.bytes(), s));
     EVOC_CUDA(cudaMemsetAsync(pl->v.get(), 0, pl->v.bytes(), s));
+    if (pl->use_slots)  // tile counters of the slots kernel, one per epoch
+      EVOC_CUDA(cudaMemsetAsync(pl->work_ctr.get(), 0, pl->work_ctr.bytes(), s));
     std::vector<cudaEvent_t> ev(ne + 1, nullptr);
     try {
       for (auto& e : ev) EVOC_CUDA(cudaEventCreate(&e));
@@ -2055,6 +2056,8 @@ void plan_debug_run(evoc_plan* pl, const float* h_init, int32_t start_epoch,
   if (pl->has_edges && e1 > e0) {
     EVOC_CUDA(cudaMemsetAsync(pl->m.get(), 0, pl->m.bytes(), s));
     EVOC_CUDA(cudaMemsetAsync(pl->v.get(), 0, pl->v.bytes(), s));
+    if (pl->use_slots)  // tile counters of the slots kernel, one per epoch
+      EVOC_CUDA(cudaMemsetAsync(pl->work_ctr.get(), 0, pl->work_ctr.bytes(), s));
     for (int32_t t = e0; t < e1; ++t) {
       const int k = t - e0;
       const float* cur = (k & 1) ? pl->e1.get() : pl->e0.get();

@@ -205,7 +205,7 @@ void plan_stats(const evoc_plan* plan, evoc_epoch_stats_t* stats);
 void plan_free(evoc_plan* plan);
 evoc_ctx* plan_ctx(const evoc_plan* plan);
 void plan_info(const evoc_plan* plan, int64_t* n_edges, int64_t* n_inc,
-               int32_t* planes, int32_t* wpb, int64_t* n_records);
+               int32_t* planes, int32_t* wpb, int64_t* n_slots);
 int64_t plan_n(const evoc_plan* plan);
 int32_t plan_n_epochs(const evoc_plan* plan);
 bool plan_has_edges(const evoc_plan* plan);

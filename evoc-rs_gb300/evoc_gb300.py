@@ -226,7 +226,7 @@ class Plan:
         self._ctx._check(self._ctx.lib.evoc_plan_info(self.handle, C.byref(e), C.byref(i),
                                                       C.byref(p), C.byref(l), C.byref(r)))
         return {"n_edges": e.value, "n_incidence": i.value, "neg_planes": p.value,
-                "warps_per_block": l.value, "n_records": r.value}
+                "warps_per_block": l.value, "n_slots": r.value}
 
     def stats(self) -> np.ndarray:
         arr = (EpochStatsC * max(self.n_epochs, 1))()

@@ -233,11 +233,12 @@ EVOC_API int evoc_plan_profile_epochs(evoc_plan_t* plan, const float* d_init,
 /* Layout facts of a plan (any pointer may be NULL): undirected edges,
  * per-node incidence entries (2 per edge), negative-count bit planes per
  * epoch, warps (32-node tiles) per thread block of the epoch kernel, and the
- * number of per-epoch fired-entry records (0 when the epoch kernel scans the
- * bit planes instead) (no counterpart). */
+ * number of gradient slots over all epochs (one per fired incidence entry and
+ * one per negative sample; 0 when the epoch kernel scans the bit planes
+ * instead) (no counterpart). */
 EVOC_API int evoc_plan_info(const evoc_plan_t* plan, int64_t* n_edges,
                             int64_t* n_incidence, int32_t* neg_planes,
-                            int32_t* warps_per_block, int64_t* n_records);
+                            int32_t* warps_per_block, int64_t* n_slots);
 
 /* Per-epoch work counts (stats[params.n_epochs]). */
 EVOC_API int evoc_plan_stats(const evoc_plan_t* plan, evoc_epoch_stats_t* stats);

@@ -122,11 +122,11 @@ def test_launch_shape_does_not_change_results(ctx, blobs_graph, monkeypatch):
         _assert_bits(o, outs[0])
 
 
-def test_records_and_scan_paths_agree(ctx, oracle, blobs_graph, monkeypatch):
-    """The per-epoch record path and the bit-plane scanning fallback."""
+def test_slots_and_scan_paths_agree(ctx, oracle, blobs_graph, monkeypatch):
+    """The per-epoch gradient-slot path and the bit-plane scanning fallback."""
     g, (ip, ix, w), _ = blobs_graph
     outs = {}
-    for path in ("records", "scan"):
+    for path in ("slots", "scan"):
         monkeypatch.setenv("EVOC_EPOCH_PATH", path)
         outs[path] = ctx.embed(g, 8, seed=21)
         plan = ctx.plan(g, 8, seed=21)
@@ -134,9 +134,9 @@ def test_records_and_scan_paths_agree(ctx, oracle, blobs_graph, monkeypatch):
         init = rng.uniform(-1, 1, (g.n, 8)).astype(np.float32)
         outs[path + "_grad"] = plan.debug_run(init, 9, 10, want_grad=True)[1]
     monkeypatch.delenv("EVOC_EPOCH_PATH")
-    _assert_bits(outs["records"], outs["scan"])
-    _assert_bits(outs["records_grad"], outs["scan_grad"], "gradient")
-    _assert_bits(outs["records"], oracle.evoc_embedding(ip, ix, w, 8, seed=21))
+    _assert_bits(outs["slots"], outs["scan"])
+    _assert_bits(outs["slots_grad"], outs["scan_grad"], "gradient")
+    _assert_bits(outs["slots"], oracle.evoc_embedding(ip, ix, w, 8, seed=21))
 
 
 def test_general_graph_path(ctx, oracle, blobs_graph):
