@@ -1206,21 +1206,26 @@ __global__ void k_slot_stats(const int64_t* __restrict__ tile_off,
 // One epoch, slots path: persistent warps; each takes the next 32-node tile
 // in tile_order (heaviest first) from the epoch's work counter. The tile's
 // slots of the epoch come in windows of SLOT_WIN. Phase 1: each lane computes
-// the contributions of SLOT_U slots (attraction, embedding.rs:213-221, or
-// repulsion, embedding.rs:237-245, from the slot's source row and the node's
-// own row) into shared memory, all loads and gathers issued first; the first
-// slot of each node run records its position. Phase 2: the slots are
-// node-major in the order of the reference's serial sum (embedding.rs:
-// 194-253), so lane l adds the run of node v0 + l onto its running gradient
-// in registers. Then Adam (embedding.rs:256-272).
-constexpr int SLOT_WIN = 256;
-constexpr int SLOT_U = 4;
+// slot contributions (attraction, embedding.rs:213-221, or repulsion,
+// embedding.rs:237-245, from the slot's source row and the node's own row)
+// into shared memory, SLOT_U slots at a time with all loads and gathers
+// issued first; the first slot of each node run records its position.
+// Phase 2: the slots are node-major in the order of the reference's serial
+// sum (embedding.rs:194-253); lane l adds the run of node v0 + l onto its
+// running gradient in registers, except that a run longer than SLOT_LONG (a
+// hub) is added by DIMP lanes, one dim each, through shared memory.
+// Then Adam (embedding.rs:256-272), lane per node.
+constexpr int SLOT_WIN = 128;
+constexpr int SLOT_U = 2;
+constexpr int SLOT_LONG = 64;
 
 template <int DIMP>
 struct alignas(16) SlotSmem {
   float rows[TILE][DIMP];      // e_cur rows of the tile's nodes
   float c[SLOT_WIN][DIMP];     // contributions of the window's slots
+  float S[TILE][DIMP + 1];     // running gradients of nodes with a long run
   int32_t start[TILE];         // first window slot of each node's run (or none)
+  int32_t end[TILE];           // one past its last
 };
 
 // Contribution of one slot; +0 where the reference adds nothing (adding +0
@@ -1253,6 +1258,49 @@ __device__ __forceinline__ void slot_contrib(float (&c)[DIMP], bool neg,
   }
 }
 
+// Phase 1 for U slots per lane: window slots ib + 32 u + lane, u < U.
+template <int DIMP, int U>
+__device__ __forceinline__ void slot_group(const EpochArgs& a, SlotSmem<DIMP>& sm,
+                                           const uint2* __restrict__ wslots, int ib, int wn,
+                                           int lane, int& carry, uint32_t& act_mask,
+                                           float two_noise, float gamma4) {
+  const unsigned FULL = 0xffffffffu;
+  uint2 sl[U];
+  float row[U][DIMP];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {  // past the end: the window's last slot again
+    const int i = ib + 32 * u + lane;
+    sl[u] = __ldcs(wslots + (i < wn ? i : wn - 1));
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) load_row<DIMP>(a.e_cur + (size_t)sl[u].x * DIMP, row[u]);
+#pragma unroll
+  for (int u = 0; u < U; ++u) {  // run starts (a repeated last slot starts nothing)
+    const int i = ib + 32 * u + lane;
+    const int node = (int)(sl[u].y & 31u);
+    int prev = __shfl_up_sync(FULL, node, 1);
+    if (lane == 0) prev = carry;
+    carry = __shfl_sync(FULL, node, 31);
+    if (i < wn && node != prev) sm.start[node] = i;
+    act_mask |= __reduce_or_sync(FULL, (i < wn && !(sl[u].y & 32u)) ? (1u << node) : 0u);
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int i = ib + 32 * u + lane;
+    if (i < wn) {
+      const int node = (int)(sl[u].y & 31u);
+      float ev[DIMP], c[DIMP];
+#pragma unroll
+      for (int d = 0; d < DIMP; ++d) ev[d] = sm.rows[node][d];
+      slot_contrib<DIMP>(c, (sl[u].y & 32u) != 0, ev, row[u], two_noise, gamma4);
+      float4* cd = reinterpret_cast<float4*>(&sm.c[i][0]);
+#pragma unroll
+      for (int q = 0; q < DIMP / 4; ++q)
+        cd[q] = make_float4(c[4 * q], c[4 * q + 1], c[4 * q + 2], c[4 * q + 3]);
+    }
+  }
+}
+
 template <int DIMP>
 __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP>& sm, int64_t tile,
                                           int lane) {
@@ -1260,7 +1308,7 @@ __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP>& sm
   const int64_t v0 = tile * TILE;
   const int nt = (int)min((int64_t)TILE, (int64_t)a.n_total - v0);
   const int64_t s0 = a.tile_off[tile], s1 = a.tile_off[tile + 1];
-  __syncwarp();  // the previous tile's readers of the shared rows are done
+  __syncwarp();  // the previous tile's readers of the shared rows and sums are done
   {
     const float4* src = reinterpret_cast<const float4*>(a.e_cur + (size_t)v0 * DIMP);
     float4* dst = reinterpret_cast<float4*>(&sm.rows[0][0]);
@@ -1274,45 +1322,15 @@ __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP>& sm
   uint32_t act_mask = 0;
   for (int64_t w0 = s0; w0 < s1; w0 += SLOT_WIN) {
     const int wn = (int)min((int64_t)SLOT_WIN, s1 - w0);
+    const uint2* wslots = a.slots + w0;
     sm.start[lane] = SLOT_WIN;  // none
     __syncwarp();
     int carry = -1;  // node of the previous slot of the window
-    for (int ib = 0; ib < wn; ib += 32 * SLOT_U) {
-      uint2 sl[SLOT_U];
-      float row[SLOT_U][DIMP];
-#pragma unroll
-      for (int u = 0; u < SLOT_U; ++u) {  // past the end: the window's last slot again
-        const int i = ib + 32 * u + lane;
-        sl[u] = __ldcs(a.slots + w0 + (i < wn ? i : wn - 1));
-      }
-#pragma unroll
-      for (int u = 0; u < SLOT_U; ++u) load_row<DIMP>(a.e_cur + (size_t)sl[u].x * DIMP, row[u]);
-#pragma unroll
-      for (int u = 0; u < SLOT_U; ++u) {  // run starts (a repeated last slot starts nothing)
-        const int i = ib + 32 * u + lane;
-        const int node = (int)(sl[u].y & 31u);
-        int prev = __shfl_up_sync(FULL, node, 1);
-        if (lane == 0) prev = carry;
-        carry = __shfl_sync(FULL, node, 31);
-        if (i < wn && node != prev) sm.start[node] = i;
-        act_mask |= __reduce_or_sync(FULL, (i < wn && !(sl[u].y & 32u)) ? (1u << node) : 0u);
-      }
-#pragma unroll
-      for (int u = 0; u < SLOT_U; ++u) {
-        const int i = ib + 32 * u + lane;
-        if (i < wn) {
-          const int node = (int)(sl[u].y & 31u);
-          float ev[DIMP], c[DIMP];
-#pragma unroll
-          for (int d = 0; d < DIMP; ++d) ev[d] = sm.rows[node][d];
-          slot_contrib<DIMP>(c, (sl[u].y & 32u) != 0, ev, row[u], two_noise, gamma4);
-          float4* cd = reinterpret_cast<float4*>(&sm.c[i][0]);
-#pragma unroll
-          for (int q = 0; q < DIMP / 4; ++q)
-            cd[q] = make_float4(c[4 * q], c[4 * q + 1], c[4 * q + 2], c[4 * q + 3]);
-        }
-      }
-    }
+    int ib = 0;
+    for (; ib + 32 * SLOT_U <= wn; ib += 32 * SLOT_U)
+      slot_group<DIMP, SLOT_U>(a, sm, wslots, ib, wn, lane, carry, act_mask, two_noise, gamma4);
+    for (; ib < wn; ib += 32)
+      slot_group<DIMP, 1>(a, sm, wslots, ib, wn, lane, carry, act_mask, two_noise, gamma4);
     __syncwarp();
     // run of node l: [start[l], first start of a later node or wn)
     const int st = sm.start[lane];
@@ -1324,7 +1342,15 @@ __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP>& sm
     }
     int en = __shfl_down_sync(FULL, sfx, 1);
     if (lane == 31) en = wn;
-    if (st != SLOT_WIN) {
+    const bool has = st != SLOT_WIN;
+    const bool is_long = has && en - st > SLOT_LONG;
+    const uint32_t longs = __ballot_sync(FULL, is_long);
+    if (is_long) {  // hand the running sum to the dim lanes
+      sm.end[lane] = en;
+#pragma unroll
+      for (int d = 0; d < DIMP; ++d) sm.S[lane][d] = g[d];
+    }
+    if (has && !is_long) {
       for (int s2 = st; s2 < en; ++s2) {
         const float4* cd = reinterpret_cast<const float4*>(&sm.c[s2][0]);
 #pragma unroll
@@ -1337,7 +1363,29 @@ __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP>& sm
         }
       }
     }
-    __syncwarp();  // contributions and run starts are read before the next window
+    if (longs) {
+      __syncwarp();
+      const int ntask = __popc(longs) * DIMP;
+      for (int tsk = lane; tsk < ntask; tsk += 32) {
+        const int node = nth_set_bit(longs, tsk / DIMP), d = tsk % DIMP;
+        const int s2b = sm.start[node], s2e = sm.end[node];
+        float acc = sm.S[node][d];
+        int s2 = s2b;
+        for (; s2 + 4 <= s2e; s2 += 4) {
+          const float x0 = sm.c[s2][d], x1 = sm.c[s2 + 1][d], x2 = sm.c[s2 + 2][d],
+                      x3 = sm.c[s2 + 3][d];
+          acc = fadd(fadd(fadd(fadd(acc, x0), x1), x2), x3);
+        }
+        for (; s2 < s2e; ++s2) acc = fadd(acc, sm.c[s2][d]);
+        sm.S[node][d] = acc;
+      }
+      __syncwarp();
+      if (is_long) {
+#pragma unroll
+        for (int d = 0; d < DIMP; ++d) g[d] = sm.S[lane][d];
+      }
+    }
+    __syncwarp();  // contributions, runs and sums are settled before the next window
   }
   __syncwarp();  // the shared rows are complete for Adam (also with no slots)
 
@@ -1389,8 +1437,10 @@ __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP>& sm
 
 using EpochKernel = void (*)(EpochArgs);
 
+// Register cap: 7 blocks of 128 threads per SM (72 registers) for DIMP <= 8
+// measured fastest; the occupancy it buys outweighs per-warp parallelism.
 template <int DIMP>
-__global__ void __launch_bounds__(128) k_epoch_slot(EpochArgs a) {
+__global__ void __launch_bounds__(128, DIMP <= 8 ? 7 : 4) k_epoch_slot(EpochArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
   SlotSmem<DIMP>& sm = reinterpret_cast<SlotSmem<DIMP>*>(smem_raw)[threadIdx.x >> 5];

@@ -162,6 +162,37 @@ def test_asymmetric_graph_vs_oracle(ctx, oracle):
     _assert_bits(ctx.embed(g, 8, seed=11), oracle.evoc_embedding(ip, ix, w, 8, seed=11))
 
 
+@pytest.mark.parametrize("dim", [4, 8, 16])
+def test_hub_nodes_vs_oracle(ctx, oracle, dim):
+    """Hub nodes (degree in the thousands, weight 1: they fire every epoch)
+    next to ordinary rows: a hub's serial gradient sum runs over hundreds of
+    terms per epoch, longer than one window of the epoch kernel."""
+    rng = np.random.default_rng(5)
+    n, deg = 3000, 6
+    hubs = {7: 2500, 1500: 900, 2999: 300}
+    rows = [list(rng.integers(0, n, size=deg)) for _ in range(n)]
+    wts = [list(rng.uniform(0.05, 0.9, size=deg)) for _ in range(n)]
+    for h, k in hubs.items():
+        nb = rng.choice(n, size=k, replace=False)
+        rows[h] += list(nb)
+        wts[h] += [1.0] * k
+        for j in nb:  # symmetric: the partners list the hub too
+            rows[j].append(h)
+            wts[j].append(1.0)
+    ip = np.zeros(n + 1, dtype=np.int64)
+    ip[1:] = np.cumsum([len(r) for r in rows])
+    ix = np.concatenate(rows).astype(np.uint32)
+    w = np.concatenate(wts).astype(np.float32)
+    g = ctx.graph_from_csr(ip, ix, w)
+    _assert_bits(ctx.embed(g, dim, seed=13), oracle.evoc_embedding(ip, ix, w, dim, seed=13))
+    init = rng.uniform(-1, 1, (n, dim)).astype(np.float32)
+    plan = ctx.plan(g, dim, seed=13)
+    _, grad = plan.debug_run(init, 4, 5, want_grad=True)
+    _, ref = oracle.evoc_embedding(ip, ix, w, dim, init=init, seed=13, start_epoch=4,
+                                   end_epoch=5, want_grad=True)
+    _assert_bits(grad, ref, "gradient")
+
+
 def test_errors_keep_context_usable(ctx):
     import evoc_gb300 as E
     with pytest.raises(E.EvocError) as ei:
