@@ -233,13 +233,7 @@ __global__ void k_inc_fill(const int64_t* __restrict__ indptr,
         inc_other[q] = c;
         inc_ps[q] = ps_from_w(weights[p], mw);
         inc_up[q] = 0;
-        // the twin entry (c -> v) is an upper entry of the sorted row c
-        int64_t lo_i = indptr[c], hi_i = indptr[c + 1] - 1;
-        while (lo_i < hi_i) {
-          const int64_t mid = (lo_i + hi_i) >> 1;
-          if ((int64_t)indices[mid] < v) lo_i = mid + 1; else hi_i = mid;
-        }
-        inc_eidx[q] = (uint32_t)(uptr[c] + (lo_i - indptr[c]) - lcnt[c]);
+        inc_eidx[q] = 0xffffffffu;  // lower entries draw no negatives
       }
       o += __popc(bal);
     }
@@ -250,7 +244,7 @@ __global__ void k_inc_fill(const int64_t* __restrict__ indptr,
       inc_other[p0 + j] = pe.y;
       inc_ps[p0 + j] = e_ps[pe.x];
       inc_up[p0 + j] = 0;
-      inc_eidx[p0 + j] = pe.x;
+      inc_eidx[p0 + j] = 0xffffffffu;  // lower entries draw no negatives
     }
   }
   int64_t o = p0 + nl;
@@ -817,12 +811,16 @@ __device__ __forceinline__ uint32_t warp_transpose32(uint32_t x, int lane) {
 // Fire and negative-count bit planes in incidence order (n_epochs <= 64).
 // F[t * W + w] bit l = entry 32 w + l fires in epoch t; N0 / N1 hold bits 0 /
 // 1 of its negative count (upper entries only). Block of 8 warps per 32 words:
-// each warp gathers the edge masks of 4 words and transposes them (lane t
-// receives epoch t and t + 32); the words are staged in shared memory and
-// every plane row leaves as one 128-byte line.
+// each warp takes the masks of 4 words and transposes them (lane t receives
+// epoch t and t + 32); the words are staged in shared memory and every plane
+// row leaves as one 128-byte line. Upper entries read their edge's masks
+// (consecutive edges); a lower entry's fire mask is the same recurrence run
+// on its own epochs-per-sample, which equals its upper twin's (both copies of
+// an edge carry the same value).
 constexpr int PLANE_BLOCK_WORDS = 32;
 __global__ void __launch_bounds__(256) k_inc_planes(
-    const uint32_t* __restrict__ inc_eidx, const uint8_t* __restrict__ inc_up, int64_t n_inc,
+    const uint32_t* __restrict__ inc_eidx, const uint8_t* __restrict__ inc_up,
+    const float* __restrict__ inc_ps, int64_t n_inc,
     int64_t W, int32_t ne, const unsigned long long* __restrict__ edge_fire,
     const unsigned long long* __restrict__ edge_neg_lo,
     const unsigned long long* __restrict__ edge_neg_hi, uint32_t* __restrict__ fplane,
@@ -832,20 +830,35 @@ __global__ void __launch_bounds__(256) k_inc_planes(
   const int64_t w0 = (int64_t)blockIdx.x * PLANE_BLOCK_WORDS;
   constexpr int J = PLANE_BLOCK_WORDS / 8;
   uint32_t e[J];
-  bool up[J];
+  bool up[J], ok[J];
+  float ps[J];
 #pragma unroll
   for (int j = 0; j < J; ++j) {
     const int64_t p = ((w0 + wid * J + j) << 5) + lane;
-    const bool ok = p < n_inc;
-    e[j] = ok ? inc_eidx[p] : 0xffffffffu;
-    up[j] = ok && inc_up[p];
+    ok[j] = p < n_inc;
+    up[j] = ok[j] && inc_up[p];
+    e[j] = up[j] ? inc_eidx[p] : 0u;
+    ps[j] = (ok[j] && !up[j]) ? inc_ps[p] : 3.0e38f;
   }
   unsigned long long fm[J], g0[J], g1[J];
 #pragma unroll
   for (int j = 0; j < J; ++j) {
-    fm[j] = e[j] != 0xffffffffu ? edge_fire[e[j]] : 0ull;
+    fm[j] = up[j] ? edge_fire[e[j]] : 0ull;
     g0[j] = up[j] ? edge_neg_lo[e[j]] : 0ull;
     g1[j] = up[j] ? edge_neg_hi[e[j]] : 0ull;
+  }
+#pragma unroll
+  for (int j = 0; j < J; ++j) {  // lower entries: fires only (embedding.rs:274-279)
+    if (ok[j] && !up[j]) {
+      float ns = ps[j];
+      unsigned long long m = 0;
+      for (int32_t t = 0; t < ne; ++t) {
+        const float tf = (float)t;
+        if (!(ns > tf)) m |= 1ull << t;
+        if (ns <= tf) ns = fadd(ns, ps[j]);
+      }
+      fm[j] = m;
+    }
   }
 #pragma unroll
   for (int j = 0; j < J; ++j) {
@@ -932,16 +945,48 @@ __device__ __forceinline__ int nth_set_bit(uint32_t m, int r) {
 }
 
 // Fill pass from the planes (n_epochs <= 64, at most 3 negatives per edge and
-// epoch): warp per tile, epochs in order. For each epoch the tile's plane
-// words are taken 64 at a time; their fire events are spread over the lanes
-// in incidence order and each writes its slots (the attraction, then its
-// negatives j = 0.., drawn here with Philox counter (j, epoch, edge)) after
-// those of the lower lanes, so every (epoch, tile) segment is written front
-// to back in the order of the reference's serial sum.
-struct PlaneFillSmem {
-  uint32_t f[64], n0[64], n1[64];
-  int32_t ex[65];  // exclusive prefix of the words' event counts
+// epoch): warp per (tile, epoch), numbered tile-major: a hub tile's epochs
+// run in parallel, and the warps of one tile read its partner ids from L2
+// together. Lane l owns plane word l of each 32-word window of the tile's entries and
+// walks its fired bits in order; its slots (each attraction, then its
+// negatives) start at the prefix of the lower lanes' slot counts, so every
+// (epoch, tile) segment holds the terms in the order of the reference's
+// serial sum. Negative draws (Philox counter (j, epoch, edge)) are queued in
+// shared memory and drawn 32 at a time.
+constexpr int DRAW_Q = 160;  // >= 31 left over + 32 lanes x 3 negatives
+struct DrawJob {
+  int64_t q;        // slot index
+  uint32_t eidx;    // edge id
+  uint32_t jn;      // draw index j | tile-local node << 8
 };
+struct PlaneFillSmem {
+  DrawJob job[DRAW_Q];
+  int64_t pb[TILE + 1];  // incidence offsets of the tile's nodes (entry -> node)
+  int64_t eb[TILE];      // edge-id bases of the tile's nodes
+};
+
+// Draws the first `cnt` queued jobs, one per lane, and writes their slots.
+__device__ __forceinline__ void drain_jobs(const DrawJob* __restrict__ job, int cnt, int lane,
+                                           int32_t t, int64_t v0, uint32_t n_total,
+                                           uint64_t seed,
+                                           const uint32_t* __restrict__ prob_of_node,
+                                           const ProbInfo* __restrict__ prob,
+                                           uint2* __restrict__ slots) {
+  if (lane < cnt) {
+    const DrawJob jb = job[lane];
+    const uint32_t node = jb.jn >> 8;
+    uint32_t nb = 0, np = n_total;
+    uint64_t sd = seed;
+    if (prob_of_node) {
+      const ProbInfo pi = prob[prob_of_node[v0 + node]];
+      nb = pi.node_base;
+      np = pi.n;
+      sd = pi.seed;
+    }
+    slots[jb.q] = make_uint2(nb + negative_draw(sd, jb.jn & 0xffu, (uint32_t)t, jb.eidx, np),
+                             node | 32u);
+  }
+}
 
 __global__ void __launch_bounds__(128) k_plane_fill(
     const int64_t* __restrict__ inc_ptr, const uint32_t* __restrict__ inc_other,
@@ -954,101 +999,79 @@ __global__ void __launch_bounds__(128) k_plane_fill(
   PlaneFillSmem& sm = sm_all[threadIdx.x >> 5];
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  const int64_t tile = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (tile >= ntiles) return;
+  const int64_t item = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (item >= (int64_t)ne * ntiles) return;
+  const int64_t tile = item / ne;
+  const int32_t t = (int32_t)(item - tile * ne);
   const int64_t v0 = tile * TILE;
   const int nt = (int)min((int64_t)TILE, n - v0);
-  const int64_t pbl = inc_ptr[v0 + min(lane, nt)];  // lanes >= nt hold the end
-  const int64_t ebl = (lane < nt) ? eidx_base[v0 + lane] : 0;
-  const int64_t P0 = __shfl_sync(FULL, pbl, 0);
-  const int64_t P1 = inc_ptr[v0 + nt];
+  sm.pb[lane] = inc_ptr[v0 + min(lane, nt)];  // lanes >= nt hold the end
+  if (lane == 0) sm.pb[TILE] = inc_ptr[v0 + nt];
+  sm.eb[lane] = (lane < nt) ? eidx_base[v0 + lane] : 0;
+  __syncwarp();
+  const int64_t P0 = sm.pb[0];
+  const int64_t P1 = sm.pb[nt];
   if (P1 <= P0) return;
   const int64_t wb = P0 >> 5, we = ((P1 - 1) >> 5) + 1;
   const uint32_t lo_mask = ~0u << (P0 & 31);
   const uint32_t hi_mask = ~0u >> (31 - (int)((P1 - 1) & 31));
-  const uint32_t n_total = (uint32_t)n;
-  for (int32_t t = 0; t < ne; ++t) {
-    const int64_t po = (int64_t)t * W;
-    int64_t cur = tile_off[(int64_t)t * ntiles + tile];
-    for (int64_t ws = wb; ws < we; ws += 64) {
-      const uint32_t xa = tile_word(fplane + po, ws + lane, wb, we, lo_mask, hi_mask);
-      const uint32_t xb = tile_word(fplane + po, ws + 32 + lane, wb, we, lo_mask, hi_mask);
-      const uint32_t na0 = xa ? nplane0[po + ws + lane] : 0u;
-      const uint32_t na1 = xa ? nplane1[po + ws + lane] : 0u;
-      const uint32_t nb0 = xb ? nplane0[po + ws + 32 + lane] : 0u;
-      const uint32_t nb1 = xb ? nplane1[po + ws + 32 + lane] : 0u;
-      const int ca = __popc(xa), cb = __popc(xb);
-      int ia = ca, ib = cb;
+  const int64_t po = (int64_t)t * W;
+  int64_t cur = tile_off[(int64_t)t * ntiles + tile];
+  int qn = 0;  // queued draws
+  for (int64_t ws = wb; ws < we; ws += 32) {
+    const int64_t w = ws + lane;
+    uint32_t x = tile_word(fplane + po, w, wb, we, lo_mask, hi_mask);
+    // negative bits are set only on fired entries: masking by x keeps the tile's
+    const uint32_t g0 = x ? nplane0[po + w] & x : 0u, g1 = x ? nplane1[po + w] & x : 0u;
+    const int cnt = __popc(x) + __popc(g0) + 2 * __popc(g1);
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(FULL, incl, o);
+      if (lane >= o) incl += y;
+    }
+    int64_t q = cur + incl - cnt;
+    cur += __shfl_sync(FULL, incl, 31);
+    const int iters = __reduce_max_sync(FULL, (unsigned)__popc(x));
+    int node = 0;  // node of this lane's current entry (entries only move forward)
+    for (int it = 0; it < iters; ++it) {
+      int nn = 0;
+      uint32_t eidx = 0;
+      int64_t q0 = 0;
+      if (x) {
+        const int b = __ffs(x) - 1;
+        x &= x - 1;
+        const int64_t p = (w << 5) + b;
+        while (node + 1 < nt && sm.pb[node + 1] <= p) ++node;
+        nn = (int)(((g0 >> b) & 1u) | (((g1 >> b) & 1u) << 1));
+        slots[q] = make_uint2(inc_other[p], (uint32_t)node);
+        q0 = q + 1;
+        q += 1 + nn;
+        eidx = (uint32_t)(p + sm.eb[node]);
+      }
+      // queue this iteration's draws: lane's nn jobs after the lower lanes'
+      int ni = nn;
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        const int ya = __shfl_up_sync(FULL, ia, o), yb = __shfl_up_sync(FULL, ib, o);
-        if (lane >= o) {
-          ia += ya;
-          ib += yb;
-        }
+        const int y = __shfl_up_sync(FULL, ni, o);
+        if (lane >= o) ni += y;
       }
-      const int tot_a = __shfl_sync(FULL, ia, 31);
-      const int total = tot_a + __shfl_sync(FULL, ib, 31);
-      if (total == 0) continue;
-      __syncwarp();  // readers of the previous window are done
-      sm.f[lane] = xa;
-      sm.f[lane + 32] = xb;
-      sm.n0[lane] = na0;
-      sm.n0[lane + 32] = nb0;
-      sm.n1[lane] = na1;
-      sm.n1[lane + 32] = nb1;
-      sm.ex[lane] = ia - ca;
-      sm.ex[lane + 32] = tot_a + ib - cb;
+      const int add = __shfl_sync(FULL, ni, 31);
+      if (add == 0) continue;
+      __syncwarp();  // earlier drains have read their jobs
+      for (int j = 0; j < nn; ++j)
+        sm.job[qn + ni - nn + j] = DrawJob{q0 + j, eidx, (uint32_t)j | ((uint32_t)node << 8)};
+      qn += add;
       __syncwarp();
-      for (int kb = 0; kb < total; kb += 32) {
-        const int k = kb + lane;
-        int wi = 0;  // word of event k: last wi with ex[wi] <= k
-#pragma unroll
-        for (int step = 32; step >= 1; step >>= 1)
-          if (wi + step < 64 && sm.ex[wi + step] <= k) wi += step;
-        const int r = k - sm.ex[wi];
-        const uint32_t fw = sm.f[wi];
-        const int u = nth_set_bit(fw, r);  // in range for any r
-        const int64_t p = ((ws + wi) << 5) + u;
-        int node = 0;
-#pragma unroll
-        for (int step = 16; step >= 1; step >>= 1) {
-          const int64_t st = __shfl_sync(FULL, pbl, node + step);
-          if (node + step < nt && st <= p) node += step;
-        }
-        const int64_t eb = __shfl_sync(FULL, ebl, node);
-        const bool ev = k < total;
-        const uint32_t nn =
-            ev ? ((sm.n0[wi] >> u) & 1u) | (((sm.n1[wi] >> u) & 1u) << 1) : 0u;
-        const int cnt = ev ? 1 + (int)nn : 0;
-        int incl = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const int y = __shfl_up_sync(FULL, incl, o);
-          if (lane >= o) incl += y;
-        }
-        if (ev) {
-          int64_t q = cur + incl - cnt;
-          slots[q] = make_uint2(inc_other[p], (uint32_t)node);
-          if (nn) {
-            const uint32_t eidx = (uint32_t)(p + eb);
-            uint32_t nb = 0, np = n_total;
-            uint64_t sd = seed;
-            if (prob_of_node) {
-              const ProbInfo pi = prob[prob_of_node[v0 + node]];
-              nb = pi.node_base;
-              np = pi.n;
-              sd = pi.seed;
-            }
-            for (uint32_t j = 0; j < nn; ++j)
-              slots[++q] = make_uint2(nb + negative_draw(sd, j, (uint32_t)t, eidx, np),
-                                      (uint32_t)node | 32u);
-          }
-        }
-        cur += __shfl_sync(FULL, incl, 31);
+      while (qn >= 32) {
+        drain_jobs(sm.job + (qn - 32), 32, lane, t, v0, (uint32_t)n, seed, prob_of_node, prob,
+                   slots);
+        qn -= 32;
       }
     }
   }
+  __syncwarp();
+  drain_jobs(sm.job, qn, lane, t, v0, (uint32_t)n, seed, prob_of_node, prob, slots);
 }
 
 // Count pass (general path): warp per tile; each lane runs the
@@ -1616,7 +1639,7 @@ static bool build_slots(evoc_plan* pl, const float* inc_ps, const uint8_t* inc_u
       npl0.alloc(pw, s);
       npl1.alloc(pw, s);
       k_inc_planes<<<(unsigned)((planes_w + PLANE_BLOCK_WORDS - 1) / PLANE_BLOCK_WORDS), 256,
-                     0, s>>>(inc_eidx, inc_up, pl->n_inc, planes_w, ne, efire.get(),
+                     0, s>>>(inc_eidx, inc_up, inc_ps, pl->n_inc, planes_w, ne, efire.get(),
                              eneg_lo.get(), eneg_hi.get(), fpl.get(), npl0.get(), npl1.get());
       EVOC_CHECK_LAUNCH();
       trace.mark("incidence planes");
@@ -1675,7 +1698,7 @@ static bool build_slots(evoc_plan* pl, const float* inc_ps, const uint8_t* inc_u
   const ProbInfo* pinfo = pl->n_problems > 1 ? pl->prob.get() : nullptr;
   const uint64_t seed0 = pl->seeds.empty() ? 0 : pl->seeds[0];
   if (use_planes) {
-    k_plane_fill<<<(unsigned)((pl->ntiles + 3) / 4), 128, 0, s>>>(
+    k_plane_fill<<<(unsigned)(((int64_t)ne * pl->ntiles + 3) / 4), 128, 0, s>>>(
         pl->inc_ptr.get(), pl->inc_other.get(), pl->eidx_base.get(), n, pl->ntiles, planes_w,
         ne, fpl.get(), npl0.get(), npl1.get(), off.get(), pon, pinfo, seed0, pl->slots.get());
   } else {
