@@ -262,6 +262,9 @@ def run_ours(args) -> dict:
     bytes_launch = float(hbm[act].mean())
     pk = peaks()
     achieved = bytes_launch / t_launch / 1e9
+    l2_peak = ctx.gather_peak(64 << 20)  # measured: random 32-B rows, L2-resident buffer
+    l2_launch = float(l2b[act].mean())
+    t_roof = max(bytes_launch / (pk["hbm_gbs"] * 1e9), l2_launch / (l2_peak * 1e9))
     traffic, traffic_src = profiled_traffic()
     if args.workload != "hierarchical_2m" or n != 2_000_000 or not info["n_slots"]:
         traffic, traffic_src = None, None
@@ -272,7 +275,12 @@ def run_ours(args) -> dict:
                 "peak_src": pk["src"], "kernel": "k_epoch_slot" if info["n_slots"] else "k_epoch",
                 "launch_ms": round(t_launch * 1e3, 4), "warps_per_block": info["warps_per_block"],
                 "epoch_path": "slots" if info["n_slots"] else "bit-planes",
-                "l2_gather_gbs": round(float(l2b[act].mean()) / t_launch / 1e9, 1)}
+                "l2": {"achieved": round(l2_launch / t_launch / 1e9, 1), "peak": round(l2_peak, 1),
+                       "unit": "GB/s", "frac": round(l2_launch / t_launch / 1e9 / l2_peak, 4),
+                       "gather_bytes_per_launch": round(l2_launch),
+                       "peak_src": "measured: evoc_gather_peak, random 32-B rows over 64 MB"},
+                "roofline_ms": round(t_roof * 1e3, 4),
+                "frac_of_roofline": round(t_roof / t_launch, 4)}
 
     res = {
         "metric": METRIC, "value": fired_per_step / (ms_step / 1e3), "unit": UNIT,

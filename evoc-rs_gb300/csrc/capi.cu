@@ -335,6 +335,16 @@ int evoc_plan_profile_epochs(evoc_plan_t* plan, const float* d_init,
   EVOC_API_END(ctx)
 }
 
+int evoc_gather_peak(evoc_ctx_t* ctx, int64_t bytes, double* gbs) {
+  EVOC_API_BEGIN
+  if (!ctx || !gbs) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (bytes < 32 || bytes > ((int64_t)1 << 36))
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "bytes out of range [32, 2^36]");
+  use_device(ctx);
+  *gbs = evoc::gather_peak(ctx, bytes);
+  EVOC_API_END(ctx)
+}
+
 int evoc_plan_info(const evoc_plan_t* plan, int64_t* n_edges,
                    int64_t* n_incidence, int32_t* neg_planes,
                    int32_t* warps_per_block, int64_t* n_slots) {

@@ -204,6 +204,9 @@ void plan_debug_run(evoc_plan* plan, const float* h_init, int32_t start_epoch,
 void plan_stats(const evoc_plan* plan, evoc_epoch_stats_t* stats);
 void plan_free(evoc_plan* plan);
 evoc_ctx* plan_ctx(const evoc_plan* plan);
+// Random 32-byte row gathers over an L2-resident buffer of `bytes`: GB/s
+// (measurement hook for the roofline's L2 bound).
+double gather_peak(evoc_ctx* ctx, int64_t bytes);
 void plan_info(const evoc_plan* plan, int64_t* n_edges, int64_t* n_inc,
                int32_t* planes, int32_t* wpb, int64_t* n_slots);
 int64_t plan_n(const evoc_plan* plan);

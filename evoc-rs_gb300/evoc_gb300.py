@@ -44,7 +44,7 @@ EXPORTED = [
     "evoc_plan_create", "evoc_plan_run_device", "evoc_plan_enqueue_device",
     "evoc_plan_profile_epochs", "evoc_plan_info", "evoc_plan_stats",
     "evoc_plan_debug_run", "evoc_plan_free", "evoc_embed_batched",
-    "evoc_knn_to_csr_noalloc",
+    "evoc_knn_to_csr_noalloc", "evoc_gather_peak",
 ]
 
 
@@ -122,6 +122,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "evoc_plan_run_device": ([vp, vp, vp], C.c_int),
         "evoc_plan_enqueue_device": ([vp, vp, vp], C.c_int),
         "evoc_plan_profile_epochs": ([vp, vp, vp, vp], C.c_int),
+        "evoc_gather_peak": ([vp, i64, C.POINTER(C.c_double)], C.c_int),
         "evoc_plan_info": ([vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i32),
                             C.POINTER(i32), C.POINTER(i64)], C.c_int),
         "evoc_plan_stats": ([vp, C.POINTER(EpochStatsC)], C.c_int),
@@ -267,6 +268,12 @@ class Context:
         if rc != EVOC_OK:
             raise EvocError(rc, self.lib.evoc_last_error(None).decode())
         self.handle = h
+
+    def gather_peak(self, nbytes: int = 64 << 20) -> float:
+        """Measured L2 random-gather GB/s for 32-byte rows over an nbytes buffer."""
+        g = C.c_double()
+        self._check(self.lib.evoc_gather_peak(self.handle, int(nbytes), C.byref(g)))
+        return g.value
 
     @property
     def stream(self) -> int:

@@ -230,6 +230,13 @@ EVOC_API int evoc_plan_enqueue_device(evoc_plan_t* plan, const float* d_init,
 EVOC_API int evoc_plan_profile_epochs(evoc_plan_t* plan, const float* d_init,
                                       float* d_out, float* epoch_ms);
 
+/* Measures the L2 random-gather bandwidth for 32-byte rows (one dim-8 f32
+ * row, the epoch kernel's source-row gather) over a device buffer of `bytes`
+ * (64 MB keeps it L2-resident): *gbs receives gathered GB/s, best of five
+ * timed launches after three warm-up launches. Measurement hook for the
+ * roofline's L2 bound (no counterpart). */
+EVOC_API int evoc_gather_peak(evoc_ctx_t* ctx, int64_t bytes, double* gbs);
+
 /* Layout facts of a plan (any pointer may be NULL): undirected edges,
  * per-node incidence entries (2 per edge), negative-count bit planes per
  * epoch, warps (32-node tiles) per thread block of the epoch kernel, and the
