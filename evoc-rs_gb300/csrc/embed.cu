@@ -1260,12 +1260,13 @@ __device__ __forceinline__ void slot_contrib(float (&c)[DIMP], bool neg,
                                              const float (&ev)[DIMP],
                                              const float (&row)[DIMP], float two_noise,
                                              float gamma4) {
-  float diff[DIMP];
+  float2 diff[DIMP / 2];
   float dsq = 0.0f;
 #pragma unroll
-  for (int d = 0; d < DIMP; ++d) {
-    diff[d] = fsub(ev[d], row[d]);
-    dsq = fadd(dsq, fmul(diff[d], diff[d]));
+  for (int h = 0; h < DIMP / 2; ++h) {
+    diff[h] = fsub2(make_float2(ev[2 * h], ev[2 * h + 1]), make_float2(row[2 * h], row[2 * h + 1]));
+    const float2 sq = fmul2(diff[h], diff[h]);
+    dsq = fadd(fadd(dsq, sq.x), sq.y);  // serial, dims in order
   }
   const float dist = fsqrt(dsq);
   const float num = neg ? gamma4 : fsub(-fmul(two_noise, dist), 2.0f);
@@ -1274,10 +1275,12 @@ __device__ __forceinline__ void slot_contrib(float (&c)[DIMP], bool neg,
   const float k = fdiv(num, den);
   const bool on = neg ? (dsq > 0.01f) : (dsq >= 1e-8f);
 #pragma unroll
-  for (int d = 0; d < DIMP; ++d) {
-    const float x = fmul(k, diff[d]);
-    const float y = neg ? fminf(fmaxf(x, -4.0f), 4.0f) : x;
-    c[d] = on ? y : 0.0f;
+  for (int h = 0; h < DIMP / 2; ++h) {
+    const float2 x = fmul2(make_float2(k, k), diff[h]);
+    const float y0 = neg ? fminf(fmaxf(x.x, -4.0f), 4.0f) : x.x;
+    const float y1 = neg ? fminf(fmaxf(x.y, -4.0f), 4.0f) : x.y;
+    c[2 * h] = on ? y0 : 0.0f;
+    c[2 * h + 1] = on ? y1 : 0.0f;
   }
 }
 
@@ -1379,10 +1382,12 @@ __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP>& sm
 #pragma unroll
         for (int q = 0; q < DIMP / 4; ++q) {
           const float4 x = cd[q];
-          g[4 * q] = fadd(g[4 * q], x.x);
-          g[4 * q + 1] = fadd(g[4 * q + 1], x.y);
-          g[4 * q + 2] = fadd(g[4 * q + 2], x.z);
-          g[4 * q + 3] = fadd(g[4 * q + 3], x.w);
+          const float2 lo = fadd2(make_float2(g[4 * q], g[4 * q + 1]), make_float2(x.x, x.y));
+          const float2 hi = fadd2(make_float2(g[4 * q + 2], g[4 * q + 3]), make_float2(x.z, x.w));
+          g[4 * q] = lo.x;
+          g[4 * q + 1] = lo.y;
+          g[4 * q + 2] = hi.x;
+          g[4 * q + 3] = hi.y;
         }
       }
     }
@@ -1432,7 +1437,9 @@ __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP>& sm
         vv[4 * i] = y.x; vv[4 * i + 1] = y.y; vv[4 * i + 2] = y.z; vv[4 * i + 3] = y.w;
       }
 #pragma unroll
-      for (int d = 0; d < DIMP; ++d) {
+#pragma unroll
+      for (int d = 0; d < DIMP; ++d) {  // scalar: a packed multiply feeding a packed
+        // add did not reproduce the unfused result
         mm[d] = fadd(mm[d], fmul(a.one_m_b1, fsub(g[d], mm[d])));
         vv[d] = fadd(vv[d], fmul(a.one_m_b2, fsub(fmul(g[d], g[d]), vv[d])));
         e[d] = fadd(e[d], fdiv(fmul(a.lr_ad, mm[d]), fadd(fsqrt(vv[d]), a.epsc)));

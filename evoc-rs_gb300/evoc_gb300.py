@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 from dataclasses import dataclass
 from pathlib import Path
 from typing import Sequence
@@ -157,6 +158,7 @@ class Graph:
     def __init__(self, ctx: "Context", handle: C.c_void_p):
         self._ctx = ctx
         self.handle = handle
+        ctx._children.add(self)
 
     @property
     def n(self) -> int:
@@ -187,9 +189,9 @@ class Graph:
         return rows, indices.astype(np.int64), weights
 
     def free(self) -> None:
-        if self.handle:
+        if self.handle and self._ctx.handle:  # a closed context freed it already
             self._ctx.lib.evoc_graph_free(self.handle)
-            self.handle = None
+        self.handle = None
 
     def __del__(self):
         try:
@@ -204,6 +206,7 @@ class Plan:
     def __init__(self, ctx: "Context", handle, n: int, dim: int, n_epochs: int):
         self._ctx = ctx
         self.handle = handle
+        ctx._children.add(self)
         self.n, self.dim, self.n_epochs = n, dim, n_epochs
 
     def run_device(self, d_init: int | None, d_out: int) -> None:
@@ -247,9 +250,9 @@ class Plan:
         return (out, grad) if want_grad else out
 
     def free(self) -> None:
-        if self.handle:
+        if self.handle and self._ctx.handle:  # a closed context freed it already
             self._ctx.lib.evoc_plan_free(self.handle)
-            self.handle = None
+        self.handle = None
 
     def __del__(self):
         try:
@@ -263,6 +266,7 @@ class Context:
 
     def __init__(self, device: int = 0, lib_path: str | None = None):
         self.lib = load_library(lib_path)
+        self._children = weakref.WeakSet()  # live graphs and plans, freed by close()
         h = C.c_void_p()
         rc = self.lib.evoc_ctx_create(device, C.byref(h))
         if rc != EVOC_OK:
@@ -285,7 +289,10 @@ class Context:
             raise EvocError(rc, self.lib.evoc_last_error(self.handle).decode())
 
     def close(self) -> None:
+        """Frees the context's live graphs and plans, then the context."""
         if getattr(self, "handle", None):
+            for child in list(self._children):
+                child.free()
             self.lib.evoc_ctx_destroy(self.handle)
             self.handle = None
 

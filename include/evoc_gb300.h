@@ -102,6 +102,8 @@ EVOC_API void evoc_embed_params_default(evoc_embed_params_t* p);
 /* Create a context on CUDA device `device`. Replaces the implicit rayon
  * global pool of the reference (no counterpart function). */
 EVOC_API int evoc_ctx_create(int device, evoc_ctx_t** out);
+/* Graphs and plans created on a context must be freed before the context is
+ * destroyed: they release their device memory on its stream. */
 EVOC_API void evoc_ctx_destroy(evoc_ctx_t* ctx);
 
 /* Message of the last failure on ctx (never NULL). With ctx == NULL the
