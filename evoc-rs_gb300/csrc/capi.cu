@@ -304,6 +304,24 @@ int evoc_plan_create(evoc_ctx_t* ctx, const evoc_graph_t* g, int32_t dim,
   EVOC_API_END(ctx)
 }
 
+int evoc_plan_create_batched(evoc_ctx_t* ctx, int32_t n_problems,
+                             const evoc_graph_t* const* graphs, int32_t dim,
+                             const evoc_embed_params_t* params, const uint64_t* seeds,
+                             evoc_plan_t** out_plan) {
+  EVOC_API_BEGIN
+  if (!ctx || n_problems <= 0 || !graphs || !params || !seeds || !out_plan)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "bad argument");
+  *out_plan = nullptr;
+  use_device(ctx);
+  std::vector<evoc::ProblemDesc> probs;
+  for (int32_t q = 0; q < n_problems; ++q) {
+    if (!graphs[q]) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL graph");
+    probs.push_back({graphs[q], seeds[q]});
+  }
+  *out_plan = evoc::plan_create(ctx, probs, dim, *params);
+  EVOC_API_END(ctx)
+}
+
 int evoc_plan_run_device(evoc_plan_t* plan, const float* d_init, float* d_out) {
   evoc_ctx* ctx = plan ? evoc::plan_ctx(plan) : nullptr;
   EVOC_API_BEGIN

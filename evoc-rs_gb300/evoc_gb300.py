@@ -45,7 +45,7 @@ EXPORTED = [
     "evoc_plan_create", "evoc_plan_run_device", "evoc_plan_enqueue_device",
     "evoc_plan_profile_epochs", "evoc_plan_info", "evoc_plan_stats",
     "evoc_plan_debug_run", "evoc_plan_free", "evoc_embed_batched",
-    "evoc_knn_to_csr_noalloc", "evoc_gather_peak",
+    "evoc_knn_to_csr_noalloc", "evoc_gather_peak", "evoc_plan_create_batched",
 ]
 
 
@@ -124,6 +124,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "evoc_plan_enqueue_device": ([vp, vp, vp], C.c_int),
         "evoc_plan_profile_epochs": ([vp, vp, vp, vp], C.c_int),
         "evoc_gather_peak": ([vp, i64, C.POINTER(C.c_double)], C.c_int),
+        "evoc_plan_create_batched": ([vp, i32, vp, i32, vp, vp, pp], C.c_int),
         "evoc_plan_info": ([vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i32),
                             C.POINTER(i32), C.POINTER(i64)], C.c_int),
         "evoc_plan_stats": ([vp, C.POINTER(EpochStatsC)], C.c_int),
@@ -381,6 +382,20 @@ class Context:
         self._check(self.lib.evoc_plan_create(self.handle, graph.handle, dim, C.byref(p),
                                               C.c_uint64(seed), C.byref(h)))
         return Plan(self, h, graph.n, dim, pr.n_epochs)
+
+    def plan_batched(self, graphs: Sequence[Graph], dim: int,
+                     params: EvocEmbeddingParams | None = None,
+                     seeds: Sequence[int] | None = None) -> Plan:
+        """One plan over many graphs; its device rows are the problems' rows in order."""
+        pr = params or EvocEmbeddingParams()
+        p = pr.to_c()
+        m = len(graphs)
+        gh = (C.c_void_p * m)(*[g.handle for g in graphs])
+        sd = (C.c_uint64 * m)(*(seeds if seeds is not None else [42] * m))
+        h = C.c_void_p()
+        self._check(self.lib.evoc_plan_create_batched(self.handle, m, gh, dim, C.byref(p), sd,
+                                                      C.byref(h)))
+        return Plan(self, h, sum(g.n for g in graphs), dim, pr.n_epochs)
 
     def embed_batched(self, graphs: Sequence[Graph], dim: int,
                       params: EvocEmbeddingParams | None = None,

@@ -215,6 +215,16 @@ EVOC_API int evoc_plan_create(evoc_ctx_t* ctx, const evoc_graph_t* g, int32_t di
                      const evoc_embed_params_t* params, uint64_t seed,
                      evoc_plan_t** out_plan);
 
+/* One plan over n_problems independent graphs (problem q uses seeds[q]): its
+ * device rows are the problems' rows concatenated in order, and every epoch
+ * is one launch over all of them. Each problem's result equals its own plan's
+ * bit for bit. The many coarse embeddings of label_prop.rs:466-479, or many
+ * clustering problems, run this way. */
+EVOC_API int evoc_plan_create_batched(evoc_ctx_t* ctx, int32_t n_problems,
+                                      const evoc_graph_t* const* graphs, int32_t dim,
+                                      const evoc_embed_params_t* params,
+                                      const uint64_t* seeds, evoc_plan_t** out_plan);
+
 /* Run the epoch loop from d_init (device n*dim, or NULL for the random
  * initialisation) and write d_out (device n*dim). d_init may equal d_out. */
 EVOC_API int evoc_plan_run_device(evoc_plan_t* plan, const float* d_init, float* d_out);

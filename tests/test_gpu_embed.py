@@ -234,3 +234,13 @@ def test_batched_equals_individual(ctx, oracle):
     outs = ctx.embed_batched(graphs, 4, p, inits=inits, seeds=seeds)
     for g, o, s, i0 in zip(graphs, outs, seeds, inits):
         _assert_bits(o, ctx.embed(g, 4, p, init=i0, seed=s))
+    # the device-resident batched plan: problems' rows concatenated in order
+    import torch
+    plan = ctx.plan_batched(graphs, 4, p, seeds=seeds)
+    d_out = torch.empty(plan.n, 4, dtype=torch.float32, device="cuda")
+    plan.run_device(None, d_out.data_ptr())
+    h = d_out.cpu().numpy()
+    base = 0
+    for g, s in zip(graphs, seeds):
+        _assert_bits(h[base:base + g.n], ctx.embed(g, 4, p, seed=s))
+        base += g.n
