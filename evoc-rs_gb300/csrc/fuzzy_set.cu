@@ -244,62 +244,113 @@ __global__ void k_forward_compact(const uint32_t* __restrict__ fcol,
   }
 }
 
-// Fuzzy union of row i: forward list (sorted by column) merged with the
-// backward list (sorted by source row). WRITE = false counts, true writes.
-template <bool WRITE>
-__global__ void k_union(const uint32_t* __restrict__ fcol,
-                        const float* __restrict__ fw,
-                        const int32_t* __restrict__ fcnt,
-                        const int64_t* __restrict__ bptr,
-                        const uint2* __restrict__ bvals, int64_t n, int32_t k,
-                        int32_t* __restrict__ out_cnt,
-                        const int64_t* __restrict__ out_ptr,
-                        uint32_t* __restrict__ out_idx,
-                        float* __restrict__ out_w) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// Fuzzy union of row i (fuzzy_graph.rs:193-205), warp per row: the forward
+// list (sorted by column, at most k entries) merged with the backward list
+// (sorted by source row). Each step loads the next 32 entries of both lists
+// (coalesced); every entry finds its rank in the other chunk by a shuffle
+// search, a column present in both is emitted once with both weights, and
+// only columns up to the smaller of the two chunks' last entries are final.
+// Emitted entries are placed by merged rank in shared memory, then the kept
+// ones (w_sym > 0) are written in order. Output goes to the row's scratch
+// region at i * k + bptr[i]; out_cnt[i] gets the kept count.
+__global__ void __launch_bounds__(256) k_union(const uint32_t* __restrict__ fcol,
+                                               const float* __restrict__ fw,
+                                               const int32_t* __restrict__ fcnt,
+                                               const int64_t* __restrict__ bptr,
+                                               const uint2* __restrict__ bvals, int64_t n,
+                                               int32_t k, int32_t* __restrict__ out_cnt,
+                                               uint2* __restrict__ tmp) {
+  __shared__ uint2 stage_all[8][64];
+  uint2* stage = stage_all[threadIdx.x >> 5];
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const uint32_t lt = (1u << lane) - 1u;
+  const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= n) return;
   const uint32_t* fa = fcol + i * (int64_t)k;
   const float* fwa = fw + i * (int64_t)k;
   const int32_t na = fcnt[i];
-  const int64_t b0 = bptr[i], b1 = bptr[i + 1];
+  const int64_t b0 = bptr[i], nb = bptr[i + 1] - b0;
+  const uint2* bv = bvals + b0;
+  uint2* out = tmp + i * (int64_t)k + b0;
   int32_t ia = 0;
-  int64_t ib = b0;
-  int64_t o = WRITE ? out_ptr[i] : 0;
+  int64_t ib = 0;
   int32_t cnt = 0;
-  uint32_t ca = (ia < na) ? fa[ia] : PAD;
-  uint2 bv = (ib < b1) ? bvals[ib] : make_uint2(PAD, 0);
-  while (ia < na || ib < b1) {
-    float w_ij = 0.0f, w_ji = 0.0f;
-    uint32_t j;
-    const uint32_t cb = (ib < b1) ? bv.x : PAD;
-    if (ia < na && (ib >= b1 || ca < cb)) {
-      j = ca;
-      w_ij = fwa[ia];
-      ++ia;
-    } else if (ia >= na || cb < ca) {
-      j = cb;
-      w_ji = __uint_as_float(bv.y);
-      ++ib;
-    } else {
-      j = ca;
-      w_ij = fwa[ia];
-      w_ji = __uint_as_float(bv.y);
-      ++ia;
-      ++ib;
+  while (ia < na || ib < nb) {
+    const bool has_a = ia + lane < na, has_b = ib + lane < nb;
+    const uint32_t a = has_a ? fa[ia + lane] : PAD;
+    const float wa = has_a ? fwa[ia + lane] : 0.0f;
+    const uint2 bb = has_b ? bv[ib + lane] : make_uint2(PAD, 0u);
+    const uint32_t b = bb.x;
+    const int ca = (int)min((int64_t)32, (int64_t)(na - ia));
+    const int cb = (int)min((int64_t)32, nb - ib);
+    // columns up to `bound` are final: every unread entry is larger
+    uint32_t bound = 0xffffffffu;
+    if (ia + 32 < na) bound = min(bound, __shfl_sync(FULL, a, 31));
+    if (ib + 32 < nb) bound = min(bound, __shfl_sync(FULL, b, 31));
+    // rank of a in the b chunk (# b < a) and of b in the a chunk (# a < b)
+    int ra = 0, rb = 0;
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1) {
+      if (__shfl_sync(FULL, b, ra + step - 1) < a) ra += step;
+      if (__shfl_sync(FULL, a, rb + step - 1) < b) rb += step;
     }
-    if (ia < na) ca = fa[ia];
-    if (ib < b1) bv = bvals[ib];
-    const float w_sym = fsub(fadd(w_ij, w_ji), fmul(w_ij, w_ji));
-    if (w_sym > 0.0f) {
-      if (WRITE) {
-        out_idx[o] = j;
-        out_w[o] = w_sym;
-        ++o;
-      }
-      ++cnt;
+    if (ra < 32 && __shfl_sync(FULL, b, ra) < a) ++ra;  // lanes past the chunk hold PAD
+    if (rb < 32 && __shfl_sync(FULL, a, rb) < b) ++rb;
+    const uint32_t b_at = __shfl_sync(FULL, b, ra & 31);
+    const uint32_t b_w = __shfl_sync(FULL, bb.y, ra & 31);
+    const uint32_t a_at = __shfl_sync(FULL, a, rb & 31);
+    const bool a_take = has_a && a <= bound;
+    const bool a_match = a_take && ra < cb && b_at == a;
+    const bool b_take = has_b && b <= bound;
+    const bool b_match = b_take && rb < ca && a_at == b;
+    const uint32_t ma = __ballot_sync(FULL, a_match), mb = __ballot_sync(FULL, b_match);
+    // merged rank = # distinct columns before this one among the taken entries
+    if (a_take) {
+      const float w_ji = a_match ? __uint_as_float(b_w) : 0.0f;
+      const float w_sym = fsub(fadd(wa, w_ji), fmul(wa, w_ji));
+      stage[lane + ra - __popc(ma & lt)] = make_uint2(a, __float_as_uint(w_sym));
     }
+    if (b_take && !b_match) {
+      const float w_ji = __uint_as_float(bb.y);
+      const float w_sym = fsub(fadd(0.0f, w_ji), fmul(0.0f, w_ji));
+      stage[lane + rb - __popc(mb & lt)] = make_uint2(b, __float_as_uint(w_sym));
+    }
+    const int na_t = __popc(__ballot_sync(FULL, a_take));
+    const int nb_t = __popc(__ballot_sync(FULL, b_take));
+    const int m = na_t + nb_t - __popc(ma);  // distinct columns emitted
+    __syncwarp();
+    // kept entries (w_sym > 0) in merged order
+    for (int base = 0; base < m; base += 32) {
+      const int e = base + lane;
+      const uint2 v = e < m ? stage[e] : make_uint2(0u, 0u);
+      const bool keep = e < m && __uint_as_float(v.y) > 0.0f;
+      const uint32_t kb = __ballot_sync(FULL, keep);
+      if (keep) out[cnt + __popc(kb & lt)] = v;
+      cnt += __popc(kb);
+    }
+    __syncwarp();
+    ia += na_t;
+    ib += nb_t;
   }
-  if (!WRITE) out_cnt[i] = cnt;
+  if (lane == 0) out_cnt[i] = cnt;
+}
+
+// Warp per row: the row's kept pairs from its scratch region into the CSR.
+__global__ void k_union_compact(const uint2* __restrict__ tmp,
+                                const int64_t* __restrict__ bptr, int64_t n, int32_t k,
+                                const int64_t* __restrict__ out_ptr,
+                                uint32_t* __restrict__ out_idx, float* __restrict__ out_w) {
+  const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (i >= n) return;
+  const uint2* src = tmp + i * (int64_t)k + bptr[i];
+  const int64_t dst = out_ptr[i], len = out_ptr[i + 1] - dst;
+  for (int64_t j = lane; j < len; j += 32) {
+    const uint2 v = src[j];
+    out_idx[dst + j] = v.x;
+    out_w[dst + j] = __uint_as_float(v.y);
+  }
 }
 
 // symmetrise == false: the directed COO of knn_to_coo in kNN order.
@@ -479,10 +530,13 @@ void fuzzy_set_device(evoc_ctx* ctx, const uint32_t* d_idx,
   trace.mark("transpose");
 
   DevBuf<int32_t> ucnt(n, s);
-  k_union<false><<<row_blocks, 256, 0, s>>>(fcol.get(), fw.get(), fcnt.get(),
-                                            bptr.get(), vals.get(), n, k,
-                                            ucnt.get(), nullptr, nullptr,
-                                            nullptr);
+  int64_t nb_total = 0;
+  EVOC_CUDA(cudaMemcpyAsync(&nb_total, bptr.get() + n, sizeof(int64_t),
+                            cudaMemcpyDeviceToHost, s));
+  EVOC_CUDA(cudaStreamSynchronize(s));
+  DevBuf<uint2> utmp(n * (int64_t)k + nb_total, s);
+  k_union<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(
+      fcol.get(), fw.get(), fcnt.get(), bptr.get(), vals.get(), n, k, ucnt.get(), utmp.get());
   EVOC_CHECK_LAUNCH();
   exclusive_scan_i32_to_i64(ucnt.get(), out->indptr.get(), n, s);
   int64_t nnz = 0;
@@ -492,15 +546,13 @@ void fuzzy_set_device(evoc_ctx* ctx, const uint32_t* d_idx,
   out->nnz = nnz;
   out->indices.alloc(nnz, s);
   out->weights.alloc(nnz, s);
-  trace.mark("union count");
-  k_union<true><<<row_blocks, 256, 0, s>>>(fcol.get(), fw.get(), fcnt.get(),
-                                           bptr.get(), vals.get(), n, k,
-                                           nullptr, out->indptr.get(),
-                                           out->indices.get(),
-                                           out->weights.get());
+  trace.mark("union merge");
+  k_union_compact<<<(unsigned)((n * 32 + 255) / 256), 256, 0, s>>>(
+      utmp.get(), bptr.get(), n, k, out->indptr.get(), out->indices.get(),
+      out->weights.get());
   EVOC_CHECK_LAUNCH();
   out->canonical = true;
-  trace.mark("union write");
+  trace.mark("union compact");
   EVOC_CUDA(cudaStreamSynchronize(s));
 }
 
