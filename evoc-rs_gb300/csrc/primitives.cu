@@ -171,55 +171,88 @@ __global__ void k_radix_hist(const uint32_t* __restrict__ keys, int64_t n,
   counts[(int64_t)threadIdx.x * tiles + blockIdx.x] = hist[threadIdx.x];
 }
 
-__global__ void k_radix_scatter(const uint32_t* __restrict__ keys_in,
-                                const uint2* __restrict__ vals_in, int64_t n,
-                                int shift, int64_t tiles,
-                                const int64_t* __restrict__ offsets,
-                                uint32_t* __restrict__ keys_out,
-                                uint2* __restrict__ vals_out) {
-  __shared__ int64_t digit_base[256];
-  __shared__ int32_t warp_cnt[RS_WARPS][256];
-  __shared__ int64_t warp_off[RS_WARPS][256];
+// Scatter of one 8-bit digit pass, tile per block. The tile is first sorted
+// by digit in shared memory (stable: rounds in element order, lanes ranked by
+// __match_any_sync, warps by per-digit prefix), then written out in digit
+// order, so each digit's elements of the tile leave as one contiguous run.
+struct RadixSmem {
+  uint32_t keys[RS_TILE];
+  uint2 vals[RS_TILE];
+  int32_t warp_cnt[2][RS_WARPS][256];  // per round (alternating): counts, then offsets
+  int32_t run[256];                 // elements of each digit placed so far
+  int32_t tile_start[256];          // digit segment starts within the tile
+  int64_t digit_base[256];          // the segments' global starts
+};
+
+__global__ void __launch_bounds__(RS_THREADS) k_radix_scatter(
+    const uint32_t* __restrict__ keys_in, const uint2* __restrict__ vals_in, int64_t n,
+    int shift, int64_t tiles, const int32_t* __restrict__ counts,
+    const int64_t* __restrict__ offsets, uint32_t* __restrict__ keys_out,
+    uint2* __restrict__ vals_out) {
+  extern __shared__ __align__(16) unsigned char rs_raw[];
+  RadixSmem& sm = *reinterpret_cast<RadixSmem*>(rs_raw);
+  const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int dd = threadIdx.x;  // the digit this thread keeps offsets for
-  digit_base[dd] = offsets[(int64_t)dd * tiles + blockIdx.x];
-  for (int w = 0; w < RS_WARPS; ++w) warp_cnt[w][dd] = 0;
+  const int dd = threadIdx.x;  // the digit this thread keeps bookkeeping for
+  const int32_t c_dd = counts[(int64_t)dd * tiles + blockIdx.x];
+  // exclusive prefix of the tile's digit counts (block scan over 256 digits)
+  int32_t x = c_dd;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int32_t y = __shfl_up_sync(FULL, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sm.run[warp] = x;  // warp totals (run is reset below)
+  __syncthreads();
+  int32_t before = 0;
+  for (int w = 0; w < warp; ++w) before += sm.run[w];
+  __syncthreads();
+  sm.tile_start[dd] = before + x - c_dd;
+  sm.digit_base[dd] = offsets[(int64_t)dd * tiles + blockIdx.x];
+  sm.run[dd] = 0;
+  for (int w = 0; w < RS_WARPS; ++w) sm.warp_cnt[0][w][dd] = sm.warp_cnt[1][w][dd] = 0;
   __syncthreads();
   const uint32_t lt_mask = (1u << lane) - 1u;
   const int64_t base = (int64_t)blockIdx.x * RS_TILE;
+  const int tile_n = (int)min((int64_t)RS_TILE, n - base);
   for (int r = 0; r < RS_ROUNDS; ++r) {
-    const int64_t g = base + r * RS_THREADS + threadIdx.x;
-    const bool valid = g < n;
+    const int e = r * RS_THREADS + threadIdx.x;
+    const bool valid = e < tile_n;
     uint32_t key = 0;
     uint2 val = make_uint2(0, 0);
     uint32_t d = 256;  // lanes past the end form their own peer group
     if (valid) {
-      key = keys_in[g];
-      val = vals_in[g];
+      key = keys_in[base + e];
+      val = vals_in[base + e];
       d = (key >> shift) & 255u;
     }
-    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t peers = __match_any_sync(FULL, d);
     const int rank = __popc(peers & lt_mask);
-    if (valid && rank == 0) warp_cnt[warp][d] = __popc(peers);
+    int32_t (*wc)[256] = sm.warp_cnt[r & 1];
+    if (valid && rank == 0) wc[warp][d] = __popc(peers);
     __syncthreads();
-    // Output offset of digit dd for each warp of this round; advance the
-    // digit's running base by the round's total. Counts are cleared for the
-    // next round.
-    int64_t run = digit_base[dd];
+    int32_t o = sm.run[dd];  // this round's warp offsets for digit dd
     for (int w = 0; w < RS_WARPS; ++w) {
-      const int32_t c = warp_cnt[w][dd];
-      warp_cnt[w][dd] = 0;
-      warp_off[w][dd] = run;
-      run += c;
+      const int32_t c = wc[w][dd];
+      wc[w][dd] = o;
+      o += c;
+      sm.warp_cnt[(r + 1) & 1][w][dd] = 0;  // last read before this round's first barrier
     }
-    digit_base[dd] = run;
+    sm.run[dd] = o;
     __syncthreads();
     if (valid) {
-      const int64_t pos = warp_off[warp][d] + rank;
-      keys_out[pos] = key;
-      vals_out[pos] = val;
+      const int pos = sm.tile_start[d] + wc[warp][d] + rank;
+      sm.keys[pos] = key;
+      sm.vals[pos] = val;
     }
-    // warp_off is rewritten only after the next round's first barrier.
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < tile_n; e += RS_THREADS) {
+    const uint32_t key = sm.keys[e];
+    const uint32_t d = (key >> shift) & 255u;
+    const int64_t pos = sm.digit_base[d] + (e - sm.tile_start[d]);
+    keys_out[pos] = key;
+    vals_out[pos] = sm.vals[e];
   }
 }
 
@@ -239,6 +272,9 @@ void radix_sort_pairs(uint32_t* keys, uint2* vals, int64_t n, int key_bits,
                       cudaStream_t s) {
   if (n <= 1 || key_bits <= 0) return;
   const int passes = (key_bits + 7) / 8;
+  EVOC_CUDA(cudaFuncSetAttribute((const void*)k_radix_scatter,  // the staged tile > 48 KB
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sizeof(RadixSmem)));
   const int64_t tiles = (n + RS_TILE - 1) / RS_TILE;
   DevBuf<uint32_t> k2(n, s);
   DevBuf<uint2> v2(n, s);
@@ -254,8 +290,8 @@ void radix_sort_pairs(uint32_t* keys, uint2* vals, int64_t n, int key_bits,
                                                        counts.get());
     EVOC_CHECK_LAUNCH();
     exclusive_scan_i32_to_i64(counts.get(), offsets.get(), 256 * tiles, s);
-    k_radix_scatter<<<(unsigned)tiles, RS_THREADS, 0, s>>>(
-        kin, vin, n, shift, tiles, offsets.get(), kout, vout);
+    k_radix_scatter<<<(unsigned)tiles, RS_THREADS, sizeof(RadixSmem), s>>>(
+        kin, vin, n, shift, tiles, counts.get(), offsets.get(), kout, vout);
     EVOC_CHECK_LAUNCH();
     std::swap(kin, kout);
     std::swap(vin, vout);
