@@ -770,21 +770,26 @@ __global__ void k_edge_sched(const float* __restrict__ e_ps, int64_t U, int32_t 
   const bool valid = e < U;
   Sched sc;
   sc.init(valid ? e_ps[e] : 3.0e38f, neg_factor, valid);
-  unsigned long long fm = 0, n0 = 0, n1 = 0;
+  uint32_t fm[2] = {0u, 0u}, n0[2] = {0u, 0u}, n1[2] = {0u, 0u};  // epochs 0-31, 32-63
   float mx = 0.0f;
-  for (int32_t t = 0; t < ne; ++t) {
-    float c = 0.0f;
-    const bool f = valid && sc.stepf((float)t, &c);
-    if (f) fm |= 1ull << t;
-    const uint32_t c3 = c >= 3.0f ? 3u : (uint32_t)c;
-    n0 |= (unsigned long long)(c3 & 1u) << t;
-    n1 |= (unsigned long long)(c3 >> 1) << t;
-    mx = fmaxf(mx, c);
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int32_t t_end = min(ne, 32 * (h + 1));
+    for (int32_t t = 32 * h; t < t_end; ++t) {
+      float c = 0.0f;
+      const bool f = valid && sc.stepf((float)t, &c);
+      const uint32_t c3 = c >= 3.0f ? 3u : (uint32_t)c;
+      const int b = t - 32 * h;
+      fm[h] |= (f ? 1u : 0u) << b;
+      n0[h] |= (c3 & 1u) << b;
+      n1[h] |= (c3 >> 1) << b;
+      mx = fmaxf(mx, c);
+    }
   }
   if (valid) {
-    fire_mask[e] = fm;
-    neg_lo[e] = n0;
-    neg_hi[e] = n1;
+    fire_mask[e] = ((unsigned long long)fm[1] << 32) | fm[0];
+    neg_lo[e] = ((unsigned long long)n0[1] << 32) | n0[0];
+    neg_hi[e] = ((unsigned long long)n1[1] << 32) | n1[0];
   }
   for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, o));
   if ((threadIdx.x & 31) == 0 && mx > 0.0f)
@@ -851,13 +856,17 @@ __global__ void __launch_bounds__(256) k_inc_planes(
   for (int j = 0; j < J; ++j) {  // lower entries: fires only (embedding.rs:274-279)
     if (ok[j] && !up[j]) {
       float ns = ps[j];
-      unsigned long long m = 0;
-      for (int32_t t = 0; t < ne; ++t) {
-        const float tf = (float)t;
-        if (!(ns > tf)) m |= 1ull << t;
-        if (ns <= tf) ns = fadd(ns, ps[j]);
+      uint32_t m[2] = {0u, 0u};
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int32_t t_end = min(ne, 32 * (h + 1));
+        for (int32_t t = 32 * h; t < t_end; ++t) {
+          const float tf = (float)t;
+          m[h] |= (!(ns > tf) ? 1u : 0u) << (t - 32 * h);
+          if (ns <= tf) ns = fadd(ns, ps[j]);
+        }
       }
-      fm[j] = m;
+      fm[j] = ((unsigned long long)m[1] << 32) | m[0];
     }
   }
 #pragma unroll
@@ -1049,18 +1058,21 @@ __global__ void __launch_bounds__(128) k_plane_fill(
         q += 1 + nn;
         eidx = (uint32_t)(p + sm.eb[node]);
       }
-      // queue this iteration's draws: lane's nn jobs after the lower lanes'
-      int ni = nn;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(FULL, ni, o);
-        if (lane >= o) ni += y;
-      }
-      const int add = __shfl_sync(FULL, ni, 31);
+      // queue this iteration's draws, level by level (draw j of every lane with
+      // more than j negatives); their order in the queue does not matter
+      const uint32_t lt = (1u << lane) - 1u;
+      const uint32_t b1 = __ballot_sync(FULL, nn >= 1), b2 = __ballot_sync(FULL, nn >= 2),
+                     b3 = __ballot_sync(FULL, nn >= 3);
+      const int c1 = __popc(b1), c2 = __popc(b2);
+      const int add = c1 + c2 + __popc(b3);
       if (add == 0) continue;
       __syncwarp();  // earlier drains have read their jobs
-      for (int j = 0; j < nn; ++j)
-        sm.job[qn + ni - nn + j] = DrawJob{q0 + j, eidx, (uint32_t)j | ((uint32_t)node << 8)};
+      if (nn >= 1) sm.job[qn + __popc(b1 & lt)] = DrawJob{q0, eidx, (uint32_t)node << 8};
+      if (nn >= 2)
+        sm.job[qn + c1 + __popc(b2 & lt)] = DrawJob{q0 + 1, eidx, 1u | ((uint32_t)node << 8)};
+      if (nn >= 3)
+        sm.job[qn + c1 + c2 + __popc(b3 & lt)] =
+            DrawJob{q0 + 2, eidx, 2u | ((uint32_t)node << 8)};
       qn += add;
       __syncwarp();
       while (qn >= 32) {
