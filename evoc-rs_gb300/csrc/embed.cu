@@ -75,7 +75,9 @@ struct evoc_plan {
   evoc::DevBuf<uint32_t> planes;
   evoc::DevBuf<uint32_t> prob_of_node;  // batched only
   evoc::DevBuf<evoc::ProbInfo> prob;    // batched only
-  evoc::DevBuf<float> e0, e1, m, v, grad;
+  evoc::DevBuf<float> emb, m, v, grad;  // emb: both embedding buffers
+  float* e0 = nullptr;                  // ping-pong halves of emb
+  float* e1 = nullptr;
   std::vector<float> lr_ad, epsc, gamma;
   float one_m_b1 = 0, one_m_b2 = 0;
   std::vector<evoc_epoch_stats_t> stats;
@@ -1869,8 +1871,9 @@ evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
                             cudaMemcpyDeviceToHost, s));
   EVOC_CUDA(cudaStreamSynchronize(s));
   pl->n_edges = U;
-  pl->e0.alloc(n * pl->dimp, s);
-  pl->e1.alloc(n * pl->dimp, s);
+  pl->emb.alloc(2 * n * pl->dimp, s);
+  pl->e0 = pl->emb.get();
+  pl->e1 = pl->emb.get() + n * pl->dimp;
   if (U == 0) {  // embedding.rs:92-96
     pl->has_edges = false;
     return pl.release();
@@ -2035,11 +2038,11 @@ void plan_stats(const evoc_plan* cpl, evoc_epoch_stats_t* out) {
 static void load_init(evoc_plan* pl, const float* d_init, cudaStream_t s) {
   const int64_t tot = pl->n * pl->dimp;
   if (d_init) {
-    k_pad<<<blocks_for(tot), 256, 0, s>>>(d_init, pl->e0.get(), pl->n, pl->dim,
+    k_pad<<<blocks_for(tot), 256, 0, s>>>(d_init, pl->e0, pl->n, pl->dim,
                                           pl->dimp);
   } else {
     k_init_random<<<blocks_for(tot), 256, 0, s>>>(
-        pl->e0.get(), pl->n, pl->dim, pl->dimp,
+        pl->e0, pl->n, pl->dim, pl->dimp,
         pl->n_problems > 1 ? pl->prob_of_node.get() : nullptr,
         pl->n_problems > 1 ? pl->prob.get() : nullptr,
         pl->seeds.empty() ? 0 : pl->seeds[0]);
@@ -2062,8 +2065,8 @@ void plan_run_device(evoc_plan* pl, const float* d_init, float* d_out) {
       EVOC_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
       try {
         for (int32_t t = 0; t < ne; ++t) {
-          const float* cur = (t & 1) ? pl->e1.get() : pl->e0.get();
-          float* nxt = (t & 1) ? pl->e0.get() : pl->e1.get();
+          const float* cur = (t & 1) ? pl->e1 : pl->e0;
+          float* nxt = (t & 1) ? pl->e0 : pl->e1;
           launch_epoch(pl, t, cur, nxt, nullptr, s);
         }
       } catch (...) {
@@ -2077,7 +2080,7 @@ void plan_run_device(evoc_plan* pl, const float* d_init, float* d_out) {
     }
     EVOC_CUDA(cudaGraphLaunch(pl->graph_exec, s));
   }
-  const float* fin = (pl->has_edges && (ne & 1)) ? pl->e1.get() : pl->e0.get();
+  const float* fin = (pl->has_edges && (ne & 1)) ? pl->e1 : pl->e0;
   k_unpad<<<blocks_for(n * pl->dim), 256, 0, s>>>(fin, d_out, n, pl->dim, pl->dimp);
   EVOC_CHECK_LAUNCH();
 }
@@ -2090,7 +2093,7 @@ void plan_profile_epochs(evoc_plan* pl, const float* d_init, float* d_out,
   for (int32_t t = 0; t < ne; ++t) epoch_ms[t] = 0.0f;
   if (n == 0) return;
   load_init(pl, d_init, s);
-  const float* fin = pl->e0.get();
+  const float* fin = pl->e0;
   if (pl->has_edges && ne > 0) {
     EVOC_CUDA(cudaMemsetAsync(pl->m.get(), 0, pl->m.bytes(), s));
     EVOC_CUDA(cudaMemsetAsync(pl->v.get(), 0, pl->v.bytes(), s));
@@ -2101,8 +2104,8 @@ void plan_profile_epochs(evoc_plan* pl, const float* d_init, float* d_out,
       for (auto& e : ev) EVOC_CUDA(cudaEventCreate(&e));
       EVOC_CUDA(cudaEventRecord(ev[0], s));
       for (int32_t t = 0; t < ne; ++t) {
-        const float* cur = (t & 1) ? pl->e1.get() : pl->e0.get();
-        float* nxt = (t & 1) ? pl->e0.get() : pl->e1.get();
+        const float* cur = (t & 1) ? pl->e1 : pl->e0;
+        float* nxt = (t & 1) ? pl->e0 : pl->e1;
         launch_epoch(pl, t, cur, nxt, nullptr, s);
         EVOC_CUDA(cudaEventRecord(ev[t + 1], s));
         fin = nxt;
@@ -2144,7 +2147,7 @@ void plan_debug_run(evoc_plan* pl, const float* h_init, int32_t start_epoch,
     grad.alloc(n * pl->dimp, s);
     EVOC_CUDA(cudaMemsetAsync(grad.get(), 0, grad.bytes(), s));
   }
-  const float* fin = pl->e0.get();
+  const float* fin = pl->e0;
   if (pl->has_edges && e1 > e0) {
     EVOC_CUDA(cudaMemsetAsync(pl->m.get(), 0, pl->m.bytes(), s));
     EVOC_CUDA(cudaMemsetAsync(pl->v.get(), 0, pl->v.bytes(), s));
@@ -2152,8 +2155,8 @@ void plan_debug_run(evoc_plan* pl, const float* h_init, int32_t start_epoch,
       EVOC_CUDA(cudaMemsetAsync(pl->work_ctr.get(), 0, pl->work_ctr.bytes(), s));
     for (int32_t t = e0; t < e1; ++t) {
       const int k = t - e0;
-      const float* cur = (k & 1) ? pl->e1.get() : pl->e0.get();
-      float* nxt = (k & 1) ? pl->e0.get() : pl->e1.get();
+      const float* cur = (k & 1) ? pl->e1 : pl->e0;
+      float* nxt = (k & 1) ? pl->e0 : pl->e1;
       launch_epoch(pl, t, cur, nxt, (t == e1 - 1) ? grad.get() : nullptr, s);
       fin = nxt;
     }
