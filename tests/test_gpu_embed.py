@@ -244,3 +244,26 @@ def test_batched_equals_individual(ctx, oracle):
     for g, s in zip(graphs, seeds):
         _assert_bits(h[base:base + g.n], ctx.embed(g, 4, p, seed=s))
         base += g.n
+
+
+def test_gather_peak_measures_and_rejects_bad_sizes(ctx):
+    import evoc_gb300 as E
+    gbs = ctx.gather_peak(8 << 20)
+    assert 50.0 < gbs < 100000.0
+    with pytest.raises(E.EvocError) as ei:
+        ctx.gather_peak(16)
+    assert ei.value.code == E.EVOC_ERR_INVALID_ARGUMENT
+
+
+def test_closing_a_context_frees_its_graphs_and_plans():
+    """Graphs and plans must not outlive their context's stream: closing the
+    context frees them first, and their later finalisers do nothing."""
+    import evoc_gb300 as E
+    c2 = E.Context(0)
+    g = c2.graph_from_adjacency([[(1, 1.0)], [(0, 1.0)]])
+    p = c2.plan(g, 4)
+    c2.close()
+    assert g.handle is None and p.handle is None
+    g.free()
+    p.free()
+    del g, p
