@@ -1468,8 +1468,8 @@ __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP>& sm
     }
     float4* eo = reinterpret_cast<float4*>(a.e_next + q);
 #pragma unroll
-    for (int i = 0; i < DIMP / 4; ++i)
-      eo[i] = make_float4(e[4 * i], e[4 * i + 1], e[4 * i + 2], e[4 * i + 3]);
+    for (int i = 0; i < DIMP / 4; ++i)  // evict-first: keep e_cur's rows in L2 for the gathers
+      __stcs(eo + i, make_float4(e[4 * i], e[4 * i + 1], e[4 * i + 2], e[4 * i + 3]));
     if (a.grad_out) {
       float4* go = reinterpret_cast<float4*>(a.grad_out + q);
 #pragma unroll
