@@ -1248,19 +1248,20 @@ __global__ void k_slot_stats(const int64_t* __restrict__ tile_off,
 // into shared memory, SLOT_U slots at a time with all loads and gathers
 // issued first; the first slot of each node run records its position.
 // Phase 2: the slots are node-major in the order of the reference's serial
-// sum (embedding.rs:194-253); lane l adds the run of node v0 + l onto its
-// running gradient in registers, except that a run longer than SLOT_LONG (a
-// hub) is added by DIMP lanes, one dim each, through shared memory.
+// sum (embedding.rs:194-253); each node present in the window is summed by
+// SLOT_PARTS lanes, each adding its DIMP / SLOT_PARTS dims of the node's run,
+// in slot order, onto the node's running gradient in shared memory.
 // Then Adam (embedding.rs:256-272), lane per node.
 constexpr int SLOT_WIN = 128;
 constexpr int SLOT_U = 2;
-constexpr int SLOT_LONG = 64;
+template <int DIMP>
+constexpr int slot_parts() { return DIMP >= 8 ? 2 : 1; }
 
 template <int DIMP>
 struct alignas(16) SlotSmem {
   float rows[TILE][DIMP];      // e_cur rows of the tile's nodes
   float c[SLOT_WIN][DIMP];     // contributions of the window's slots
-  float S[TILE][DIMP + 1];     // running gradients of nodes with a long run
+  float S[TILE][DIMP];         // running gradients
   int32_t start[TILE];         // first window slot of each node's run (or none)
   int32_t end[TILE];           // one past its last
 };
@@ -1353,12 +1354,11 @@ __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP>& sm
     const float4* src = reinterpret_cast<const float4*>(a.e_cur + (size_t)v0 * DIMP);
     float4* dst = reinterpret_cast<float4*>(&sm.rows[0][0]);
     for (int i = lane; i < nt * (DIMP / 4); i += 32) dst[i] = __ldg(src + i);
+    float4* sz = reinterpret_cast<float4*>(&sm.S[0][0]);
+    for (int i = lane; i < TILE * (DIMP / 4); i += 32) sz[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   const float two_noise = fmul(2.0f, a.noise);
   const float gamma4 = fmul(a.gamma, 4.0f);
-  float g[DIMP];
-#pragma unroll
-  for (int d = 0; d < DIMP; ++d) g[d] = 0.0f;
   uint32_t act_mask = 0;
   for (int64_t w0 = s0; w0 < s1; w0 += SLOT_WIN) {
     const int wn = (int)min((int64_t)SLOT_WIN, s1 - w0);
@@ -1382,50 +1382,30 @@ __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP>& sm
     }
     int en = __shfl_down_sync(FULL, sfx, 1);
     if (lane == 31) en = wn;
-    const bool has = st != SLOT_WIN;
-    const bool is_long = has && en - st > SLOT_LONG;
-    const uint32_t longs = __ballot_sync(FULL, is_long);
-    if (is_long) {  // hand the running sum to the dim lanes
-      sm.end[lane] = en;
+    sm.end[lane] = en;
+    const uint32_t present = __ballot_sync(FULL, st != SLOT_WIN);
+    __syncwarp();
+    constexpr int PARTS = slot_parts<DIMP>(), PD = DIMP / PARTS;  // dims per lane
+    const int ntask = __popc(present) * PARTS;
+    for (int tsk = lane; tsk < ntask; tsk += 32) {
+      const int node = nth_set_bit(present, tsk / PARTS), d0 = (tsk % PARTS) * PD;
+      const int s2b = sm.start[node], s2e = sm.end[node];
+      float4* srow = reinterpret_cast<float4*>(&sm.S[node][d0]);
+      float4 acc[PD / 4];
 #pragma unroll
-      for (int d = 0; d < DIMP; ++d) sm.S[lane][d] = g[d];
-    }
-    if (has && !is_long) {
-      for (int s2 = st; s2 < en; ++s2) {
-        const float4* cd = reinterpret_cast<const float4*>(&sm.c[s2][0]);
+      for (int q = 0; q < PD / 4; ++q) acc[q] = srow[q];
+      for (int s2 = s2b; s2 < s2e; ++s2) {
+        const float4* cd = reinterpret_cast<const float4*>(&sm.c[s2][d0]);
 #pragma unroll
-        for (int q = 0; q < DIMP / 4; ++q) {
+        for (int q = 0; q < PD / 4; ++q) {
           const float4 x = cd[q];
-          const float2 lo = fadd2(make_float2(g[4 * q], g[4 * q + 1]), make_float2(x.x, x.y));
-          const float2 hi = fadd2(make_float2(g[4 * q + 2], g[4 * q + 3]), make_float2(x.z, x.w));
-          g[4 * q] = lo.x;
-          g[4 * q + 1] = lo.y;
-          g[4 * q + 2] = hi.x;
-          g[4 * q + 3] = hi.y;
+          const float2 lo = fadd2(make_float2(acc[q].x, acc[q].y), make_float2(x.x, x.y));
+          const float2 hi = fadd2(make_float2(acc[q].z, acc[q].w), make_float2(x.z, x.w));
+          acc[q] = make_float4(lo.x, lo.y, hi.x, hi.y);
         }
       }
-    }
-    if (longs) {
-      __syncwarp();
-      const int ntask = __popc(longs) * DIMP;
-      for (int tsk = lane; tsk < ntask; tsk += 32) {
-        const int node = nth_set_bit(longs, tsk / DIMP), d = tsk % DIMP;
-        const int s2b = sm.start[node], s2e = sm.end[node];
-        float acc = sm.S[node][d];
-        int s2 = s2b;
-        for (; s2 + 4 <= s2e; s2 += 4) {
-          const float x0 = sm.c[s2][d], x1 = sm.c[s2 + 1][d], x2 = sm.c[s2 + 2][d],
-                      x3 = sm.c[s2 + 3][d];
-          acc = fadd(fadd(fadd(fadd(acc, x0), x1), x2), x3);
-        }
-        for (; s2 < s2e; ++s2) acc = fadd(acc, sm.c[s2][d]);
-        sm.S[node][d] = acc;
-      }
-      __syncwarp();
-      if (is_long) {
 #pragma unroll
-        for (int d = 0; d < DIMP; ++d) g[d] = sm.S[lane][d];
-      }
+      for (int q = 0; q < PD / 4; ++q) srow[q] = acc[q];
     }
     __syncwarp();  // contributions, runs and sums are settled before the next window
   }
@@ -1434,11 +1414,11 @@ __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP>& sm
   if (lane < nt) {  // Adam, embedding.rs:256-272
     const size_t q = (size_t)(v0 + lane) * DIMP;
     const bool act = (act_mask >> lane) & 1u;
-    float e[DIMP];
+    float e[DIMP], g[DIMP];
 #pragma unroll
     for (int d = 0; d < DIMP; ++d) {
       e[d] = sm.rows[lane][d];
-      if (!act) g[d] = 0.0f;
+      g[d] = act ? sm.S[lane][d] : 0.0f;
     }
     if (act) {
       const float4* m4 = reinterpret_cast<const float4*>(a.m + q);
