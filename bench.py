@@ -27,8 +27,8 @@ independent problems, n log-uniform in [2,000, 150,000], 384-d, 5-60
 isotropic clusters (sigma 0.15) on the sphere each, k = 15, dim 4, problem p
 seeded 1000 + p; all problems run as one plan (one launch per epoch). Its
 value is the device time of that loop; e2e takes the kNN lists from pinned
-host memory through the C ABI (fuzzy set per problem, then one batched
-embedding with host outputs).
+host memory through the C ABI (one batched fuzzy set giving a block-diagonal
+graph, then one embedding of its blocks with host outputs).
 """
 from __future__ import annotations
 
@@ -385,11 +385,11 @@ def run_batched(args) -> dict:
         e2e_steps = max(1, min(args.steps, args.e2e_steps))
         torch.cuda.synchronize()
         t = time.perf_counter()
+        sizes_h = [int(ih.shape[0]) for ih, _ in host]
         for _ in range(e2e_steps):
-            gs = [ctx.fuzzy_set(ih, dh, float(k), True) for ih, dh in host]
-            ctx.embed_batched(gs, dim, params, seeds=seeds)
-            for g in gs:
-                g.free()
+            gb = ctx.fuzzy_set_batched(host, float(k), True)
+            ctx.embed_blocks(gb, sizes_h, dim, params, seeds=seeds)
+            gb.free()
         torch.cuda.synchronize()
         e2e_s = (time.perf_counter() - t) / e2e_steps
     ms_step = ms_total / args.steps

@@ -31,6 +31,47 @@ __global__ void k_validate_indices(const uint32_t* __restrict__ idx,
 
 void use_device(evoc_ctx* ctx) { EVOC_CUDA(cudaSetDevice(ctx->device)); }
 
+// Concatenated kNN lists of many problems: each entry of problem p (rows
+// [row_start[p], row_start[p + 1])) gets the problem's first row added, so
+// the lists form one block-diagonal kNN graph; padding stays padding, and an
+// index outside the problem sets the status.
+__global__ void k_knn_offset(uint32_t* __restrict__ idx, int64_t total, int32_t k,
+                             const int64_t* __restrict__ row_start, int32_t m,
+                             int32_t* __restrict__ status) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= total * (int64_t)k) return;
+  const uint32_t v = idx[e];
+  if (v == 0xFFFFFFFFu) return;
+  const int64_t row = e / k;
+  int lo = 0, hi = m - 1;  // last problem whose first row is <= row
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (row_start[mid] <= row) lo = mid; else hi = mid - 1;
+  }
+  const int64_t base = row_start[lo], np = row_start[lo + 1] - base;
+  if ((int64_t)v >= np) {
+    atomicOr(status, (int32_t)evoc::ST_BAD_INDEX);
+    return;
+  }
+  idx[e] = (uint32_t)(v + base);
+}
+
+std::vector<evoc::ProblemDesc> block_problems(const evoc_graph_t* g, int32_t m,
+                                              const int64_t* n_per, const uint64_t* seeds) {
+  if (!g || m <= 0 || !n_per || !seeds)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "bad argument");
+  std::vector<evoc::ProblemDesc> probs;
+  int64_t b = 0;
+  for (int32_t q = 0; q < m; ++q) {
+    if (n_per[q] < 0) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "negative block size");
+    probs.push_back({g, seeds[q], b, n_per[q]});
+    b += n_per[q];
+  }
+  if (b != g->n)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "block sizes do not add up to the graph's n");
+  return probs;
+}
+
 }  // namespace
 
 void evoc::set_thread_error(const std::string& message) { g_thread_error = message; }
@@ -209,6 +250,53 @@ int evoc_fuzzy_set(evoc_ctx_t* ctx, const uint32_t* knn_idx,
   EVOC_API_END(ctx)
 }
 
+int evoc_fuzzy_set_batched(evoc_ctx_t* ctx, int32_t n_problems,
+                           const uint32_t* const* knn_idx, const float* const* knn_dist,
+                           const int64_t* n_per, int32_t k, float effective_n_neighbours,
+                           int symmetrise, evoc_graph_t** out_graph) {
+  EVOC_API_BEGIN
+  if (!ctx || !out_graph || n_problems <= 0 || !knn_idx || !knn_dist || !n_per)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "bad argument");
+  *out_graph = nullptr;
+  if (k <= 0) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "k must be positive");
+  std::vector<int64_t> start(n_problems + 1, 0);
+  for (int32_t q = 0; q < n_problems; ++q) {
+    if (n_per[q] <= 0)
+      throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT,
+                        "empty kNN graph (build_fuzzy_simplicial_set reads row 0)");
+    if (!knn_idx[q] || !knn_dist[q])
+      throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL kNN array");
+    start[q + 1] = start[q] + n_per[q];
+  }
+  const int64_t n = start[n_problems];
+  if (n >= (int64_t)0xFFFFFFFFu)
+    throw evoc::Error(EVOC_ERR_UNSUPPORTED, "more than 2^32-2 points in total");
+  use_device(ctx);
+  cudaStream_t s = ctx->stream;
+  evoc::DevBuf<uint32_t> di(n * (int64_t)k, s);
+  evoc::DevBuf<float> dd(n * (int64_t)k, s);
+  evoc::DevBuf<int64_t> dstart(n_problems + 1, s);
+  for (int32_t q = 0; q < n_problems; ++q) {
+    const size_t off = (size_t)start[q] * k, cnt = (size_t)n_per[q] * k;
+    EVOC_CUDA(cudaMemcpyAsync(di.get() + off, knn_idx[q], cnt * sizeof(uint32_t),
+                              cudaMemcpyHostToDevice, s));
+    EVOC_CUDA(cudaMemcpyAsync(dd.get() + off, knn_dist[q], cnt * sizeof(float),
+                              cudaMemcpyHostToDevice, s));
+  }
+  EVOC_CUDA(cudaMemcpyAsync(dstart.get(), start.data(), start.size() * sizeof(int64_t),
+                            cudaMemcpyHostToDevice, s));
+  k_knn_offset<<<(unsigned)((n * k + 255) / 256), 256, 0, s>>>(di.get(), n, k, dstart.get(),
+                                                              n_problems, ctx->status.get());
+  EVOC_CHECK_LAUNCH();
+  evoc::check_status(ctx, "batched kNN");  // synchronises: `start` goes out of scope
+  std::unique_ptr<evoc_graph> g(new evoc_graph());
+  evoc::fuzzy_set_device(ctx, di.get(), dd.get(), n, k, effective_n_neighbours,
+                         symmetrise != 0, nullptr, nullptr, g.get());
+  evoc::check_status(ctx, "fuzzy set");
+  *out_graph = g.release();
+  EVOC_API_END(ctx)
+}
+
 int evoc_graph_from_csr(evoc_ctx_t* ctx, const int64_t* indptr,
                         const uint32_t* indices, const float* weights,
                         int64_t n, evoc_graph_t** out_graph) {
@@ -319,6 +407,36 @@ int evoc_plan_create_batched(evoc_ctx_t* ctx, int32_t n_problems,
     probs.push_back({graphs[q], seeds[q]});
   }
   *out_plan = evoc::plan_create(ctx, probs, dim, *params);
+  EVOC_API_END(ctx)
+}
+
+int evoc_plan_create_blocks(evoc_ctx_t* ctx, const evoc_graph_t* g, int32_t n_problems,
+                            const int64_t* n_per, int32_t dim,
+                            const evoc_embed_params_t* params, const uint64_t* seeds,
+                            evoc_plan_t** out_plan) {
+  EVOC_API_BEGIN
+  if (!ctx || !params || !out_plan) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "bad argument");
+  *out_plan = nullptr;
+  std::vector<evoc::ProblemDesc> probs = block_problems(g, n_problems, n_per, seeds);
+  use_device(ctx);
+  if (n_problems == 1) probs[0].begin = probs[0].count = -1;  // the whole graph
+  *out_plan = evoc::plan_create(ctx, probs, dim, *params);
+  EVOC_API_END(ctx)
+}
+
+int evoc_embed_blocks(evoc_ctx_t* ctx, const evoc_graph_t* g, int32_t n_problems,
+                      const int64_t* n_per, int32_t dim, const evoc_embed_params_t* params,
+                      const float* const* inits, const uint64_t* seeds, float* const* outs) {
+  EVOC_API_BEGIN
+  if (!ctx || !params || !outs) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "bad argument");
+  std::vector<evoc::ProblemDesc> probs = block_problems(g, n_problems, n_per, seeds);
+  for (int32_t q = 0; q < n_problems; ++q)
+    if (n_per[q] > 0 && !outs[q]) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL output");
+  use_device(ctx);
+  if (n_problems == 1) probs[0].begin = probs[0].count = -1;
+  std::unique_ptr<evoc_plan, void (*)(evoc_plan*)> pl(
+      evoc::plan_create(ctx, probs, dim, *params), evoc::plan_free);
+  evoc::plan_upload_init_and_run(pl.get(), inits, outs, 0);
   EVOC_API_END(ctx)
 }
 

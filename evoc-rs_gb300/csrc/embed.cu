@@ -1738,6 +1738,26 @@ int64_t plan_n(const evoc_plan* p) { return p->n; }
 int32_t plan_n_epochs(const evoc_plan* p) { return p->params.n_epochs; }
 bool plan_has_edges(const evoc_plan* p) { return p->has_edges; }
 
+namespace {
+// Thread per row of a block-diagonal graph: every column must lie in the
+// row's own problem.
+__global__ void k_check_blocks(const int64_t* __restrict__ indptr,
+                               const uint32_t* __restrict__ indices, int64_t n,
+                               const uint32_t* __restrict__ prob_of_node,
+                               const ProbInfo* __restrict__ prob, int32_t* __restrict__ status) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const ProbInfo pi = prob[prob_of_node[r]];
+  for (int64_t p = indptr[r]; p < indptr[r + 1]; ++p) {
+    const uint32_t c = indices[p];
+    if (c < pi.node_base || c - pi.node_base >= pi.n) {
+      atomicOr(status, (int32_t)ST_CROSS_BLOCK);
+      return;
+    }
+  }
+}
+}  // namespace
+
 evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
                        int32_t dim, const evoc_embed_params_t& params) {
   cudaStream_t s = ctx->stream;
@@ -1754,14 +1774,30 @@ evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
   pl->n_problems = (int32_t)probs.size();
   int64_t n = 0, nnz = 0;
   bool canonical = true;
+  // blocks: every problem is a row range of one block-diagonal graph
+  const bool blocks = probs.size() > 1 && probs[0].begin >= 0;
   for (auto& p : probs) {
     if (!p.graph || p.graph->ctx != ctx)
       throw Error(EVOC_ERR_INVALID_ARGUMENT, "graph belongs to another context");
+    if (blocks) {
+      if (p.graph != probs[0].graph || p.begin != n || p.count < 0)
+        throw Error(EVOC_ERR_INVALID_ARGUMENT, "blocks must tile one graph in order");
+      pl->node_base.push_back(n);
+      pl->seeds.push_back(p.seed);
+      n += p.count;
+      continue;
+    }
     pl->node_base.push_back(n);
     pl->seeds.push_back(p.seed);
     n += p.graph->n;
     nnz += p.graph->nnz;
     canonical = canonical && p.graph->canonical;
+  }
+  if (blocks) {
+    if (n != probs[0].graph->n)
+      throw Error(EVOC_ERR_INVALID_ARGUMENT, "block sizes do not add up to the graph's n");
+    nnz = probs[0].graph->nnz;
+    canonical = probs[0].graph->canonical;
   }
   if (n >= (int64_t)0xFFFFFFFFu)
     throw Error(EVOC_ERR_UNSUPPORTED, "more than 2^32-2 nodes in total");
@@ -1798,6 +1834,28 @@ evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
     indptr = probs[0].graph->indptr.get();
     indices = probs[0].graph->indices.get();
     weights = probs[0].graph->weights.get();
+  } else if (blocks) {
+    indptr = probs[0].graph->indptr.get();
+    indices = probs[0].graph->indices.get();
+    weights = probs[0].graph->weights.get();
+    std::vector<uint32_t> pon_host(n);
+    std::vector<ProbInfo> info;
+    for (size_t q = 0; q < probs.size(); ++q) {
+      info.push_back(ProbInfo{(uint32_t)probs[q].begin, (uint32_t)probs[q].count, probs[q].seed});
+      for (int64_t i = 0; i < probs[q].count; ++i) pon_host[probs[q].begin + i] = (uint32_t)q;
+    }
+    pl->prob_of_node.alloc(n, s);
+    pl->prob.alloc(info.size(), s);
+    EVOC_CUDA(cudaMemcpyAsync(pl->prob_of_node.get(), pon_host.data(), n * sizeof(uint32_t),
+                              cudaMemcpyHostToDevice, s));
+    EVOC_CUDA(cudaMemcpyAsync(pl->prob.get(), info.data(), info.size() * sizeof(ProbInfo),
+                              cudaMemcpyHostToDevice, s));
+    if (nnz > 0) {  // every edge must stay inside its problem
+      k_check_blocks<<<blocks_for(n), 256, 0, s>>>(indptr, indices, n, pl->prob_of_node.get(),
+                                                   pl->prob.get(), ctx->status.get());
+      EVOC_CHECK_LAUNCH();
+    }
+    check_status(ctx, "block-diagonal graph");  // synchronises: host vectors go out of scope
   } else {
     cat_ptr.alloc(n + 1, s);
     cat_idx.alloc(nnz, s);

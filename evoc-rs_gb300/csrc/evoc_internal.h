@@ -43,6 +43,7 @@ enum StatusBit : int32_t {
   ST_EMPTY_ROW = 4,      // empty kNN row with local_connectivity > 0
   ST_TOO_MANY_NEG = 8,   // negative count per edge-epoch above the limit
   ST_INTERNAL = 16,      // self-check failed
+  ST_CROSS_BLOCK = 32,   // an edge joins two problems of a block-diagonal graph
 };
 
 // ---------------------------------------------------------------------------
@@ -184,9 +185,13 @@ void fuzzy_set_device(evoc_ctx* ctx, const uint32_t* d_idx,
                       float* d_sigmas_out, float* d_rhos_out, evoc_graph* out);
 
 // ---- embed.cu --------------------------------------------------------------
+// One problem of a plan: a whole graph, or (begin >= 0) the rows [begin,
+// begin + count) of a block-diagonal graph shared by all the plan's problems.
 struct ProblemDesc {
   const evoc_graph* graph;
   uint64_t seed;
+  int64_t begin = -1;
+  int64_t count = -1;
 };
 
 }  // namespace evoc

@@ -39,6 +39,8 @@ void check_status(evoc_ctx* ctx, const char* where) {
   if (st & ST_EMPTY_ROW)
     throw Error(EVOC_ERR_INVALID_INPUT,
                 w + ": empty kNN row with local_connectivity > 0");
+  if (st & ST_CROSS_BLOCK)
+    throw Error(EVOC_ERR_INVALID_INPUT, w + ": an edge joins two problems (graph not block-diagonal)");
   if (st & ST_TOO_MANY_NEG)
     throw Error(EVOC_ERR_UNSUPPORTED,
                 w + ": more than 2^20 negative samples per edge and epoch "

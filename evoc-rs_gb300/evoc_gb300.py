@@ -46,6 +46,7 @@ EXPORTED = [
     "evoc_plan_profile_epochs", "evoc_plan_info", "evoc_plan_stats",
     "evoc_plan_debug_run", "evoc_plan_free", "evoc_embed_batched",
     "evoc_knn_to_csr_noalloc", "evoc_gather_peak", "evoc_plan_create_batched",
+    "evoc_fuzzy_set_batched", "evoc_plan_create_blocks", "evoc_embed_blocks",
 ]
 
 
@@ -125,6 +126,9 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "evoc_plan_profile_epochs": ([vp, vp, vp, vp], C.c_int),
         "evoc_gather_peak": ([vp, i64, C.POINTER(C.c_double)], C.c_int),
         "evoc_plan_create_batched": ([vp, i32, vp, i32, vp, vp, pp], C.c_int),
+        "evoc_fuzzy_set_batched": ([vp, i32, vp, vp, vp, i32, f32, C.c_int, pp], C.c_int),
+        "evoc_plan_create_blocks": ([vp, vp, i32, vp, i32, vp, vp, pp], C.c_int),
+        "evoc_embed_blocks": ([vp, vp, i32, vp, i32, vp, vp, vp, vp], C.c_int),
         "evoc_plan_info": ([vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i32),
                             C.POINTER(i32), C.POINTER(i64)], C.c_int),
         "evoc_plan_stats": ([vp, C.POINTER(EpochStatsC)], C.c_int),
@@ -396,6 +400,58 @@ class Context:
         self._check(self.lib.evoc_plan_create_batched(self.handle, m, gh, dim, C.byref(p), sd,
                                                       C.byref(h)))
         return Plan(self, h, sum(g.n for g in graphs), dim, pr.n_epochs)
+
+    def fuzzy_set_batched(self, knn: Sequence[tuple[np.ndarray, np.ndarray]],
+                          effective_n_neighbours: float, symmetrise: bool = True) -> Graph:
+        """One block-diagonal graph from many problems' (idx, dist) kNN lists."""
+        m = len(knn)
+        idx = [np.ascontiguousarray(i, dtype=np.uint32) for i, _ in knn]
+        dst = [_f32(d) for _, d in knn]
+        k = idx[0].shape[1]
+        if any(i.ndim != 2 or i.shape[1] != k or i.shape != d.shape for i, d in zip(idx, dst)):
+            raise EvocError(EVOC_ERR_INVALID_ARGUMENT, "every problem needs n x k arrays")
+        ih = (C.c_void_p * m)(*[i.ctypes.data for i in idx])
+        dh = (C.c_void_p * m)(*[d.ctypes.data for d in dst])
+        nh = (C.c_int64 * m)(*[i.shape[0] for i in idx])
+        h = C.c_void_p()
+        self._check(self.lib.evoc_fuzzy_set_batched(self.handle, m, ih, dh, nh, k,
+                                                    float(effective_n_neighbours),
+                                                    int(bool(symmetrise)), C.byref(h)))
+        return Graph(self, h)
+
+    def plan_blocks(self, graph: Graph, sizes: Sequence[int], dim: int,
+                    params: EvocEmbeddingParams | None = None,
+                    seeds: Sequence[int] | None = None) -> Plan:
+        """A plan over the blocks of a block-diagonal graph (block q: sizes[q] rows)."""
+        pr = params or EvocEmbeddingParams()
+        p = pr.to_c()
+        m = len(sizes)
+        nh = (C.c_int64 * m)(*sizes)
+        sd = (C.c_uint64 * m)(*(seeds if seeds is not None else [42] * m))
+        h = C.c_void_p()
+        self._check(self.lib.evoc_plan_create_blocks(self.handle, graph.handle, m, nh, dim,
+                                                     C.byref(p), sd, C.byref(h)))
+        return Plan(self, h, int(sum(sizes)), dim, pr.n_epochs)
+
+    def embed_blocks(self, graph: Graph, sizes: Sequence[int], dim: int,
+                     params: EvocEmbeddingParams | None = None,
+                     inits: Sequence[np.ndarray] | None = None,
+                     seeds: Sequence[int] | None = None) -> list[np.ndarray]:
+        """Embeddings of the blocks of a block-diagonal graph, one array per block."""
+        p = (params or EvocEmbeddingParams()).to_c()
+        m = len(sizes)
+        outs = [np.zeros((n, dim), dtype=np.float32) for n in sizes]
+        nh = (C.c_int64 * m)(*sizes)
+        oh = (C.c_void_p * m)(*[o.ctypes.data for o in outs])
+        sd = (C.c_uint64 * m)(*(seeds if seeds is not None else [42] * m))
+        keep = None
+        ih = None
+        if inits is not None:
+            keep = [_f32(x) for x in inits]
+            ih = (C.c_void_p * m)(*[x.ctypes.data for x in keep])
+        self._check(self.lib.evoc_embed_blocks(self.handle, graph.handle, m, nh, dim,
+                                               C.byref(p), ih, sd, oh))
+        return outs
 
     def embed_batched(self, graphs: Sequence[Graph], dim: int,
                       params: EvocEmbeddingParams | None = None,

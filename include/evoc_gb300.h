@@ -145,6 +145,19 @@ EVOC_API int evoc_fuzzy_set_device(evoc_ctx_t* ctx, const uint32_t* d_knn_idx,
                           float* d_sigmas, float* d_rhos,
                           evoc_graph_t** out_graph);
 
+/* The fuzzy sets of n_problems independent kNN graphs in one pass: problem q
+ * has n_per[q] rows of knn_idx[q] / knn_dist[q] (host, n_per[q] x k, indices
+ * local to the problem, EVOC_KNN_PAD padding). The result is one
+ * block-diagonal graph whose rows are the problems' rows in order; block q
+ * equals evoc_fuzzy_set of problem q alone, with its indices shifted by the
+ * sizes of the problems before it. Use it with evoc_plan_create_blocks or
+ * evoc_embed_blocks (no counterpart: many clustering problems at once). */
+EVOC_API int evoc_fuzzy_set_batched(evoc_ctx_t* ctx, int32_t n_problems,
+                                    const uint32_t* const* knn_idx,
+                                    const float* const* knn_dist, const int64_t* n_per,
+                                    int32_t k, float effective_n_neighbours, int symmetrise,
+                                    evoc_graph_t** out_graph);
+
 /* Upload a weighted adjacency list (the reference's Vec<Vec<(usize, T)>>)
  * given as CSR: indptr[n+1], indices[nnz], weights[nnz] on the host. */
 EVOC_API int evoc_graph_from_csr(evoc_ctx_t* ctx, const int64_t* indptr,
@@ -224,6 +237,23 @@ EVOC_API int evoc_plan_create_batched(evoc_ctx_t* ctx, int32_t n_problems,
                                       const evoc_graph_t* const* graphs, int32_t dim,
                                       const evoc_embed_params_t* params,
                                       const uint64_t* seeds, evoc_plan_t** out_plan);
+
+/* evoc_plan_create_batched for the blocks of one block-diagonal graph (as
+ * evoc_fuzzy_set_batched makes): block q is rows [sum of n_per[0..q), + n_per[q]),
+ * and an edge between two blocks is an error (EVOC_ERR_INVALID_INPUT). */
+EVOC_API int evoc_plan_create_blocks(evoc_ctx_t* ctx, const evoc_graph_t* g,
+                                     int32_t n_problems, const int64_t* n_per, int32_t dim,
+                                     const evoc_embed_params_t* params,
+                                     const uint64_t* seeds, evoc_plan_t** out_plan);
+
+/* evoc_embed_batched for the blocks of one block-diagonal graph: outs[q]
+ * (host, n_per[q] * dim) receives block q's embedding, which equals
+ * evoc_embed of block q alone with seeds[q]; inits is NULL or one host
+ * array per block. */
+EVOC_API int evoc_embed_blocks(evoc_ctx_t* ctx, const evoc_graph_t* g, int32_t n_problems,
+                               const int64_t* n_per, int32_t dim,
+                               const evoc_embed_params_t* params, const float* const* inits,
+                               const uint64_t* seeds, float* const* outs);
 
 /* Run the epoch loop from d_init (device n*dim, or NULL for the random
  * initialisation) and write d_out (device n*dim). d_init may equal d_out. */

@@ -267,3 +267,55 @@ def test_closing_a_context_frees_its_graphs_and_plans():
     g.free()
     p.free()
     del g, p
+
+
+def test_blocks_equal_separate_problems(ctx):
+    """Many problems as one block-diagonal graph: the batched fuzzy set's
+    blocks equal the problems' own fuzzy sets (indices shifted), and the
+    blocks' embeddings (host outputs and device plan) equal separate runs."""
+    import torch
+    import evoc_gb300 as E
+    import workloads as W
+    sizes, knn, graphs, seeds = [300, 1200, 40, 800], [], [], []
+    for q, n in enumerate(sizes):
+        x, _ = W.blobs_sphere_np(n, 32, 4, 0.1, seed=200 + q)
+        idx, dist = W.knn_np(x, 10)
+        idx[::7, 9] = 0xFFFFFFFF  # some ragged rows
+        knn.append((idx, dist))
+        graphs.append(ctx.fuzzy_set(idx, dist, 10.0, True))
+        seeds.append(3000 + q)
+    gb = ctx.fuzzy_set_batched(knn, 10.0, True)
+    ip, ix, w = gb.export()
+    base = 0
+    for n, g in zip(sizes, graphs):
+        rip, rix, rw = g.export()
+        assert np.array_equal(ip[base:base + n + 1] - ip[base], rip)
+        assert np.array_equal(ix[ip[base]:ip[base + n]] - base, rix)
+        _assert_bits(w[ip[base]:ip[base + n]], rw, "weights")
+        base += n
+    p = E.EvocEmbeddingParams(n_epochs=20)
+    outs = ctx.embed_blocks(gb, sizes, 4, p, seeds=seeds)
+    for o, g, s in zip(outs, graphs, seeds):
+        _assert_bits(o, ctx.embed(g, 4, p, seed=s))
+    plan = ctx.plan_blocks(gb, sizes, 4, p, seeds=seeds)
+    d_out = torch.empty(plan.n, 4, dtype=torch.float32, device="cuda")
+    plan.run_device(None, d_out.data_ptr())
+    _assert_bits(d_out.cpu().numpy(), np.concatenate(outs))
+
+
+def test_blocks_reject_bad_input(ctx):
+    import evoc_gb300 as E
+    idx = np.array([[1], [0], [5]], np.uint32)  # 5 is outside a 3-row problem
+    dist = np.ones((3, 1), np.float32)
+    ok = np.array([[1], [0]], np.uint32), np.ones((2, 1), np.float32)
+    with pytest.raises(E.EvocError) as ei:
+        ctx.fuzzy_set_batched([ok, (idx, dist)], 1.0)
+    assert ei.value.code == E.EVOC_ERR_INVALID_INPUT
+    g = ctx.fuzzy_set_batched([ok, ok], 1.0)
+    with pytest.raises(E.EvocError) as ei:
+        ctx.plan_blocks(g, [2, 3], 4)
+    assert ei.value.code == E.EVOC_ERR_INVALID_ARGUMENT
+    cross = ctx.graph_from_adjacency([[(2, 1.0)], [(0, 1.0)], [(0, 1.0)], [(1, 1.0)]])
+    with pytest.raises(E.EvocError) as ei:
+        ctx.plan_blocks(cross, [2, 2], 4)
+    assert ei.value.code == E.EVOC_ERR_INVALID_INPUT
