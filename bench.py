@@ -191,6 +191,27 @@ def cpu_epochs_sample(ip, ix, w, dim, seed, stats, t0: int, n_ep: int, max_secon
     return fired / tsec, cores, tsec
 
 
+def combine_replicas(res: dict, world: int, device) -> dict:
+    """N independent replicas (the path has no exchange step): the step time is
+    the maximum over ranks and the value counts every rank's work."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([res["ms_per_step"]], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    out = dict(res)
+    out["ms_per_step"] = float(t.item())
+    out["value"] = world * res["config"]["edge_updates_per_step"] / (out["ms_per_step"] / 1e3)
+    out["n_gpus"] = world
+    return out
+
+
+def _barrier() -> None:
+    """All ranks reach the timed region together (no-op on one process)."""
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        dist.barrier()
+
+
 def run_ours(args) -> dict:
     import torch
     import evoc_gb300 as E
@@ -220,11 +241,13 @@ def run_ours(args) -> dict:
     ev1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler() as clk:
         torch.cuda.synchronize()
+        _barrier()
         ev0.record(stream)
         for _ in range(args.steps):
             plan.enqueue_device(None, out.data_ptr())
         ev1.record(stream)
         torch.cuda.synchronize()
+        _barrier()
         ms_total = ev0.elapsed_time(ev1)
 
         # end to end through the C ABI with pinned host buffers
@@ -499,13 +522,7 @@ def main() -> None:
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
-        res = run_ours(args)
-        t = torch.tensor([res["ms_per_step"]], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        per_step = res["config"]["edge_updates_per_step"]
-        res["ms_per_step"] = float(t.item())
-        res["value"] = world * per_step / (res["ms_per_step"] / 1e3)
-        res["n_gpus"] = world
+        res = combine_replicas(run_ours(args), world, "cuda")
         if rank == 0:
             print(json.dumps(res))
         dist.destroy_process_group()
