@@ -748,13 +748,14 @@ __global__ void __launch_bounds__(128) k_epoch(EpochArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// Fast path: per-epoch records of the fired entries.
+// Fast path: per-epoch gradient slots.
 //
-// The epochs-per-sample schedule does not depend on the embedding, so the
-// set-up lists, for every epoch and every 32-node tile, the incidence entries
-// that fire, in incidence order, as records (partner id, tile-local node |
-// negative count << 5, edge id). The epoch kernel then streams its tile's
-// records (coalesced, next chunk prefetched) instead of scanning fire bits.
+// The epochs-per-sample schedule and the negative draws do not depend on the
+// embedding, so the set-up lists, for every epoch and every 32-node tile, the
+// terms of the reference's gradient sums in their order: one slot (source
+// row, tile-local node | 32 for a negative) per fired incidence entry and per
+// negative sample it draws. The epoch kernel streams its tile's slots instead
+// of scanning fire bits.
 // ---------------------------------------------------------------------------
 // Per-edge schedule (n_epochs <= 64): thread per undirected edge runs the
 // recurrence once (embedding.rs:274-286) and stores the epochs in which the
@@ -1571,8 +1572,8 @@ void fill_eidx_src(uint2* out, const uint32_t* e_src, int64_t U, cudaStream_t s)
 void add_counts(const int32_t* a, const int32_t* b, int32_t* out, int64_t n,
                 cudaStream_t s);
 
-// Launch order of the records kernels: sort key per tile = ~(its records over
-// all epochs), so that an ascending sort puts the heaviest tiles (hub nodes)
+// Launch order of the slots kernel: sort key per tile = ~(its slots over all
+// epochs), so that an ascending sort puts the heaviest tiles (hub nodes)
 // first and their long serial sums overlap the many light tiles.
 __global__ void k_tile_weight(const int32_t* __restrict__ counts, int64_t ntiles, int32_t ne,
                               uint32_t* __restrict__ keys, uint2* __restrict__ vals) {
@@ -1984,7 +1985,7 @@ evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
   lptr.release();
 
   trace.mark("incidence lists");
-  // schedule: per-epoch records (fast path) or bit planes (fallback)
+  // schedule: per-epoch gradient slots (fast path) or bit planes (fallback)
   const float neg_factor = 1.5f / params.negative_sample_rate;  // embedding.rs:116
   pl->W = (n_inc + 31) / 32;
   if (ne > 0 && !build_slots(pl.get(), inc_ps.get(), inc_up.get(), inc_eidx.get(),
