@@ -22,6 +22,17 @@ the undirected edges fired (epoch_of_next_sample <= t) / time.
 
 --impl reference times the CPU oracle alone on the same workload.
 
+--workload warm_start_c5 measures the learned warm start: an MLP
+768 -> 512 -> 512 -> 8 (BF16 tensor-core GEMMs, FP32 accumulation, GELU) is
+trained on the GPU on plain-method layouts of 20 seeded 2M-point instances of
+the generator above (seeds 100-119), then a fresh 1M-point instance (seed 777)
+is embedded plain (random init, 50 epochs) and warm (prediction as the
+initial embedding, fewer epochs). Its value is the plain time-to-embedding
+(fuzzy set + set-up + init + epochs, from the device kNN graph) over the warm
+one at the smallest epoch count whose trustworthiness@15 and kNN label
+accuracy match the plain run's; the same epoch count from a random init is
+reported beside it.
+
 --workload batch_c4 measures the batched configuration instead: 256
 independent problems, n log-uniform in [2,000, 150,000], 384-d, 5-60
 isotropic clusters (sigma 0.15) on the sphere each, k = 15, dim 4, problem p
@@ -55,8 +66,13 @@ WORKLOADS = {
     "anisotropic_200k": dict(n=200_000, d=512, k=15, dim=8, seed=1),
     "blobs_10k": dict(n=10_000, d=384, k=15, dim=4, seed=42),
     "batch_c4": dict(n=256, d=384, k=15, dim=4, seed=1000),  # n = number of problems
+    # n = points of the fresh evaluation instance
+    "warm_start_c5": dict(n=1_000_000, d=768, k=30, dim=8, seed=777, hidden=512,
+                          train_n=2_000_000, train_instances=20, train_seed=100),
 }
 METRIC_C4 = "edge-updates/s, 256 batched problems (EVoC node embedding, 50 epochs)"
+METRIC_C5 = ("time-to-embedding speed-up at 1M pts, learned warm start vs plain "
+             "(equal trustworthiness@15 and kNN label accuracy)")
 
 
 def peaks() -> dict:
@@ -456,6 +472,110 @@ def run_batched(args) -> dict:
     }
 
 
+def run_warm_start(args) -> dict:
+    import torch
+    import evoc_gb300 as E
+    import warm_start as WS
+    torch.cuda.init()
+    cfg = dict(WORKLOADS["warm_start_c5"])
+    n = args.n or cfg["n"]
+    n_tr = args.c5_train_n or cfg["train_n"]
+    m_tr = args.c5_train_instances or cfg["train_instances"]
+    d, k, dim, seed, hid = cfg["d"], cfg["k"], cfg["dim"], cfg["seed"], cfg["hidden"]
+    ctx = E.Context(0)
+    t0 = time.time()
+    train = [WS.training_instance(ctx, n_tr, d, k, dim, seed=cfg["train_seed"] + s)
+             for s in range(m_tr)]
+    prep_s = time.time() - t0
+    tp = E.MlpTrainParams(steps=args.c5_steps, batch=8192, align_every=250, align_rows=65536,
+                          lr=1e-3, seed=1)
+    net, hist, train_s = WS.train(ctx, train, hid, dim, tp)
+    del train
+    torch.cuda.empty_cache()
+    ev = WS.make_instance(ctx, n, d, k, seed, keep_points=True)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def plain_run(n_epochs, init_fn=None):
+        g = WS.fuzzy_graph(ctx, ev)
+        init = init_fn() if init_fn else None
+        out = WS.embed_device(ctx, g, n, dim, n_epochs, seed, init=init)
+        g.free()
+        return out
+
+    with ClockSampler() as clk:
+        t_plain, e_plain = WS.timed(lambda: plain_run(50), args.c5_reps)
+        q_plain = WS.quality(ev["x"], e_plain, ev["labels"], n_queries=args.c5_queries)
+        del e_plain
+        # the network's forward pass alone (device time, CUDA events)
+        pred = WS.predict(net, ev)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(5):
+            net.predict_device(ev["xb"].data_ptr(), n, pred.data_ptr())
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        predict_ms = ev0.elapsed_time(ev1) / 5
+        q_pred = WS.quality(ev["x"], pred, ev["labels"], n_queries=args.c5_queries)
+        rows, chosen = [], None
+        for ew in args.c5_epochs:
+            t_w, e_w = WS.timed(lambda: plain_run(ew, lambda: WS.predict(net, ev)), args.c5_reps)
+            q_w = WS.quality(ev["x"], e_w, ev["labels"], n_queries=args.c5_queries)
+            del e_w
+            t_r, e_r = WS.timed(lambda: plain_run(ew), 1)
+            q_r = WS.quality(ev["x"], e_r, ev["labels"], n_queries=args.c5_queries)
+            del e_r
+            row = {"epochs": ew, "warm_ms": round(t_w * 1e3, 2), "warm": q_w,
+                   "random_init_ms": round(t_r * 1e3, 2), "random_init": q_r}
+            rows.append(row)
+            ok = (q_w["trustworthiness"] >= q_plain["trustworthiness"] - args.c5_tol and
+                  q_w["knn_label_acc"] >= q_plain["knn_label_acc"] - args.c5_tol)
+            if ok and chosen is None:
+                chosen = row
+    flops_fwd = 2.0 * n * (d * hid + hid * hid + hid * dim)
+    tflops = flops_fwd / (predict_ms / 1e3) / 1e12
+    flops_train = 3.0 * 2.0 * 8192 * (d * hid + hid * hid + hid * dim) * args.c5_steps
+    pk = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
+        if (ROOT / "MEASURED_PEAKS.json").exists() else {"bf16_tflops": 1900.0}
+    peak = float(pk["bf16_tflops"])
+    value = (t_plain / (chosen["warm_ms"] / 1e3)) if chosen else None
+    chunks = (n + 65535) // 65536
+    return {
+        "metric": METRIC_C5, "value": value, "unit": "x", "n_gpus": 1,
+        "steps": args.c5_reps, "warmup": 0, "ms_per_step": chosen["warm_ms"] if chosen else None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16 (MLP GEMMs, f32 accumulate); f32 (embedding)",
+        "data": "synthetic (seeded, no dataset)",
+        "config": {"workload": "warm_start_c5", "n": n, "d": d, "k": k, "dim": dim,
+                   "mlp": f"{d}->{hid}->{hid}->{dim} GELU", "train_instances": m_tr,
+                   "train_n": n_tr, "train_seeds": f"{cfg['train_seed']}..{cfg['train_seed'] + m_tr - 1}",
+                   "eval_seed": seed, "train_steps": args.c5_steps, "batch": 8192,
+                   "train_data_prep_s": round(prep_s, 1), "train_s": round(train_s, 2),
+                   "train_tflops": round(flops_train / train_s / 1e12, 1),
+                   "loss_first_last": [float(hist[:50].mean()), float(hist[-50:].mean())],
+                   "quality_tolerance": args.c5_tol,
+                   "time": "wall clock, synchronised, median of reps: fuzzy set + plan set-up "
+                           "+ init (network prediction or random) + epochs, from the device kNN graph",
+                   "ari": None,
+                   "ari_note": "labels need the reference's MST / condensed-tree / persistence "
+                               "code, which stays on its Rust side; trustworthiness@15 and kNN "
+                               "label accuracy stand in"},
+        "plain": {"epochs": 50, "ms": round(t_plain * 1e3, 2), **q_plain},
+        "prediction_only": q_pred,
+        "warm": rows, "chosen_epochs": chosen["epochs"] if chosen else None,
+        "e2e": None,
+        "gpu_launches": int(3 * chunks * (1 + args.c5_reps) + (chosen["epochs"] + 2 if chosen else 0)),
+        "gpu_launches_note": "network forward (3 per 65,536-row chunk) and epoch loop of the "
+                             "chosen warm run; fuzzy-set and set-up kernels not counted",
+        "roofline": {"bound": "tensor", "kernel": "k_gemm (network forward, 1M rows)",
+                     "achieved": round(tflops, 1), "peak": peak, "unit": "TFLOP/s",
+                     "frac": round(tflops / peak, 4), "traffic": None,
+                     "peak_src": "measured (cuBLAS bf16 burst)" if "hbm_gbs" in pk else "fallback",
+                     "predict_ms": round(predict_ms, 3)},
+        "clocks": clk.summary(),
+    }
+
+
 def run_reference(args) -> dict:
     """The reference's CPU path (the C++ restatement; Rust is not available)
     on the same workload: each step is one epoch of the embedding loop
@@ -506,6 +626,13 @@ def main() -> None:
     ap.add_argument("--cpu-t0", type=int, default=1, help="first epoch of the CPU sample")
     ap.add_argument("--cpu-epochs", type=int, default=49, help="epochs in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--c5-train-instances", type=int, default=None)
+    ap.add_argument("--c5-train-n", type=int, default=None)
+    ap.add_argument("--c5-steps", type=int, default=3000)
+    ap.add_argument("--c5-epochs", type=int, nargs="+", default=[5, 10, 15, 20, 30])
+    ap.add_argument("--c5-reps", type=int, default=3)
+    ap.add_argument("--c5-queries", type=int, default=2048)
+    ap.add_argument("--c5-tol", type=float, default=0.005)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -526,6 +653,9 @@ def main() -> None:
         if rank == 0:
             print(json.dumps(res))
         dist.destroy_process_group()
+        return
+    if args.workload == "warm_start_c5":
+        print(json.dumps(run_warm_start(args)))
         return
     print(json.dumps(run_batched(args) if args.workload == "batch_c4" else run_ours(args)))
 

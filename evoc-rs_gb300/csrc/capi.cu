@@ -558,4 +558,124 @@ int evoc_embed_batched(evoc_ctx_t* ctx, int32_t n_problems,
   EVOC_API_END(ctx)
 }
 
+// ---- learned warm start ----------------------------------------------------
+
+void evoc_mlp_train_params_default(evoc_mlp_train_params_t* p) {
+  if (!p) return;
+  p->steps = 3000;
+  p->batch = 8192;
+  p->align_every = 250;
+  p->align_rows = 65536;
+  p->lr = 1e-3f;
+  p->beta1 = 0.9f;
+  p->beta2 = 0.999f;
+  p->eps = 1e-8f;
+  p->seed = 0;
+}
+
+int evoc_mlp_create(evoc_ctx_t* ctx, int32_t in_dim, int32_t hidden, int32_t out_dim,
+                    uint64_t seed, evoc_mlp_t** out) {
+  EVOC_API_BEGIN
+  if (!ctx || !out) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL argument");
+  *out = nullptr;
+  use_device(ctx);
+  *out = evoc::mlp_create(ctx, in_dim, hidden, out_dim, seed);
+  EVOC_API_END(ctx)
+}
+
+void evoc_mlp_free(evoc_mlp_t* mlp) {
+  if (!mlp) return;
+  evoc_ctx* ctx = evoc::mlp_ctx(mlp);
+  if (ctx) cudaSetDevice(ctx->device);
+  evoc::mlp_free(mlp);
+}
+
+int64_t evoc_mlp_n_params(const evoc_mlp_t* mlp) { return mlp ? evoc::mlp_n_params(mlp) : 0; }
+
+int evoc_mlp_get_params(const evoc_mlp_t* mlp, float* params) {
+  evoc_ctx* ctx = mlp ? evoc::mlp_ctx(mlp) : nullptr;
+  EVOC_API_BEGIN
+  if (!mlp || !params) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL argument");
+  use_device(ctx);
+  evoc::mlp_get_params(mlp, params);
+  EVOC_API_END(ctx)
+}
+
+int evoc_mlp_set_params(evoc_mlp_t* mlp, const float* params) {
+  evoc_ctx* ctx = mlp ? evoc::mlp_ctx(mlp) : nullptr;
+  EVOC_API_BEGIN
+  if (!mlp || !params) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL argument");
+  use_device(ctx);
+  evoc::mlp_set_params(mlp, params);
+  EVOC_API_END(ctx)
+}
+
+int evoc_mlp_predict(evoc_mlp_t* mlp, const float* x, int64_t n, float* out) {
+  evoc_ctx* ctx = mlp ? evoc::mlp_ctx(mlp) : nullptr;
+  EVOC_API_BEGIN
+  if (!mlp || n < 0 || (n > 0 && (!x || !out)))
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "bad argument");
+  use_device(ctx);
+  evoc::mlp_predict_host(mlp, x, n, out);
+  EVOC_API_END(ctx)
+}
+
+int evoc_mlp_predict_device(evoc_mlp_t* mlp, const uint16_t* d_x_bf16, int64_t n,
+                            float* d_out) {
+  evoc_ctx* ctx = mlp ? evoc::mlp_ctx(mlp) : nullptr;
+  EVOC_API_BEGIN
+  if (!mlp || n < 0 || (n > 0 && (!d_x_bf16 || !d_out)))
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "bad argument");
+  if (((uintptr_t)d_x_bf16 & 15) != 0)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "points must be 16-byte aligned");
+  use_device(ctx);
+  evoc::mlp_predict_device(mlp, d_x_bf16, n, d_out);
+  EVOC_CUDA(cudaStreamSynchronize(ctx->stream));
+  EVOC_API_END(ctx)
+}
+
+int evoc_mlp_gradients(evoc_mlp_t* mlp, const float* x, const float* target, int64_t n,
+                       float* loss, float* grad) {
+  evoc_ctx* ctx = mlp ? evoc::mlp_ctx(mlp) : nullptr;
+  EVOC_API_BEGIN
+  if (!mlp || !x || !target || !loss || !grad || n <= 0)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "bad argument");
+  use_device(ctx);
+  evoc::mlp_gradients_host(mlp, x, target, n, loss, grad);
+  EVOC_API_END(ctx)
+}
+
+int evoc_mlp_fit_device(evoc_mlp_t* mlp, int32_t n_instances, const uint16_t* const* d_x_bf16,
+                        const float* const* d_layouts, const int64_t* n_rows,
+                        const evoc_mlp_train_params_t* params, float* loss_history) {
+  evoc_ctx* ctx = mlp ? evoc::mlp_ctx(mlp) : nullptr;
+  EVOC_API_BEGIN
+  if (!mlp || n_instances <= 0 || !d_x_bf16 || !d_layouts || !n_rows || !params)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "bad argument");
+  for (int32_t i = 0; i < n_instances; ++i)
+    if (((uintptr_t)d_x_bf16[i] & 15) != 0 || ((uintptr_t)d_layouts[i] & 3) != 0)
+      throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "misaligned instance buffer");
+  use_device(ctx);
+  evoc::mlp_fit_device(mlp, n_instances, d_x_bf16, d_layouts, n_rows, params, loss_history);
+  EVOC_API_END(ctx)
+}
+
+int evoc_to_bf16_device(evoc_ctx_t* ctx, const float* d_in, int64_t count, uint16_t* d_out) {
+  EVOC_API_BEGIN
+  if (!ctx || count < 0 || (count > 0 && (!d_in || !d_out)))
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "bad argument");
+  use_device(ctx);
+  evoc::to_bf16_device(ctx, d_in, count, d_out);
+  EVOC_CUDA(cudaStreamSynchronize(ctx->stream));
+  EVOC_API_END(ctx)
+}
+
+int evoc_procrustes(const double* m, int32_t d, double* r) {
+  evoc_ctx* ctx = nullptr;
+  EVOC_API_BEGIN
+  if (!m || !r || d < 1 || d > 16) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "bad argument");
+  evoc::procrustes(m, d, r);
+  EVOC_API_END(ctx)
+}
+
 }  // extern "C"

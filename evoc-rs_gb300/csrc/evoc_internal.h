@@ -194,6 +194,28 @@ struct ProblemDesc {
   int64_t count = -1;
 };
 
+// ---- mlp.cu ----------------------------------------------------------------
+}  // namespace evoc
+
+struct evoc_mlp;  // defined in mlp.cu
+
+namespace evoc {
+evoc_mlp* mlp_create(evoc_ctx* ctx, int in, int hid, int out, uint64_t seed);
+void mlp_free(evoc_mlp* net);
+evoc_ctx* mlp_ctx(const evoc_mlp* net);
+int64_t mlp_n_params(const evoc_mlp* net);
+void mlp_dims(const evoc_mlp* net, int32_t* in, int32_t* hid, int32_t* out);
+void mlp_get_params(const evoc_mlp* net, float* host);
+void mlp_set_params(evoc_mlp* net, const float* host);
+void mlp_predict_device(evoc_mlp* net, const uint16_t* x, int64_t n, float* y);
+void mlp_predict_host(evoc_mlp* net, const float* x, int64_t n, float* y);
+void mlp_gradients_host(evoc_mlp* net, const float* x, const float* target, int64_t n,
+                        float* loss, float* grad);
+void mlp_fit_device(evoc_mlp* net, int32_t m, const uint16_t* const* xs,
+                    const float* const* layouts, const int64_t* ns,
+                    const evoc_mlp_train_params_t* p, float* loss_history);
+void to_bf16_device(evoc_ctx* ctx, const float* x, int64_t count, uint16_t* y);
+void procrustes(const double* m, int d, double* r);
 }  // namespace evoc
 
 struct evoc_plan;  // defined in embed.cu

@@ -1,0 +1,1024 @@
+// mlp.cu — the learned warm start.
+//
+// A multilayer perceptron in_dim -> hidden -> hidden -> out_dim, with GELU after
+// both hidden layers, predicts an initial embedding from the input points so
+// that the embedding optimiser needs fewer epochs. It is trained on layouts
+// that the plain optimiser itself produced, each aligned to the network's
+// current prediction by an orthogonal Procrustes rotation (layouts are
+// defined only up to isometry), with a mean-squared-error loss and Adam.
+//
+// Numerics: weights and activations feed the tensor cores as BF16 and are
+// accumulated in FP32 (mma.sync m16n8k16); pre-activations, the loss, all
+// gradients and the Adam state are FP32; an FP32 master copy of every
+// parameter is what Adam updates, and its BF16 copy is refreshed each step.
+// Every reduction has a fixed order, so results are reproducible run to run.
+//
+// Parameters are packed in one float array:
+//   [W1 (hidden x in_dim), b1 (hidden), W2 (hidden x hidden), b2 (hidden),
+//    W3 (out_dim x hidden), b3 (out_dim)]
+// with every weight matrix row-major, output by input (a Linear layer's
+// layout).
+#include "evoc_internal.h"
+#include "evoc_device.cuh"
+
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+
+using bf16 = __nv_bfloat16;
+
+struct evoc_mlp {
+  evoc_ctx* ctx = nullptr;
+  int in = 0, hid = 0, out = 0;
+  int64_t n_params = 0;
+  int64_t o_w1 = 0, o_b1 = 0, o_w2 = 0, o_b2 = 0, o_w3 = 0, o_b3 = 0;
+  evoc::DevBuf<float> master, adam_m, adam_v, grad;
+  evoc::DevBuf<bf16> wb;  // BF16 copy of `master`, same packing
+  int64_t adam_steps = 0;
+};
+
+namespace evoc {
+namespace {
+
+// ---------------------------------------------------------------------------
+// Tensor-core GEMM: C[M x N] = sum_k A(m, k) * B(n, k), BF16 in, FP32 out.
+//
+// Each operand is stored either K-major (row m holds A(m, 0..K) contiguously,
+// leading dimension ld) or MN-major (row k holds A(0..M, k) contiguously).
+// The forward layers are K-major x K-major; the input-gradient GEMM reads a
+// weight matrix MN-major; the weight gradients read both operands MN-major
+// (the batch is the reduction dimension). Tiles move global -> shared memory
+// with 16-byte cp.async in their stored layout, and ldmatrix (.trans for
+// MN-major tiles) builds the m16n8k16 fragments.
+//
+// 256 threads = 8 warps as 2 (M) x 4 (N), each warp owning a 64 x 32 piece of
+// the 128 x 128 block tile; K advances 32 at a time through a 3-stage ring.
+// ---------------------------------------------------------------------------
+constexpr int GBM = 128, GBN = 128, GBK = 32, GSTAGES = 3, GTHREADS = 256;
+constexpr int KPAD = GBK + 8;   // K-major tile row, in elements (80 bytes)
+constexpr int MNPAD = GBM + 8;  // MN-major tile row, in elements (272 bytes)
+constexpr int GTILE = (GBM * KPAD > GBK * MNPAD) ? GBM * KPAD : GBK * MNPAD;
+constexpr int GEMM_SMEM = GSTAGES * 2 * GTILE * (int)sizeof(bf16);
+
+enum GemmEpi : int {
+  EPI_BIAS_GELU = 0,  // pre = acc + bias (f32, optional); outb = bf16(gelu(pre))
+  EPI_GELU_GRAD = 1,  // outb = bf16(acc * gelu'(pre))
+  EPI_PARTIAL = 2,    // outf[split][m][n] = acc
+};
+
+struct GemmArgs {
+  const bf16* a;
+  int64_t lda;
+  const bf16* b;
+  int64_t ldb;
+  int M, N, K;
+  int kchunk;          // rows of K per split (multiple of GBK)
+  const float* bias;   // EPI_BIAS_GELU
+  float* pre;          // EPI_BIAS_GELU: written if not null; EPI_GELU_GRAD: read
+  bf16* outb;          // [M][N]
+  float* outf;         // EPI_PARTIAL: [splits][M][N]
+};
+
+__device__ __forceinline__ float gelu(float x) {
+  return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f));
+}
+__device__ __forceinline__ float gelu_grad(float x) {
+  const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
+  const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
+  return cdf + x * pdf;
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  const int n = valid ? 16 : 0;  // 0: fill the 16 bytes with zeros, read nothing
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "r"(n));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
+
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const bf16* p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(a));
+}
+__device__ __forceinline__ void ldsm_x4_t(uint32_t (&r)[4], const bf16* p) {
+  const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(a));
+}
+__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], uint32_t b0,
+                                         uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Stage one operand tile (rows r0.. of the M or N dimension, K from kb) into
+// shared memory. 512 chunks of 16 bytes per tile, two per thread. Chunks
+// outside [0, rows) x [kb, kend) are zero-filled.
+template <bool KMAJ>
+__device__ __forceinline__ void load_tile(bf16* dst, const bf16* src, int64_t ld, int r0,
+                                          int rows, int kb, int kend, int tid) {
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const int c = tid + i * GTHREADS;
+    if (KMAJ) {  // 128 rows x 4 chunks of 8 along K
+      const int r = c >> 2, kc = (c & 3) << 3;
+      const bool ok = (r0 + r < rows) && (kb + kc < kend);
+      const bf16* g = ok ? src + (int64_t)(r0 + r) * ld + kb + kc : src;
+      cp_async16(dst + r * KPAD + kc, g, ok);
+    } else {  // 32 rows of K x 16 chunks of 8 along M (or N)
+      const int kr = c >> 4, mc = (c & 15) << 3;
+      const bool ok = (kb + kr < kend) && (r0 + mc < rows);
+      const bf16* g = ok ? src + (int64_t)(kb + kr) * ld + r0 + mc : src;
+      cp_async16(dst + kr * MNPAD + mc, g, ok);
+    }
+  }
+}
+
+template <bool A_KMAJ, bool B_KMAJ, int EPI>
+__global__ void __launch_bounds__(GTHREADS) k_gemm(GemmArgs g) {
+  extern __shared__ __align__(16) unsigned char gsm[];
+  bf16* sA = reinterpret_cast<bf16*>(gsm);
+  bf16* sB = sA + GSTAGES * GTILE;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = warp >> 2, wn = warp & 3;
+  const int m0 = blockIdx.y * GBM, n0 = blockIdx.x * GBN;
+  const int kbeg = blockIdx.z * g.kchunk;
+  const int kend = min(g.K, kbeg + g.kchunk);
+  const int ntiles = kend > kbeg ? (kend - kbeg + GBK - 1) / GBK : 0;
+
+  float acc[4][4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) acc[i][j][e] = 0.0f;
+
+#pragma unroll
+  for (int s = 0; s < GSTAGES - 1; ++s) {
+    if (s < ntiles) {
+      load_tile<A_KMAJ>(sA + s * GTILE, g.a, g.lda, m0, g.M, kbeg + s * GBK, kend, tid);
+      load_tile<B_KMAJ>(sB + s * GTILE, g.b, g.ldb, n0, g.N, kbeg + s * GBK, kend, tid);
+    }
+    cp_async_commit();
+  }
+
+  const int q = lane >> 3, r = lane & 7;
+  for (int t = 0; t < ntiles; ++t) {
+    cp_async_wait<GSTAGES - 2>();
+    __syncthreads();
+    {  // prefetch tile t + STAGES - 1 into the stage computed at t - 1
+      const int tn = t + GSTAGES - 1;
+      if (tn < ntiles) {
+        const int st = tn % GSTAGES;
+        load_tile<A_KMAJ>(sA + st * GTILE, g.a, g.lda, m0, g.M, kbeg + tn * GBK, kend, tid);
+        load_tile<B_KMAJ>(sB + st * GTILE, g.b, g.ldb, n0, g.N, kbeg + tn * GBK, kend, tid);
+      }
+      cp_async_commit();
+    }
+    const bf16* tA = sA + (t % GSTAGES) * GTILE;
+    const bf16* tB = sB + (t % GSTAGES) * GTILE;
+#pragma unroll
+    for (int kk = 0; kk < GBK; kk += 16) {
+      uint32_t af[4][4], bfr[4][2];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int mr = wm * 64 + i * 16;
+        if (A_KMAJ)
+          ldsm_x4(af[i], tA + (mr + (lane & 15)) * KPAD + kk + ((lane >> 4) << 3));
+        else
+          ldsm_x4_t(af[i], tA + (kk + r + ((q >> 1) << 3)) * MNPAD + mr + ((q & 1) << 3));
+      }
+#pragma unroll
+      for (int jj = 0; jj < 2; ++jj) {
+        const int nc = wn * 32 + jj * 16;
+        uint32_t tb[4];
+        if (B_KMAJ)
+          ldsm_x4(tb, tB + (nc + r + ((q >> 1) << 3)) * KPAD + kk + ((q & 1) << 3));
+        else
+          ldsm_x4_t(tb, tB + (kk + r + ((q & 1) << 3)) * MNPAD + nc + ((q >> 1) << 3));
+        bfr[2 * jj][0] = tb[0];
+        bfr[2 * jj][1] = tb[1];
+        bfr[2 * jj + 1][0] = tb[2];
+        bfr[2 * jj + 1][1] = tb[3];
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) mma_bf16(acc[i][j], af[i], bfr[j][0], bfr[j][1]);
+    }
+  }
+  cp_async_wait<0>();
+
+  // Epilogue: thread (g, c) of each 16 x 8 fragment holds rows g and g + 8,
+  // columns 2c and 2c + 1.
+  const int gq = lane >> 2, cq = lane & 3;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int col = n0 + wn * 32 + j * 8 + 2 * cq;
+      if (col >= g.N) continue;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int row = m0 + wm * 64 + i * 16 + gq + 8 * h;
+        if (row >= g.M) continue;
+        const float v0 = acc[i][j][2 * h], v1 = acc[i][j][2 * h + 1];
+        const int64_t o = (int64_t)row * g.N + col;
+        if (EPI == EPI_BIAS_GELU) {
+          const float p0 = v0 + g.bias[col], p1 = v1 + g.bias[col + 1];
+          if (g.pre) *reinterpret_cast<float2*>(g.pre + o) = make_float2(p0, p1);
+          *reinterpret_cast<__nv_bfloat162*>(g.outb + o) = __floats2bfloat162_rn(gelu(p0), gelu(p1));
+        } else if (EPI == EPI_GELU_GRAD) {
+          const float2 p = *reinterpret_cast<const float2*>(g.pre + o);
+          *reinterpret_cast<__nv_bfloat162*>(g.outb + o) =
+              __floats2bfloat162_rn(v0 * gelu_grad(p.x), v1 * gelu_grad(p.y));
+        } else {
+          *reinterpret_cast<float2*>(g.outf + (int64_t)blockIdx.z * g.M * g.N + o) =
+              make_float2(v0, v1);
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Output layer (hidden -> out_dim, out_dim <= 16), one warp per row.
+// Inference writes y. Training also forms the MSE gradient
+//   dY = 2 (y - target) / (rows * out_dim),
+// its back-projection dH2 = (dY W3) * gelu'(H2) in BF16, and per-block sums of
+// (y - target)^2.
+// ---------------------------------------------------------------------------
+constexpr int MLP_MAX_OUT = 16;
+constexpr int HEAD_THREADS = 256;
+
+template <bool TRAIN>
+__global__ void __launch_bounds__(HEAD_THREADS)
+    k_head(const bf16* __restrict__ a2, const float* __restrict__ h2, int hid, int out,
+           int64_t rows, const bf16* __restrict__ w3, const float* __restrict__ b3,
+           float* __restrict__ y, const float* __restrict__ target, float grad_scale,
+           float* __restrict__ dy, bf16* __restrict__ dh2, float* __restrict__ loss_part) {
+  extern __shared__ float w3s[];  // [out][hid]
+  __shared__ float wsum[HEAD_THREADS / 32];
+  for (int i = threadIdx.x; i < out * hid; i += blockDim.x) w3s[i] = __bfloat162float(w3[i]);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nchunks = hid >> 3;
+  float lsum = 0.0f;
+  for (int64_t row = (int64_t)blockIdx.x * (HEAD_THREADS / 32) + warp; row < rows;
+       row += (int64_t)gridDim.x * (HEAD_THREADS / 32)) {
+    float acc[MLP_MAX_OUT];
+#pragma unroll
+    for (int o = 0; o < MLP_MAX_OUT; ++o) acc[o] = 0.0f;
+    for (int c = lane; c < nchunks; c += 32) {
+      const uint4 raw = *reinterpret_cast<const uint4*>(a2 + row * hid + c * 8);
+      const bf16* av = reinterpret_cast<const bf16*>(&raw);
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        const float x = __bfloat162float(av[e]);
+#pragma unroll
+        for (int o = 0; o < MLP_MAX_OUT; ++o)
+          if (o < out) acc[o] += x * w3s[o * hid + c * 8 + e];
+      }
+    }
+#pragma unroll
+    for (int o = 0; o < MLP_MAX_OUT; ++o) {
+      if (o >= out) break;
+#pragma unroll
+      for (int sh = 16; sh > 0; sh >>= 1) acc[o] += __shfl_xor_sync(0xffffffffu, acc[o], sh);
+      acc[o] += b3[o];
+    }
+    if (!TRAIN) {
+#pragma unroll
+      for (int o = 0; o < MLP_MAX_OUT; ++o)
+        if (o < out && lane == o) y[row * out + o] = acc[o];
+      continue;
+    }
+    float gy[MLP_MAX_OUT];
+    float rsum = 0.0f;
+#pragma unroll
+    for (int o = 0; o < MLP_MAX_OUT; ++o) {
+      gy[o] = 0.0f;
+      if (o < out) {
+        const float d = acc[o] - target[row * out + o];
+        rsum += d * d;
+        gy[o] = d * grad_scale;
+        if (lane == o) dy[row * out + o] = gy[o];
+      }
+    }
+    lsum += rsum;  // identical on every lane; lane 0's copy is summed below
+    for (int c = lane; c < nchunks; c += 32) {
+      const float4 p0 = *reinterpret_cast<const float4*>(h2 + row * hid + c * 8);
+      const float4 p1 = *reinterpret_cast<const float4*>(h2 + row * hid + c * 8 + 4);
+      const float pv[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
+      __align__(16) bf16 res[8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e) {
+        float da = 0.0f;
+#pragma unroll
+        for (int o = 0; o < MLP_MAX_OUT; ++o)
+          if (o < out) da += gy[o] * w3s[o * hid + c * 8 + e];
+        res[e] = __float2bfloat16_rn(da * gelu_grad(pv[e]));
+      }
+      *reinterpret_cast<uint4*>(dh2 + row * hid + c * 8) = *reinterpret_cast<const uint4*>(res);
+    }
+  }
+  if (TRAIN) {
+    if (lane == 0) wsum[warp] = lsum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float s = 0.0f;
+      for (int w = 0; w < HEAD_THREADS / 32; ++w) s += wsum[w];
+      loss_part[blockIdx.x] = s;
+    }
+  }
+}
+
+// Column sums over row splits (thread per column c < hid):
+//   pw[z][o][c] = sum_{b in split z} dy[b][o] * a2[b][c]   (o < out; skipped if out == 0)
+//   pb[z][c]    = sum_{b in split z} dh[b][c]
+//   pb3[z][o]   = sum_{b in split z} dy[b][o]               (threads c < out of block 0)
+__global__ void k_colreduce(const float* __restrict__ dy, int out, const bf16* __restrict__ a2,
+                            const bf16* __restrict__ dh, int hid, int64_t rows,
+                            int64_t rows_per_split, float* __restrict__ pw,
+                            float* __restrict__ pb, float* __restrict__ pb3) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  const int z = blockIdx.y;
+  const int64_t b0 = (int64_t)z * rows_per_split;
+  const int64_t b1 = min(rows, b0 + rows_per_split);
+  if (c >= hid) return;
+  float acc[MLP_MAX_OUT];
+#pragma unroll
+  for (int o = 0; o < MLP_MAX_OUT; ++o) acc[o] = 0.0f;
+  float accb = 0.0f, acc3 = 0.0f;
+  const bool do3 = pb3 && blockIdx.x == 0 && c < out;
+  for (int64_t b = b0; b < b1; ++b) {
+    accb += __bfloat162float(dh[b * hid + c]);
+    if (out > 0) {
+      const float x = __bfloat162float(a2[b * hid + c]);
+#pragma unroll
+      for (int o = 0; o < MLP_MAX_OUT; ++o)
+        if (o < out) acc[o] += dy[b * out + o] * x;
+    }
+    if (do3) acc3 += dy[b * out + c];
+  }
+  pb[(int64_t)z * hid + c] = accb;
+#pragma unroll
+  for (int o = 0; o < MLP_MAX_OUT; ++o)
+    if (o < out) pw[((int64_t)z * out + o) * hid + c] = acc[o];
+  if (do3) pb3[(int64_t)z * out + c] = acc3;
+}
+
+// grad[i] = sum_{z < splits} part[z * count + i], in split order.
+__global__ void k_sum_splits(const float* __restrict__ part, int splits, int64_t count,
+                             float* __restrict__ grad) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  float s = 0.0f;
+  for (int z = 0; z < splits; ++z) s += part[(int64_t)z * count + i];
+  grad[i] = s;
+}
+
+// Adam with bias correction (Kingma & Ba, 2015): bc1 = 1 / (1 - beta1^t),
+// bc2 = 1 / (1 - beta2^t).
+__global__ void k_adam(float* __restrict__ p, float* __restrict__ m, float* __restrict__ v,
+                       const float* __restrict__ g, bf16* __restrict__ pb, int64_t count,
+                       float lr, float beta1, float beta2, float eps, float bc1, float bc2) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const float gi = g[i];
+  const float mi = beta1 * m[i] + (1.0f - beta1) * gi;
+  const float vi = beta2 * v[i] + (1.0f - beta2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  const float pi = p[i] - lr * (mi * bc1) / (sqrtf(vi * bc2) + eps);
+  p[i] = pi;
+  pb[i] = __float2bfloat16_rn(pi);
+}
+
+__global__ void k_to_bf16(const float* __restrict__ x, int64_t count, bf16* __restrict__ y) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) y[i] = __float2bfloat16_rn(x[i]);
+}
+
+// Row indices drawn uniformly with replacement from [0, n), keyed by (seed, draw).
+__global__ void k_sample_rows(uint32_t* __restrict__ rows, int64_t count, uint32_t n,
+                              uint64_t seed, uint32_t draw) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const uint4 o = philox4x32_10(make_uint4((uint32_t)i, draw, 0x4D4C5052u, 0x53414D50u),
+                                make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
+  rows[i] = __umulhi(o.x, n);
+}
+
+// dst[i][w] = src[rows[i]][w] for rows of `words` 32-bit words.
+__global__ void k_gather_rows(const uint32_t* __restrict__ src, int64_t words,
+                              const uint32_t* __restrict__ rows, int64_t count,
+                              uint32_t* __restrict__ dst) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count * words) return;
+  const int64_t i = t / words, w = t - i * words;
+  dst[t] = src[(int64_t)rows[i] * words + w];
+}
+
+// out[r][j] = sum_i (x[r][i] - xmean[i]) * R[i][j] + ymean[j], d <= 16.
+// aff = [R (d x d), xmean (d), ymean (d)].
+__global__ void k_affine_rows(const float* __restrict__ x, int64_t rows, int d,
+                              const float* __restrict__ aff, float* __restrict__ out) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  float xc[MLP_MAX_OUT];
+#pragma unroll
+  for (int i = 0; i < MLP_MAX_OUT; ++i) xc[i] = i < d ? x[r * d + i] - aff[d * d + i] : 0.0f;
+  for (int j = 0; j < d; ++j) {
+    float s = aff[d * d + d + j];
+#pragma unroll
+    for (int i = 0; i < MLP_MAX_OUT; ++i)
+      if (i < d) s += xc[i] * aff[i * d + j];
+    out[r * d + j] = s;
+  }
+}
+
+__global__ void k_loss_total(const float* __restrict__ part, int nparts, float scale,
+                             float* __restrict__ dst) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  float s = 0.0f;
+  for (int i = 0; i < nparts; ++i) s += part[i];
+  *dst = s * scale;
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+inline unsigned blocks_for(int64_t n, int threads) {
+  return (unsigned)((n + threads - 1) / threads);
+}
+
+template <bool A_KMAJ, bool B_KMAJ, int EPI>
+void launch_gemm(const GemmArgs& ga, int splits, cudaStream_t s) {
+  EVOC_CUDA(cudaFuncSetAttribute(k_gemm<A_KMAJ, B_KMAJ, EPI>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, GEMM_SMEM));
+  dim3 grid((unsigned)((ga.N + GBN - 1) / GBN), (unsigned)((ga.M + GBM - 1) / GBM),
+            (unsigned)splits);
+  k_gemm<A_KMAJ, B_KMAJ, EPI><<<grid, GTHREADS, GEMM_SMEM, s>>>(ga);
+  EVOC_CHECK_LAUNCH();
+}
+
+// Splits of the K dimension so that tiles x splits covers about two waves.
+void choose_splits(int M, int N, int K, int num_sms, int* splits, int* kchunk) {
+  const int tiles = ((M + GBM - 1) / GBM) * ((N + GBN - 1) / GBN);
+  int want = std::max(1, (2 * num_sms + tiles - 1) / tiles);
+  const int ktiles = std::max(1, (K + GBK - 1) / GBK);
+  want = std::min(want, ktiles);
+  const int per = (ktiles + want - 1) / want;
+  *kchunk = per * GBK;
+  *splits = std::max(1, (K + *kchunk - 1) / *kchunk);
+}
+
+// Scratch of one forward/backward pass over `rows` rows.
+struct MlpScratch {
+  DevBuf<bf16> x, a1, a2, dh1, dh2;
+  DevBuf<float> h1, h2, target, dy, part, loss_part, loss;
+  DevBuf<uint32_t> rows;
+  int64_t cap = 0;
+  int head_grid = 0;
+};
+
+int head_grid_for(const evoc_mlp* net, int64_t rows) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>(
+      (rows + HEAD_THREADS / 32 - 1) / (HEAD_THREADS / 32), 8LL * net->ctx->num_sms));
+}
+
+size_t head_smem(const evoc_mlp* net) { return (size_t)net->out * net->hid * sizeof(float); }
+
+void set_head_smem(const evoc_mlp* net) {
+  const int bytes = (int)head_smem(net);
+  EVOC_CUDA(cudaFuncSetAttribute(k_head<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  EVOC_CUDA(cudaFuncSetAttribute(k_head<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+}
+
+// Split-K partial buffer size of one training pass: the largest of the three
+// weight-gradient reductions.
+int64_t partial_floats(const evoc_mlp* net, int64_t rows, int* s1, int* kc1, int* s2, int* kc2,
+                       int* s3, int64_t* rps3) {
+  const int sms = net->ctx->num_sms;
+  choose_splits(net->hid, net->in, (int)rows, sms, s1, kc1);
+  choose_splits(net->hid, net->hid, (int)rows, sms, s2, kc2);
+  const int colblocks = (net->hid + 127) / 128;
+  int want3 = std::max(1, (2 * sms + colblocks - 1) / colblocks);
+  *rps3 = std::max<int64_t>(1, (rows + want3 - 1) / want3);
+  *s3 = (int)((rows + *rps3 - 1) / *rps3);
+  const int64_t p1 = (int64_t)*s1 * net->hid * net->in;
+  const int64_t p2 = (int64_t)*s2 * net->hid * net->hid;
+  const int64_t p3 = (int64_t)*s3 * ((int64_t)net->out * net->hid + 2 * net->hid + net->out);
+  return std::max(p1, std::max(p2, p3));
+}
+
+void alloc_scratch(const evoc_mlp* net, MlpScratch& sc, int64_t rows, bool train) {
+  cudaStream_t s = net->ctx->stream;
+  sc.cap = rows;
+  sc.x.alloc((size_t)rows * net->in, s);
+  sc.a1.alloc((size_t)rows * net->hid, s);
+  sc.a2.alloc((size_t)rows * net->hid, s);
+  sc.head_grid = head_grid_for(net, rows);
+  if (!train) return;
+  int s1, kc1, s2, kc2, s3;
+  int64_t rps3;
+  const int64_t pf = partial_floats(net, rows, &s1, &kc1, &s2, &kc2, &s3, &rps3);
+  sc.h1.alloc((size_t)rows * net->hid, s);
+  sc.h2.alloc((size_t)rows * net->hid, s);
+  sc.dh1.alloc((size_t)rows * net->hid, s);
+  sc.dh2.alloc((size_t)rows * net->hid, s);
+  sc.target.alloc((size_t)rows * net->out, s);
+  sc.dy.alloc((size_t)rows * net->out, s);
+  sc.part.alloc((size_t)pf, s);
+  sc.loss_part.alloc((size_t)sc.head_grid, s);
+  sc.rows.alloc((size_t)rows, s);
+}
+
+// Forward over `rows` rows of BF16 input x (device); inference writes y.
+void forward(const evoc_mlp* net, const bf16* x, int64_t rows, MlpScratch& sc, bool train,
+             float* y) {
+  cudaStream_t s = net->ctx->stream;
+  const bf16* wb = net->wb.get();
+  const float* mp = net->master.get();
+  GemmArgs g1{};
+  g1.a = x; g1.lda = net->in;
+  g1.b = wb + net->o_w1; g1.ldb = net->in;
+  g1.M = (int)rows; g1.N = net->hid; g1.K = net->in; g1.kchunk = ((net->in + GBK - 1) / GBK) * GBK;
+  g1.bias = mp + net->o_b1;
+  g1.pre = train ? sc.h1.get() : nullptr;
+  g1.outb = sc.a1.get();
+  launch_gemm<true, true, EPI_BIAS_GELU>(g1, 1, s);
+  GemmArgs g2{};
+  g2.a = sc.a1.get(); g2.lda = net->hid;
+  g2.b = wb + net->o_w2; g2.ldb = net->hid;
+  g2.M = (int)rows; g2.N = net->hid; g2.K = net->hid; g2.kchunk = ((net->hid + GBK - 1) / GBK) * GBK;
+  g2.bias = mp + net->o_b2;
+  g2.pre = train ? sc.h2.get() : nullptr;
+  g2.outb = sc.a2.get();
+  launch_gemm<true, true, EPI_BIAS_GELU>(g2, 1, s);
+  if (!train) {
+    k_head<false><<<head_grid_for(net, rows), HEAD_THREADS, head_smem(net), s>>>(
+        sc.a2.get(), nullptr, net->hid, net->out, rows, wb + net->o_w3, mp + net->o_b3, y,
+        nullptr, 0.0f, nullptr, nullptr, nullptr);
+    EVOC_CHECK_LAUNCH();
+  }
+}
+
+// Forward + backward over the batch in sc.x / sc.target (rows rows); leaves
+// the packed gradient in net->grad and the mean-squared error in *loss_dst.
+void forward_backward(evoc_mlp* net, int64_t rows, MlpScratch& sc, float* loss_dst) {
+  cudaStream_t s = net->ctx->stream;
+  const bf16* wb = net->wb.get();
+  const float* mp = net->master.get();
+  forward(net, sc.x.get(), rows, sc, true, nullptr);
+  const int hg = head_grid_for(net, rows);
+  const float scale = 1.0f / (float)((double)rows * net->out);
+  k_head<true><<<hg, HEAD_THREADS, head_smem(net), s>>>(
+      sc.a2.get(), sc.h2.get(), net->hid, net->out, rows, wb + net->o_w3, mp + net->o_b3,
+      nullptr, sc.target.get(), 2.0f * scale, sc.dy.get(), sc.dh2.get(), sc.loss_part.get());
+  EVOC_CHECK_LAUNCH();
+  k_loss_total<<<1, 32, 0, s>>>(sc.loss_part.get(), hg, scale, loss_dst);
+  EVOC_CHECK_LAUNCH();
+  // dH1 = (dH2 W2) * gelu'(H1): W2 is [out][in] = [K][N], read MN-major.
+  GemmArgs gd{};
+  gd.a = sc.dh2.get(); gd.lda = net->hid;
+  gd.b = wb + net->o_w2; gd.ldb = net->hid;
+  gd.M = (int)rows; gd.N = net->hid; gd.K = net->hid; gd.kchunk = ((net->hid + GBK - 1) / GBK) * GBK;
+  gd.pre = sc.h1.get();
+  gd.outb = sc.dh1.get();
+  launch_gemm<true, false, EPI_GELU_GRAD>(gd, 1, s);
+
+  int s1, kc1, s2, kc2, s3;
+  int64_t rps3;
+  partial_floats(net, rows, &s1, &kc1, &s2, &kc2, &s3, &rps3);
+  float* grad = net->grad.get();
+  // dW2 = dH2^T A1 (both [batch][hidden]: MN-major with the batch as K).
+  GemmArgs gw2{};
+  gw2.a = sc.dh2.get(); gw2.lda = net->hid;
+  gw2.b = sc.a1.get(); gw2.ldb = net->hid;
+  gw2.M = net->hid; gw2.N = net->hid; gw2.K = (int)rows; gw2.kchunk = kc2;
+  gw2.outf = sc.part.get();
+  launch_gemm<false, false, EPI_PARTIAL>(gw2, s2, s);
+  const int64_t cw2 = (int64_t)net->hid * net->hid;
+  k_sum_splits<<<blocks_for(cw2, 256), 256, 0, s>>>(sc.part.get(), s2, cw2, grad + net->o_w2);
+  EVOC_CHECK_LAUNCH();
+  // dW1 = dH1^T X.
+  GemmArgs gw1{};
+  gw1.a = sc.dh1.get(); gw1.lda = net->hid;
+  gw1.b = sc.x.get(); gw1.ldb = net->in;
+  gw1.M = net->hid; gw1.N = net->in; gw1.K = (int)rows; gw1.kchunk = kc1;
+  gw1.outf = sc.part.get();
+  launch_gemm<false, false, EPI_PARTIAL>(gw1, s1, s);
+  const int64_t cw1 = (int64_t)net->hid * net->in;
+  k_sum_splits<<<blocks_for(cw1, 256), 256, 0, s>>>(sc.part.get(), s1, cw1, grad + net->o_w1);
+  EVOC_CHECK_LAUNCH();
+  // dW3, db2, db3 in one column pass; then db1.
+  float* pw3 = sc.part.get();
+  float* pb2 = pw3 + (int64_t)s3 * net->out * net->hid;
+  float* pb3 = pb2 + (int64_t)s3 * net->hid;
+  float* pb1 = pb3 + (int64_t)s3 * net->out;
+  dim3 cg((unsigned)((net->hid + 127) / 128), (unsigned)s3);
+  k_colreduce<<<cg, 128, 0, s>>>(sc.dy.get(), net->out, sc.a2.get(), sc.dh2.get(), net->hid,
+                                 rows, rps3, pw3, pb2, pb3);
+  EVOC_CHECK_LAUNCH();
+  k_colreduce<<<cg, 128, 0, s>>>(nullptr, 0, nullptr, sc.dh1.get(), net->hid, rows, rps3,
+                                 nullptr, pb1, nullptr);
+  EVOC_CHECK_LAUNCH();
+  const int64_t cw3 = (int64_t)net->out * net->hid;
+  k_sum_splits<<<blocks_for(cw3, 256), 256, 0, s>>>(pw3, s3, cw3, grad + net->o_w3);
+  k_sum_splits<<<blocks_for(net->hid, 256), 256, 0, s>>>(pb2, s3, net->hid, grad + net->o_b2);
+  k_sum_splits<<<1, 32, 0, s>>>(pb3, s3, net->out, grad + net->o_b3);
+  k_sum_splits<<<blocks_for(net->hid, 256), 256, 0, s>>>(pb1, s3, net->hid, grad + net->o_b1);
+  EVOC_CHECK_LAUNCH();
+}
+
+void adam_step(evoc_mlp* net, float lr, float beta1, float beta2, float eps) {
+  net->adam_steps += 1;
+  const double t = (double)net->adam_steps;
+  const float bc1 = (float)(1.0 / (1.0 - std::pow((double)beta1, t)));
+  const float bc2 = (float)(1.0 / (1.0 - std::pow((double)beta2, t)));
+  k_adam<<<blocks_for(net->n_params, 256), 256, 0, net->ctx->stream>>>(
+      net->master.get(), net->adam_m.get(), net->adam_v.get(), net->grad.get(), net->wb.get(),
+      net->n_params, lr, beta1, beta2, eps, bc1, bc2);
+  EVOC_CHECK_LAUNCH();
+}
+
+void refresh_bf16(evoc_mlp* net) {
+  k_to_bf16<<<blocks_for(net->n_params, 256), 256, 0, net->ctx->stream>>>(
+      net->master.get(), net->n_params, net->wb.get());
+  EVOC_CHECK_LAUNCH();
+}
+
+// splitmix64: the host-side generator of the initial weights.
+uint64_t splitmix64(uint64_t& s) {
+  uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Orthogonal Procrustes: the orthogonal R (d x d) maximising tr(R^T M), i.e.
+// R = U V^T for M = U S V^T, by one-sided Jacobi rotations on the columns of
+// M (Hestenes' method). For M = X^T Y with centred X, Y it minimises
+// ||X R - Y||_F. Columns with a vanishing singular value get an orthonormal
+// completion.
+// ---------------------------------------------------------------------------
+void procrustes(const double* m, int d, double* r) {
+  std::vector<double> a(m, m + (size_t)d * d), v((size_t)d * d, 0.0), u((size_t)d * d, 0.0);
+  for (int i = 0; i < d; ++i) v[(size_t)i * d + i] = 1.0;
+  auto A = [&](int i, int j) -> double& { return a[(size_t)i * d + j]; };
+  auto V = [&](int i, int j) -> double& { return v[(size_t)i * d + j]; };
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    bool rotated = false;
+    for (int p = 0; p < d - 1; ++p) {
+      for (int q = p + 1; q < d; ++q) {
+        double alpha = 0, beta = 0, gamma = 0;
+        for (int i = 0; i < d; ++i) {
+          alpha += A(i, p) * A(i, p);
+          beta += A(i, q) * A(i, q);
+          gamma += A(i, p) * A(i, q);
+        }
+        if (std::fabs(gamma) <= 1e-15 * std::sqrt(alpha * beta) || gamma == 0.0) continue;
+        rotated = true;
+        const double zeta = (beta - alpha) / (2.0 * gamma);
+        const double t = (zeta >= 0 ? 1.0 : -1.0) / (std::fabs(zeta) + std::sqrt(1.0 + zeta * zeta));
+        const double c = 1.0 / std::sqrt(1.0 + t * t), s = c * t;
+        for (int i = 0; i < d; ++i) {
+          const double ap = A(i, p), aq = A(i, q);
+          A(i, p) = c * ap - s * aq;
+          A(i, q) = s * ap + c * aq;
+          const double vp = V(i, p), vq = V(i, q);
+          V(i, p) = c * vp - s * vq;
+          V(i, q) = s * vp + c * vq;
+        }
+      }
+    }
+    if (!rotated) break;
+  }
+  // U = A S^-1, columns in order of decreasing singular value get first pick
+  // when a completion is needed.
+  std::vector<double> sig(d);
+  double smax = 0;
+  for (int j = 0; j < d; ++j) {
+    double s2 = 0;
+    for (int i = 0; i < d; ++i) s2 += A(i, j) * A(i, j);
+    sig[j] = std::sqrt(s2);
+    smax = std::max(smax, sig[j]);
+  }
+  std::vector<int> order(d);
+  for (int j = 0; j < d; ++j) order[j] = j;
+  std::sort(order.begin(), order.end(), [&](int x, int y) { return sig[x] > sig[y]; });
+  std::vector<bool> done(d, false);
+  for (int j : order) {
+    if (sig[j] > 1e-12 * smax && smax > 0) {
+      for (int i = 0; i < d; ++i) u[(size_t)i * d + j] = A(i, j) / sig[j];
+      done[j] = true;
+    }
+  }
+  for (int j : order) {
+    if (done[j]) continue;
+    for (int e = 0; e < d && !done[j]; ++e) {  // Gram-Schmidt on unit vectors
+      std::vector<double> w(d, 0.0);
+      w[e] = 1.0;
+      for (int k = 0; k < d; ++k) {
+        if (!done[k]) continue;
+        double dot = 0;
+        for (int i = 0; i < d; ++i) dot += w[i] * u[(size_t)i * d + k];
+        for (int i = 0; i < d; ++i) w[i] -= dot * u[(size_t)i * d + k];
+      }
+      double nrm = 0;
+      for (int i = 0; i < d; ++i) nrm += w[i] * w[i];
+      nrm = std::sqrt(nrm);
+      if (nrm < 1e-6) continue;
+      for (int i = 0; i < d; ++i) u[(size_t)i * d + j] = w[i] / nrm;
+      done[j] = true;
+    }
+  }
+  for (int i = 0; i < d; ++i)
+    for (int j = 0; j < d; ++j) {
+      double s = 0;
+      for (int k = 0; k < d; ++k) s += u[(size_t)i * d + k] * V(j, k);
+      r[(size_t)i * d + j] = s;
+    }
+}
+
+evoc_mlp* mlp_create(evoc_ctx* ctx, int in, int hid, int out, uint64_t seed) {
+  if (in <= 0 || hid <= 0 || out <= 0 || in % 8 != 0 || hid % 8 != 0)
+    throw Error(EVOC_ERR_INVALID_ARGUMENT, "in_dim and hidden must be positive multiples of 8");
+  if (out > MLP_MAX_OUT) throw Error(EVOC_ERR_UNSUPPORTED, "out_dim must be in 1..16");
+  if (in > 65536 || hid > 8192)
+    throw Error(EVOC_ERR_UNSUPPORTED, "in_dim above 65536 or hidden above 8192");
+  if ((size_t)out * hid * sizeof(float) > 200 * 1024)
+    throw Error(EVOC_ERR_UNSUPPORTED, "out_dim x hidden too large for the output layer");
+  std::unique_ptr<evoc_mlp> net(new evoc_mlp());
+  net->ctx = ctx;
+  net->in = in;
+  net->hid = hid;
+  net->out = out;
+  net->o_w1 = 0;
+  net->o_b1 = net->o_w1 + (int64_t)hid * in;
+  net->o_w2 = net->o_b1 + hid;
+  net->o_b2 = net->o_w2 + (int64_t)hid * hid;
+  net->o_w3 = net->o_b2 + hid;
+  net->o_b3 = net->o_w3 + (int64_t)out * hid;
+  net->n_params = net->o_b3 + out;
+  cudaStream_t s = ctx->stream;
+  const size_t np = (size_t)net->n_params;
+  net->master.alloc(np, s);
+  net->adam_m.alloc(np, s);
+  net->adam_v.alloc(np, s);
+  net->grad.alloc(np, s);
+  net->wb.alloc(np, s);
+  // Linear-layer initialisation: weights and biases uniform in
+  // [-1/sqrt(fan_in), 1/sqrt(fan_in)).
+  std::vector<float> h(np);
+  uint64_t st = seed;
+  auto fill = [&](int64_t off, int64_t count, int fan_in) {
+    const double bound = 1.0 / std::sqrt((double)fan_in);
+    for (int64_t i = 0; i < count; ++i) {
+      const double u = (double)(splitmix64(st) >> 11) * (1.0 / 9007199254740992.0);
+      h[(size_t)(off + i)] = (float)((2.0 * u - 1.0) * bound);
+    }
+  };
+  fill(net->o_w1, (int64_t)hid * in, in);
+  fill(net->o_b1, hid, in);
+  fill(net->o_w2, (int64_t)hid * hid, hid);
+  fill(net->o_b2, hid, hid);
+  fill(net->o_w3, (int64_t)out * hid, hid);
+  fill(net->o_b3, out, hid);
+  EVOC_CUDA(cudaMemcpyAsync(net->master.get(), h.data(), np * sizeof(float),
+                            cudaMemcpyHostToDevice, s));
+  EVOC_CUDA(cudaMemsetAsync(net->adam_m.get(), 0, np * sizeof(float), s));
+  EVOC_CUDA(cudaMemsetAsync(net->adam_v.get(), 0, np * sizeof(float), s));
+  EVOC_CUDA(cudaMemsetAsync(net->grad.get(), 0, np * sizeof(float), s));
+  refresh_bf16(net.get());
+  set_head_smem(net.get());
+  EVOC_CUDA(cudaStreamSynchronize(s));
+  return net.release();
+}
+
+void mlp_free(evoc_mlp* net) {
+  if (!net) return;
+  cudaStream_t s = net->ctx ? net->ctx->stream : nullptr;
+  net->master.release();
+  net->adam_m.release();
+  net->adam_v.release();
+  net->grad.release();
+  net->wb.release();
+  if (s) cudaStreamSynchronize(s);
+  delete net;
+}
+
+evoc_ctx* mlp_ctx(const evoc_mlp* net) { return net->ctx; }
+int64_t mlp_n_params(const evoc_mlp* net) { return net->n_params; }
+void mlp_dims(const evoc_mlp* net, int32_t* in, int32_t* hid, int32_t* out) {
+  if (in) *in = net->in;
+  if (hid) *hid = net->hid;
+  if (out) *out = net->out;
+}
+
+void mlp_get_params(const evoc_mlp* net, float* host) {
+  cudaStream_t s = net->ctx->stream;
+  EVOC_CUDA(cudaMemcpyAsync(host, net->master.get(), net->master.bytes(), cudaMemcpyDeviceToHost, s));
+  EVOC_CUDA(cudaStreamSynchronize(s));
+}
+
+void mlp_set_params(evoc_mlp* net, const float* host) {
+  cudaStream_t s = net->ctx->stream;
+  EVOC_CUDA(cudaMemcpyAsync(net->master.get(), host, net->master.bytes(), cudaMemcpyHostToDevice, s));
+  EVOC_CUDA(cudaMemsetAsync(net->adam_m.get(), 0, net->adam_m.bytes(), s));
+  EVOC_CUDA(cudaMemsetAsync(net->adam_v.get(), 0, net->adam_v.bytes(), s));
+  net->adam_steps = 0;
+  refresh_bf16(net);
+  EVOC_CUDA(cudaStreamSynchronize(s));
+}
+
+void to_bf16_device(evoc_ctx* ctx, const float* x, int64_t count, uint16_t* y) {
+  if (count == 0) return;
+  k_to_bf16<<<blocks_for(count, 256), 256, 0, ctx->stream>>>(x, count, reinterpret_cast<bf16*>(y));
+  EVOC_CHECK_LAUNCH();
+}
+
+constexpr int64_t PREDICT_CHUNK = 65536;
+
+void mlp_predict_device(evoc_mlp* net, const uint16_t* x, int64_t n, float* y) {
+  if (n == 0) return;
+  MlpScratch sc;
+  const int64_t chunk = std::min(n, PREDICT_CHUNK);
+  alloc_scratch(net, sc, chunk, false);
+  const bf16* xb = reinterpret_cast<const bf16*>(x);
+  for (int64_t r0 = 0; r0 < n; r0 += chunk) {
+    const int64_t rows = std::min(chunk, n - r0);
+    forward(net, xb + r0 * net->in, rows, sc, false, y + r0 * net->out);
+  }
+}
+
+void mlp_predict_host(evoc_mlp* net, const float* x, int64_t n, float* y) {
+  if (n == 0) return;
+  cudaStream_t s = net->ctx->stream;
+  const int64_t chunk = std::min(n, PREDICT_CHUNK);
+  MlpScratch sc;
+  alloc_scratch(net, sc, chunk, false);
+  DevBuf<float> xf((size_t)chunk * net->in, s), yd((size_t)chunk * net->out, s);
+  for (int64_t r0 = 0; r0 < n; r0 += chunk) {
+    const int64_t rows = std::min(chunk, n - r0);
+    EVOC_CUDA(cudaMemcpyAsync(xf.get(), x + r0 * net->in, (size_t)rows * net->in * sizeof(float),
+                              cudaMemcpyHostToDevice, s));
+    to_bf16_device(net->ctx, xf.get(), rows * net->in, reinterpret_cast<uint16_t*>(sc.x.get()));
+    forward(net, sc.x.get(), rows, sc, false, yd.get());
+    EVOC_CUDA(cudaMemcpyAsync(y + r0 * net->out, yd.get(), (size_t)rows * net->out * sizeof(float),
+                              cudaMemcpyDeviceToHost, s));
+  }
+  EVOC_CUDA(cudaStreamSynchronize(s));
+}
+
+void mlp_gradients_host(evoc_mlp* net, const float* x, const float* target, int64_t n,
+                        float* loss, float* grad) {
+  if (n <= 0) throw Error(EVOC_ERR_INVALID_ARGUMENT, "n must be positive");
+  if (n > (1LL << 24)) throw Error(EVOC_ERR_UNSUPPORTED, "at most 2^24 rows per gradient call");
+  cudaStream_t s = net->ctx->stream;
+  MlpScratch sc;
+  alloc_scratch(net, sc, n, true);
+  DevBuf<float> xf((size_t)n * net->in, s), ld(1, s);
+  EVOC_CUDA(cudaMemcpyAsync(xf.get(), x, xf.bytes(), cudaMemcpyHostToDevice, s));
+  EVOC_CUDA(cudaMemcpyAsync(sc.target.get(), target, (size_t)n * net->out * sizeof(float),
+                            cudaMemcpyHostToDevice, s));
+  to_bf16_device(net->ctx, xf.get(), n * net->in, reinterpret_cast<uint16_t*>(sc.x.get()));
+  forward_backward(net, n, sc, ld.get());
+  EVOC_CUDA(cudaMemcpyAsync(grad, net->grad.get(), net->grad.bytes(), cudaMemcpyDeviceToHost, s));
+  EVOC_CUDA(cudaMemcpyAsync(loss, ld.get(), sizeof(float), cudaMemcpyDeviceToHost, s));
+  EVOC_CUDA(cudaStreamSynchronize(s));
+}
+
+// Training on layouts of several instances: every `align_every` steps each
+// instance's layout is re-aligned to the network's prediction on a fixed
+// sample of its rows (means removed, Procrustes rotation, prediction mean
+// added); each step then draws `batch` rows of one instance (round robin)
+// and takes one Adam step on the MSE against the aligned layout.
+void mlp_fit_device(evoc_mlp* net, int32_t m, const uint16_t* const* xs,
+                    const float* const* layouts, const int64_t* ns,
+                    const evoc_mlp_train_params_t* p, float* loss_history) {
+  if (m <= 0 || !xs || !layouts || !ns || !p) throw Error(EVOC_ERR_INVALID_ARGUMENT, "bad argument");
+  if (p->steps < 0 || p->batch <= 0 || p->batch > (1 << 22) || p->align_every <= 0 ||
+      p->align_rows <= 0)
+    throw Error(EVOC_ERR_INVALID_ARGUMENT, "bad training parameters");
+  for (int32_t i = 0; i < m; ++i) {
+    if (!xs[i] || !layouts[i] || ns[i] <= 0 || ns[i] >= 0xFFFFFFFFLL)
+      throw Error(EVOC_ERR_INVALID_ARGUMENT, "bad instance " + std::to_string(i));
+  }
+  cudaStream_t s = net->ctx->stream;
+  const int d = net->out;
+  const int64_t batch = p->batch;
+  MlpScratch sc;
+  alloc_scratch(net, sc, batch, true);
+  // aligned layouts and the fixed alignment sample of every instance
+  std::vector<DevBuf<float>> aligned(m);
+  std::vector<DevBuf<uint32_t>> sample(m);
+  std::vector<int64_t> ns_sample(m);
+  for (int32_t i = 0; i < m; ++i) {
+    aligned[i].alloc((size_t)ns[i] * d, s);
+    EVOC_CUDA(cudaMemcpyAsync(aligned[i].get(), layouts[i], (size_t)ns[i] * d * sizeof(float),
+                              cudaMemcpyDeviceToDevice, s));
+    ns_sample[i] = std::min<int64_t>(ns[i], p->align_rows);
+    sample[i].alloc((size_t)ns_sample[i], s);
+    k_sample_rows<<<blocks_for(ns_sample[i], 256), 256, 0, s>>>(
+        sample[i].get(), ns_sample[i], (uint32_t)ns[i], p->seed ^ 0xA11A11A11ull, (uint32_t)i);
+    EVOC_CHECK_LAUNCH();
+  }
+  const int64_t max_sample = *std::max_element(ns_sample.begin(), ns_sample.end());
+  MlpScratch sp;  // prediction on an alignment sample
+  alloc_scratch(net, sp, std::min<int64_t>(max_sample, PREDICT_CHUNK), false);
+  DevBuf<bf16> xs_s((size_t)max_sample * net->in, s);
+  DevBuf<float> pred((size_t)max_sample * d, s), tsamp((size_t)max_sample * d, s);
+  DevBuf<float> aff((size_t)d * d + 2 * d, s);
+  DevBuf<float> losses((size_t)std::max(1, p->steps), s);
+  std::vector<float> hp((size_t)max_sample * d), ht((size_t)max_sample * d);
+  std::vector<float> haff((size_t)d * d + 2 * d);
+
+  auto realign = [&](int32_t i) {
+    const int64_t k = ns_sample[i];
+    k_gather_rows<<<blocks_for(k * net->in / 2, 256), 256, 0, s>>>(
+        reinterpret_cast<const uint32_t*>(xs[i]), net->in / 2, sample[i].get(), k,
+        reinterpret_cast<uint32_t*>(xs_s.get()));
+    EVOC_CHECK_LAUNCH();
+    k_gather_rows<<<blocks_for(k * d, 256), 256, 0, s>>>(
+        reinterpret_cast<const uint32_t*>(layouts[i]), d, sample[i].get(), k,
+        reinterpret_cast<uint32_t*>(tsamp.get()));
+    EVOC_CHECK_LAUNCH();
+    const int64_t chunk = std::min<int64_t>(k, PREDICT_CHUNK);
+    for (int64_t r0 = 0; r0 < k; r0 += chunk) {
+      const int64_t rows = std::min(chunk, k - r0);
+      forward(net, xs_s.get() + r0 * net->in, rows, sp, false, pred.get() + r0 * d);
+    }
+    EVOC_CUDA(cudaMemcpyAsync(hp.data(), pred.get(), (size_t)k * d * sizeof(float),
+                              cudaMemcpyDeviceToHost, s));
+    EVOC_CUDA(cudaMemcpyAsync(ht.data(), tsamp.get(), (size_t)k * d * sizeof(float),
+                              cudaMemcpyDeviceToHost, s));
+    EVOC_CUDA(cudaStreamSynchronize(s));
+    std::vector<double> tm(d, 0.0), pm(d, 0.0), mm((size_t)d * d, 0.0), rr((size_t)d * d);
+    for (int64_t r = 0; r < k; ++r)
+      for (int j = 0; j < d; ++j) {
+        tm[j] += ht[(size_t)r * d + j];
+        pm[j] += hp[(size_t)r * d + j];
+      }
+    for (int j = 0; j < d; ++j) {
+      tm[j] /= (double)k;
+      pm[j] /= (double)k;
+    }
+    for (int64_t r = 0; r < k; ++r)
+      for (int a = 0; a < d; ++a) {
+        const double ta = ht[(size_t)r * d + a] - tm[a];
+        for (int b = 0; b < d; ++b) mm[(size_t)a * d + b] += ta * (hp[(size_t)r * d + b] - pm[b]);
+      }
+    procrustes(mm.data(), d, rr.data());
+    for (int j = 0; j < d * d; ++j) haff[j] = (float)rr[j];
+    for (int j = 0; j < d; ++j) {
+      haff[(size_t)d * d + j] = (float)tm[j];
+      haff[(size_t)d * d + d + j] = (float)pm[j];
+    }
+    EVOC_CUDA(cudaMemcpyAsync(aff.get(), haff.data(), haff.size() * sizeof(float),
+                              cudaMemcpyHostToDevice, s));
+    k_affine_rows<<<blocks_for(ns[i], 256), 256, 0, s>>>(layouts[i], ns[i], d, aff.get(),
+                                                         aligned[i].get());
+    EVOC_CHECK_LAUNCH();
+    EVOC_CUDA(cudaStreamSynchronize(s));  // haff is reused by the next call
+  };
+
+  for (int32_t step = 0; step < p->steps; ++step) {
+    if (step % p->align_every == 0)
+      for (int32_t i = 0; i < m; ++i) realign(i);
+    const int32_t i = step % m;
+    k_sample_rows<<<blocks_for(batch, 256), 256, 0, s>>>(sc.rows.get(), batch, (uint32_t)ns[i],
+                                                         p->seed, (uint32_t)step);
+    EVOC_CHECK_LAUNCH();
+    k_gather_rows<<<blocks_for(batch * net->in / 2, 256), 256, 0, s>>>(
+        reinterpret_cast<const uint32_t*>(xs[i]), net->in / 2, sc.rows.get(), batch,
+        reinterpret_cast<uint32_t*>(sc.x.get()));
+    EVOC_CHECK_LAUNCH();
+    k_gather_rows<<<blocks_for(batch * d, 256), 256, 0, s>>>(
+        reinterpret_cast<const uint32_t*>(aligned[i].get()), d, sc.rows.get(), batch,
+        reinterpret_cast<uint32_t*>(sc.target.get()));
+    EVOC_CHECK_LAUNCH();
+    forward_backward(net, batch, sc, losses.get() + step);
+    adam_step(net, p->lr, p->beta1, p->beta2, p->eps);
+  }
+  if (loss_history && p->steps > 0)
+    EVOC_CUDA(cudaMemcpyAsync(loss_history, losses.get(), (size_t)p->steps * sizeof(float),
+                              cudaMemcpyDeviceToHost, s));
+  EVOC_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace evoc

@@ -47,6 +47,10 @@ EXPORTED = [
     "evoc_plan_debug_run", "evoc_plan_free", "evoc_embed_batched",
     "evoc_knn_to_csr_noalloc", "evoc_gather_peak", "evoc_plan_create_batched",
     "evoc_fuzzy_set_batched", "evoc_plan_create_blocks", "evoc_embed_blocks",
+    "evoc_mlp_train_params_default", "evoc_mlp_create", "evoc_mlp_free",
+    "evoc_mlp_n_params", "evoc_mlp_get_params", "evoc_mlp_set_params", "evoc_mlp_predict",
+    "evoc_mlp_predict_device", "evoc_mlp_gradients", "evoc_mlp_fit_device",
+    "evoc_to_bf16_device", "evoc_procrustes",
 ]
 
 
@@ -66,6 +70,39 @@ class EmbedParamsC(C.Structure):
         ("beta2", C.c_float),
         ("eps", C.c_float),
     ]
+
+
+class MlpTrainParamsC(C.Structure):
+    _fields_ = [
+        ("steps", C.c_int32),
+        ("batch", C.c_int32),
+        ("align_every", C.c_int32),
+        ("align_rows", C.c_int32),
+        ("lr", C.c_float),
+        ("beta1", C.c_float),
+        ("beta2", C.c_float),
+        ("eps", C.c_float),
+        ("seed", C.c_uint64),
+    ]
+
+
+@dataclass
+class MlpTrainParams:
+    """evoc_mlp_train_params_t with its defaults."""
+    steps: int = 3000
+    batch: int = 8192
+    align_every: int = 250
+    align_rows: int = 65536
+    lr: float = 1e-3
+    beta1: float = 0.9
+    beta2: float = 0.999
+    eps: float = 1e-8
+    seed: int = 0
+
+    def to_c(self) -> MlpTrainParamsC:
+        return MlpTrainParamsC(int(self.steps), int(self.batch), int(self.align_every),
+                               int(self.align_rows), self.lr, self.beta1, self.beta2,
+                               self.eps, int(self.seed))
 
 
 class EpochStatsC(C.Structure):
@@ -137,6 +174,18 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "evoc_embed_batched": ([vp, i32, vp, i32, C.POINTER(EmbedParamsC), vp, vp, vp], C.c_int),
         "evoc_knn_to_csr_noalloc": ([vp, vp, i64, i32, f32, vp, vp, vp, i64, C.POINTER(i64), vp],
                                     C.c_int),
+        "evoc_mlp_train_params_default": ([C.POINTER(MlpTrainParamsC)], None),
+        "evoc_mlp_create": ([vp, i32, i32, i32, u64, pp], C.c_int),
+        "evoc_mlp_free": ([vp], None),
+        "evoc_mlp_n_params": ([vp], i64),
+        "evoc_mlp_get_params": ([vp, vp], C.c_int),
+        "evoc_mlp_set_params": ([vp, vp], C.c_int),
+        "evoc_mlp_predict": ([vp, vp, i64, vp], C.c_int),
+        "evoc_mlp_predict_device": ([vp, vp, i64, vp], C.c_int),
+        "evoc_mlp_gradients": ([vp, vp, vp, i64, vp, vp], C.c_int),
+        "evoc_mlp_fit_device": ([vp, i32, vp, vp, vp, C.POINTER(MlpTrainParamsC), vp], C.c_int),
+        "evoc_to_bf16_device": ([vp, vp, i64, vp], C.c_int),
+        "evoc_procrustes": ([vp, i32, vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(lib, name)
@@ -266,6 +315,99 @@ class Plan:
             pass
 
 
+class Mlp:
+    """The learned warm start (evoc_mlp_t): in_dim -> hidden -> hidden -> out_dim."""
+
+    def __init__(self, ctx: "Context", handle, in_dim: int, hidden: int, out_dim: int):
+        self._ctx = ctx
+        self.handle = handle
+        ctx._children.add(self)
+        self.in_dim, self.hidden, self.out_dim = in_dim, hidden, out_dim
+
+    @property
+    def n_params(self) -> int:
+        return int(self._ctx.lib.evoc_mlp_n_params(self.handle))
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.n_params, dtype=np.float32)
+        self._ctx._check(self._ctx.lib.evoc_mlp_get_params(self.handle, _ptr(out)))
+        return out
+
+    def set_params(self, params) -> None:
+        p = _f32(params)
+        if p.shape != (self.n_params,):
+            raise ValueError(f"expected {self.n_params} parameters")
+        self._ctx._check(self._ctx.lib.evoc_mlp_set_params(self.handle, _ptr(p)))
+
+    def unpack(self, flat: np.ndarray) -> dict:
+        """Split a packed parameter (or gradient) array into named arrays."""
+        i, h, o = self.in_dim, self.hidden, self.out_dim
+        sizes = [("w1", (h, i)), ("b1", (h,)), ("w2", (h, h)), ("b2", (h,)),
+                 ("w3", (o, h)), ("b3", (o,))]
+        out, at = {}, 0
+        for name, shape in sizes:
+            cnt = int(np.prod(shape))
+            out[name] = flat[at:at + cnt].reshape(shape)
+            at += cnt
+        return out
+
+    def predict(self, x) -> np.ndarray:
+        xx = _f32(x)
+        n = xx.shape[0]
+        out = np.zeros((n, self.out_dim), dtype=np.float32)
+        self._ctx._check(self._ctx.lib.evoc_mlp_predict(self.handle, _ptr(xx), n, _ptr(out)))
+        return out
+
+    def predict_device(self, d_x_bf16: int, n: int, d_out: int) -> None:
+        self._ctx._check(self._ctx.lib.evoc_mlp_predict_device(
+            self.handle, C.c_void_p(d_x_bf16), int(n), C.c_void_p(d_out)))
+
+    def gradients(self, x, target) -> tuple[float, np.ndarray]:
+        xx, tt = _f32(x), _f32(target)
+        loss = np.zeros(1, dtype=np.float32)
+        grad = np.zeros(self.n_params, dtype=np.float32)
+        self._ctx._check(self._ctx.lib.evoc_mlp_gradients(
+            self.handle, _ptr(xx), _ptr(tt), xx.shape[0], _ptr(loss), _ptr(grad)))
+        return float(loss[0]), grad
+
+    def fit_device(self, d_points_bf16: Sequence[int], d_layouts: Sequence[int],
+                   n_rows: Sequence[int], params: MlpTrainParams | None = None) -> np.ndarray:
+        """Train on device-resident (BF16 points, f32 layout) instances; returns
+        the per-step mean squared error."""
+        p = (params or MlpTrainParams()).to_c()
+        m = len(n_rows)
+        xh = (C.c_void_p * m)(*[int(a) for a in d_points_bf16])
+        lh = (C.c_void_p * m)(*[int(a) for a in d_layouts])
+        nh = np.ascontiguousarray(n_rows, dtype=np.int64)
+        hist = np.zeros(max(1, p.steps), dtype=np.float32)
+        self._ctx._check(self._ctx.lib.evoc_mlp_fit_device(
+            self.handle, m, xh, lh, _ptr(nh), C.byref(p), _ptr(hist)))
+        return hist[:p.steps]
+
+    def free(self) -> None:
+        if self.handle and self._ctx.handle:  # a closed context freed it already
+            self._ctx.lib.evoc_mlp_free(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def procrustes(m, lib_path: str | None = None) -> np.ndarray:
+    """evoc_procrustes: the orthogonal R maximising trace(R^T M) (host only)."""
+    lib = load_library(lib_path)
+    mm = np.ascontiguousarray(m, dtype=np.float64)
+    d = mm.shape[0]
+    r = np.zeros((d, d), dtype=np.float64)
+    rc = lib.evoc_procrustes(_ptr(mm), d, _ptr(r))
+    if rc != EVOC_OK:
+        raise EvocError(rc, lib.evoc_last_error(None).decode())
+    return r
+
+
 class Context:
     """One CUDA device and stream (evoc_ctx_t)."""
 
@@ -277,6 +419,16 @@ class Context:
         if rc != EVOC_OK:
             raise EvocError(rc, self.lib.evoc_last_error(None).decode())
         self.handle = h
+
+    def mlp(self, in_dim: int, hidden: int, out_dim: int, seed: int = 0) -> Mlp:
+        h = C.c_void_p()
+        self._check(self.lib.evoc_mlp_create(self.handle, in_dim, hidden, out_dim, seed,
+                                             C.byref(h)))
+        return Mlp(self, h, in_dim, hidden, out_dim)
+
+    def to_bf16_device(self, d_in: int, count: int, d_out: int) -> None:
+        self._check(self.lib.evoc_to_bf16_device(self.handle, C.c_void_p(d_in), int(count),
+                                                 C.c_void_p(d_out)))
 
     def gather_peak(self, nbytes: int = 64 << 20) -> float:
         """Measured L2 random-gather GB/s for 32-byte rows over an nbytes buffer."""

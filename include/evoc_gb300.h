@@ -315,6 +315,79 @@ EVOC_API int evoc_embed_batched(evoc_ctx_t* ctx, int32_t n_problems,
                        const float* const* inits, const uint64_t* seeds,
                        float* const* outs);
 
+/* ---- learned warm start ----------------------------------------------------
+ * No counterpart in the reference: a multilayer perceptron
+ *   in_dim -> hidden -> GELU -> hidden -> GELU -> out_dim
+ * that predicts an initial embedding (the `initial_embedding` argument of
+ * evoc_embedding, embedding.rs:48-76) from the input points, so a run needs
+ * fewer epochs. BF16 tensor-core GEMMs with FP32 accumulation; FP32 master
+ * weights trained by Adam on layouts the plain optimiser produced, each
+ * aligned to the current prediction by an orthogonal Procrustes rotation.
+ *
+ * Parameters are one packed float array of evoc_mlp_n_params() values:
+ *   W1 (hidden x in_dim), b1 (hidden), W2 (hidden x hidden), b2 (hidden),
+ *   W3 (out_dim x hidden), b3 (out_dim)
+ * with weight matrices row-major, output by input.
+ * in_dim and hidden are multiples of 8; 1 <= out_dim <= 16. */
+typedef struct evoc_mlp evoc_mlp_t;
+
+typedef struct {
+  int32_t steps;       /* Adam steps                                  (3000)  */
+  int32_t batch;       /* rows per step, drawn with replacement       (8192)  */
+  int32_t align_every; /* steps between Procrustes re-alignments      (250)   */
+  int32_t align_rows;  /* rows per instance that fix the rotation     (65536) */
+  float lr;            /* Adam step size                              (1e-3)  */
+  float beta1;         /*                                             (0.9)   */
+  float beta2;         /*                                             (0.999) */
+  float eps;           /*                                             (1e-8)  */
+  uint64_t seed;       /* row sampling                                (0)     */
+} evoc_mlp_train_params_t;
+
+EVOC_API void evoc_mlp_train_params_default(evoc_mlp_train_params_t* p);
+
+/* Create a network with seeded Linear-layer initialisation (uniform in
+ * +-1/sqrt(fan_in)). Free it before destroying its context. */
+EVOC_API int evoc_mlp_create(evoc_ctx_t* ctx, int32_t in_dim, int32_t hidden,
+                             int32_t out_dim, uint64_t seed, evoc_mlp_t** out);
+EVOC_API void evoc_mlp_free(evoc_mlp_t* mlp);
+EVOC_API int64_t evoc_mlp_n_params(const evoc_mlp_t* mlp);
+
+/* FP32 master parameters, packed as above (host arrays of n_params).
+ * evoc_mlp_set_params also resets the Adam state. */
+EVOC_API int evoc_mlp_get_params(const evoc_mlp_t* mlp, float* params);
+EVOC_API int evoc_mlp_set_params(evoc_mlp_t* mlp, const float* params);
+
+/* Predict out (n x out_dim) from points x (n x in_dim): host f32 buffers, or
+ * device buffers with BF16 points (16-byte aligned) and f32 output. */
+EVOC_API int evoc_mlp_predict(evoc_mlp_t* mlp, const float* x, int64_t n, float* out);
+EVOC_API int evoc_mlp_predict_device(evoc_mlp_t* mlp, const uint16_t* d_x_bf16,
+                                     int64_t n, float* d_out);
+
+/* Parity hook: the mean squared error of the prediction against target
+ * (n x out_dim) and its gradient for every parameter (packed as above), for
+ * host points x (n x in_dim, rounded to BF16). Does not update the network. */
+EVOC_API int evoc_mlp_gradients(evoc_mlp_t* mlp, const float* x, const float* target,
+                                int64_t n, float* loss, float* grad);
+
+/* Train on n_instances (points, layout) pairs in device memory: d_x_bf16[i]
+ * (n_rows[i] x in_dim BF16, 16-byte aligned) and d_layouts[i]
+ * (n_rows[i] x out_dim f32, e.g. evoc_embed output). loss_history (host,
+ * params->steps floats, or NULL) receives each step's mean squared error. */
+EVOC_API int evoc_mlp_fit_device(evoc_mlp_t* mlp, int32_t n_instances,
+                                 const uint16_t* const* d_x_bf16,
+                                 const float* const* d_layouts, const int64_t* n_rows,
+                                 const evoc_mlp_train_params_t* params,
+                                 float* loss_history);
+
+/* Round count f32 values to BF16 (nearest even) on the device. */
+EVOC_API int evoc_to_bf16_device(evoc_ctx_t* ctx, const float* d_in, int64_t count,
+                                 uint16_t* d_out);
+
+/* Host only: the orthogonal d x d matrix R maximising trace(R^T M) for a
+ * row-major d x d M (R = U V^T for M = U S V^T), 1 <= d <= 16. With
+ * M = X^T Y for centred X and Y, X R is the rotation of X closest to Y. */
+EVOC_API int evoc_procrustes(const double* m, int32_t d, double* r);
+
 #ifdef __cplusplus
 }
 #endif
