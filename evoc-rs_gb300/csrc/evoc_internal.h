@@ -44,6 +44,7 @@ enum StatusBit : int32_t {
   ST_TOO_MANY_NEG = 8,   // negative count per edge-epoch above the limit
   ST_INTERNAL = 16,      // self-check failed
   ST_CROSS_BLOCK = 32,   // an edge joins two problems of a block-diagonal graph
+  ST_WAIT_TIMEOUT = 64,  // a bounded wait on an mbarrier gave up
 };
 
 // ---------------------------------------------------------------------------

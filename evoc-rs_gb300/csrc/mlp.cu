@@ -251,6 +251,249 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm(GemmArgs g) {
 }
 
 // ---------------------------------------------------------------------------
+// Forward layer on the 5th-generation tensor cores (tcgen05):
+//   out = bf16(gelu(A W^T + bias)), pre = A W^T + bias (optional)
+// A [M][K] and W [N][K] are K-major BF16. One CTA computes a 128 x 256 tile
+// whose FP32 accumulator lives in tensor memory (256 columns x 128 lanes).
+//
+// Mainloop: K advances 64 elements (one 128-byte swizzle atom) per stage
+// through a 4-stage shared-memory ring filled by cp.async in the 128-byte
+// swizzled K-major layout (row r, 16-byte chunk c at r * 128 + ((c ^ (r % 8))
+// * 16), 8-row groups 1024 bytes apart). One thread issues the four
+// K = 16 MMAs of a stage (M = 128, N = 256, kind::f16 with BF16 inputs, FP32
+// accumulation) and commits them to the stage's mbarrier; the ring slot is
+// refilled once that barrier reports the MMAs done. Every wait is bounded
+// (about two seconds of %globaltimer); on expiry the kernel records
+// ST_WAIT_TIMEOUT, drains its own copies, frees its tensor memory and
+// returns without writing.
+//
+// Epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. +31 (its rows) and
+// columns 128 (w / 4) .. +127 with tcgen05.ld, adds the bias, applies GELU
+// and stores BF16 (and the FP32 pre-activation when asked).
+// ---------------------------------------------------------------------------
+constexpr int TC_BM = 128, TC_BN = 256, TC_BK = 64, TC_STAGES = 4, TC_THREADS = 256;
+constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;
+constexpr int TC_B_BYTES = TC_BN * TC_BK * 2;
+constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
+constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024;  // + alignment slack
+constexpr uint32_t TC_TMEM_COLS = 256;
+constexpr unsigned long long TC_WAIT_NS = 2000000000ull;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+// Wait for the completion of the phase with the given parity; false on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t t0) {
+  const uint32_t a = smem_u32(bar);
+  while (true) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (global_ns() - t0 > TC_WAIT_NS) return false;
+  }
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void fence_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart (stride byte offset), descriptor version 1.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) |
+         ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+// Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+constexpr uint32_t tc_idesc(int m, int n) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
+         ((uint32_t)(m >> 4) << 24);
+}
+__device__ __forceinline__ void tc_mma(uint32_t tmem_d, uint64_t da, uint64_t db, uint32_t idesc,
+                                       uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+      ::"r"(tmem_d), "l"(da), "l"(db), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+        "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// One stage: A rows m0.. (128 x 64) and W rows n0.. (256 x 64) at K offset kb.
+__device__ __forceinline__ void tc_load_stage(unsigned char* st, const GemmArgs& g, int m0, int n0,
+                                              int kb, int tid) {
+  unsigned char* sa = st;
+  unsigned char* sb = st + TC_A_BYTES;
+#pragma unroll
+  for (int i = 0; i < (TC_BM * 8) / TC_THREADS; ++i) {
+    const int c = tid + i * TC_THREADS, r = c >> 3, ch = c & 7;
+    const int gm = m0 + r, gk = kb + ch * 8;
+    const bool ok = gm < g.M && gk < g.K;
+    const bf16* src = ok ? g.a + (int64_t)gm * g.lda + gk : g.a;
+    cp_async16(sa + r * 128 + ((ch ^ (r & 7)) << 4), src, ok);
+  }
+#pragma unroll
+  for (int i = 0; i < (TC_BN * 8) / TC_THREADS; ++i) {
+    const int c = tid + i * TC_THREADS, r = c >> 3, ch = c & 7;
+    const int gn = n0 + r, gk = kb + ch * 8;
+    const bool ok = gn < g.N && gk < g.K;
+    const bf16* src = ok ? g.b + (int64_t)gn * g.ldb + gk : g.b;
+    cp_async16(sb + r * 128 + ((ch ^ (r & 7)) << 4), src, ok);
+  }
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_gemm_tc(GemmArgs g, int32_t* __restrict__ status) {
+  extern __shared__ unsigned char tc_raw[];
+  __shared__ __align__(8) uint64_t mbar[TC_STAGES];
+  __shared__ uint32_t tmem_slot;
+  const uint32_t raw = smem_u32(tc_raw);
+  unsigned char* ring = tc_raw + (((raw + 1023u) & ~1023u) - raw);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
+  const int kt = (g.K + TC_BK - 1) / TC_BK;
+  const uint64_t t0 = global_ns();
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_slot)),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < TC_STAGES; ++s) mbar_init(&mbar[s], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+
+#pragma unroll
+  for (int s = 0; s < TC_STAGES - 1; ++s) {
+    if (s < kt) tc_load_stage(ring + s * TC_STAGE_BYTES, g, m0, n0, s * TC_BK, tid);
+    cp_async_commit();
+  }
+  constexpr uint32_t idesc = tc_idesc(TC_BM, TC_BN);
+  bool ok = true;
+  for (int t = 0; t < kt; ++t) {
+    const int st = t % TC_STAGES;
+    cp_async_wait<TC_STAGES - 2>();
+    fence_async_smem();  // this thread's copies -> visible to the tensor cores
+    // barrier + block-wide vote: every thread leaves the loop together
+    if (!__syncthreads_and(ok ? 1 : 0)) {
+      ok = false;
+      break;
+    }
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t a0 = smem_u32(ring + st * TC_STAGE_BYTES);
+      const uint32_t b0 = a0 + TC_A_BYTES;
+#pragma unroll
+      for (int k = 0; k < TC_BK / 16; ++k)
+        tc_mma(tmem, sw128_desc(a0 + k * 32), sw128_desc(b0 + k * 32), idesc,
+               (t > 0 || k > 0) ? 1u : 0u);
+      tc_commit(&mbar[st]);
+    }
+    const int tn = t + TC_STAGES - 1;  // refill the slot read by tile t - 1
+    if (tn < kt) {
+      const int sn = tn % TC_STAGES;
+      if (t >= 1) ok = mbar_wait(&mbar[sn], (uint32_t)(((t - 1) / TC_STAGES) & 1), t0);
+      if (ok) tc_load_stage(ring + sn * TC_STAGE_BYTES, g, m0, n0, tn * TC_BK, tid);
+    }
+    cp_async_commit();
+  }
+  cp_async_wait<0>();
+  if (ok) ok = mbar_wait(&mbar[(kt - 1) % TC_STAGES], (uint32_t)(((kt - 1) / TC_STAGES) & 1), t0);
+  // every thread agrees on success before any tensor-memory read
+  ok = __syncthreads_and(ok ? 1 : 0) != 0;
+  tc_fence_after();
+  if (!ok) {
+    if (tid == 0) atomicOr(status, (int32_t)ST_WAIT_TIMEOUT);
+  } else {
+    const int lg = warp & 3, half = warp >> 2;
+    const int row = m0 + lg * 32 + lane;
+#pragma unroll 1
+    for (int c = 0; c < TC_BN / 2; c += 16) {
+      const int col = half * (TC_BN / 2) + c;
+      uint32_t v[16];
+      tc_ld16(tmem + ((uint32_t)(lg * 32) << 16) + (uint32_t)col, v);
+      const int n = n0 + col;
+      if (row < g.M && n < g.N) {
+        float p[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          p[j] = __uint_as_float(v[j]) + (n + j < g.N ? g.bias[n + j] : 0.0f);
+        const int64_t o = (int64_t)row * g.N + n;
+        if (n + 16 <= g.N) {
+          __align__(16) bf16 hb[16];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) hb[j] = __float2bfloat16_rn(gelu(p[j]));
+          uint4* dst = reinterpret_cast<uint4*>(g.outb + o);
+          dst[0] = reinterpret_cast<const uint4*>(hb)[0];
+          dst[1] = reinterpret_cast<const uint4*>(hb)[1];
+          if (g.pre) {
+            float4* pd = reinterpret_cast<float4*>(g.pre + o);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              pd[j] = make_float4(p[4 * j], p[4 * j + 1], p[4 * j + 2], p[4 * j + 3]);
+          }
+        } else {
+          for (int j = 0; j < 16 && n + j < g.N; ++j) {
+            g.outb[o + j] = __float2bfloat16_rn(gelu(p[j]));
+            if (g.pre) g.pre[o + j] = p[j];
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Output layer (hidden -> out_dim, out_dim <= 16), one warp per row.
 // Inference writes y. Training also forms the MSE gradient
 //   dY = 2 (y - target) / (rows * out_dim),
@@ -472,6 +715,24 @@ void launch_gemm(const GemmArgs& ga, int splits, cudaStream_t s) {
   EVOC_CHECK_LAUNCH();
 }
 
+// Forward layers run on tcgen05 unless EVOC_MLP_GEMM=mma selects the
+// mma.sync kernel (the cross-check of the two paths).
+bool use_tcgen05() {
+  const char* e = std::getenv("EVOC_MLP_GEMM");
+  return !(e && std::strcmp(e, "mma") == 0);
+}
+
+void launch_forward_gemm(const GemmArgs& ga, evoc_ctx* ctx) {
+  if (!use_tcgen05()) {
+    launch_gemm<true, true, EPI_BIAS_GELU>(ga, 1, ctx->stream);
+    return;
+  }
+  EVOC_CUDA(cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
+  dim3 grid((unsigned)((ga.N + TC_BN - 1) / TC_BN), (unsigned)((ga.M + TC_BM - 1) / TC_BM));
+  k_gemm_tc<<<grid, TC_THREADS, TC_SMEM, ctx->stream>>>(ga, ctx->status.get());
+  EVOC_CHECK_LAUNCH();
+}
+
 // Splits of the K dimension so that tiles x splits covers about two waves.
 void choose_splits(int M, int N, int K, int num_sms, int* splits, int* kchunk) {
   const int tiles = ((M + GBM - 1) / GBM) * ((N + GBN - 1) / GBN);
@@ -557,7 +818,7 @@ void forward(const evoc_mlp* net, const bf16* x, int64_t rows, MlpScratch& sc, b
   g1.bias = mp + net->o_b1;
   g1.pre = train ? sc.h1.get() : nullptr;
   g1.outb = sc.a1.get();
-  launch_gemm<true, true, EPI_BIAS_GELU>(g1, 1, s);
+  launch_forward_gemm(g1, net->ctx);
   GemmArgs g2{};
   g2.a = sc.a1.get(); g2.lda = net->hid;
   g2.b = wb + net->o_w2; g2.ldb = net->hid;
@@ -565,7 +826,7 @@ void forward(const evoc_mlp* net, const bf16* x, int64_t rows, MlpScratch& sc, b
   g2.bias = mp + net->o_b2;
   g2.pre = train ? sc.h2.get() : nullptr;
   g2.outb = sc.a2.get();
-  launch_gemm<true, true, EPI_BIAS_GELU>(g2, 1, s);
+  launch_forward_gemm(g2, net->ctx);
   if (!train) {
     k_head<false><<<head_grid_for(net, rows), HEAD_THREADS, head_smem(net), s>>>(
         sc.a2.get(), nullptr, net->hid, net->out, rows, wb + net->o_w3, mp + net->o_b3, y,
@@ -852,7 +1113,7 @@ void to_bf16_device(evoc_ctx* ctx, const float* x, int64_t count, uint16_t* y) {
   EVOC_CHECK_LAUNCH();
 }
 
-constexpr int64_t PREDICT_CHUNK = 65536;
+constexpr int64_t PREDICT_CHUNK = 262144;
 
 void mlp_predict_device(evoc_mlp* net, const uint16_t* x, int64_t n, float* y) {
   if (n == 0) return;
@@ -864,6 +1125,7 @@ void mlp_predict_device(evoc_mlp* net, const uint16_t* x, int64_t n, float* y) {
     const int64_t rows = std::min(chunk, n - r0);
     forward(net, xb + r0 * net->in, rows, sc, false, y + r0 * net->out);
   }
+  check_status(net->ctx, "evoc_mlp_predict_device");
 }
 
 void mlp_predict_host(evoc_mlp* net, const float* x, int64_t n, float* y) {
@@ -882,7 +1144,7 @@ void mlp_predict_host(evoc_mlp* net, const float* x, int64_t n, float* y) {
     EVOC_CUDA(cudaMemcpyAsync(y + r0 * net->out, yd.get(), (size_t)rows * net->out * sizeof(float),
                               cudaMemcpyDeviceToHost, s));
   }
-  EVOC_CUDA(cudaStreamSynchronize(s));
+  check_status(net->ctx, "evoc_mlp_predict");
 }
 
 void mlp_gradients_host(evoc_mlp* net, const float* x, const float* target, int64_t n,
@@ -900,7 +1162,7 @@ void mlp_gradients_host(evoc_mlp* net, const float* x, const float* target, int6
   forward_backward(net, n, sc, ld.get());
   EVOC_CUDA(cudaMemcpyAsync(grad, net->grad.get(), net->grad.bytes(), cudaMemcpyDeviceToHost, s));
   EVOC_CUDA(cudaMemcpyAsync(loss, ld.get(), sizeof(float), cudaMemcpyDeviceToHost, s));
-  EVOC_CUDA(cudaStreamSynchronize(s));
+  check_status(net->ctx, "evoc_mlp_gradients");
 }
 
 // Training on layouts of several instances: every `align_every` steps each
@@ -989,6 +1251,7 @@ void mlp_fit_device(evoc_mlp* net, int32_t m, const uint16_t* const* xs,
       haff[(size_t)d * d + j] = (float)tm[j];
       haff[(size_t)d * d + d + j] = (float)pm[j];
     }
+    check_status(net->ctx, "evoc_mlp_fit_device (alignment)");
     EVOC_CUDA(cudaMemcpyAsync(aff.get(), haff.data(), haff.size() * sizeof(float),
                               cudaMemcpyHostToDevice, s));
     k_affine_rows<<<blocks_for(ns[i], 256), 256, 0, s>>>(layouts[i], ns[i], d, aff.get(),
@@ -1018,7 +1281,7 @@ void mlp_fit_device(evoc_mlp* net, int32_t m, const uint16_t* const* xs,
   if (loss_history && p->steps > 0)
     EVOC_CUDA(cudaMemcpyAsync(loss_history, losses.get(), (size_t)p->steps * sizeof(float),
                               cudaMemcpyDeviceToHost, s));
-  EVOC_CUDA(cudaStreamSynchronize(s));
+  check_status(net->ctx, "evoc_mlp_fit_device");
 }
 
 }  // namespace evoc

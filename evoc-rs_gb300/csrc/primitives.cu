@@ -41,6 +41,8 @@ void check_status(evoc_ctx* ctx, const char* where) {
                 w + ": empty kNN row with local_connectivity > 0");
   if (st & ST_CROSS_BLOCK)
     throw Error(EVOC_ERR_INVALID_INPUT, w + ": an edge joins two problems (graph not block-diagonal)");
+  if (st & ST_WAIT_TIMEOUT)
+    throw Error(EVOC_ERR_INTERNAL, w + ": a tensor-core wait timed out (results discarded)");
   if (st & ST_TOO_MANY_NEG)
     throw Error(EVOC_ERR_UNSUPPORTED,
                 w + ": more than 2^20 negative samples per edge and epoch "

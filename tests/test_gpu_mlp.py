@@ -75,6 +75,33 @@ def test_gradients_match_oracle(ctx, i, h, o, n):
         _close(got[name], want[name], name)
 
 
+@pytest.mark.parametrize("i,h,o,n", DIMS + [(128, 512, 8, 1000)])
+def test_tcgen05_forward_matches_mma_sync(ctx, i, h, o, n, monkeypatch):
+    """The tcgen05 forward layers (default) and the mma.sync kernel give the
+    same prediction up to FP32 accumulation order, and both match the oracle."""
+    net = _net(ctx, i, h, o)
+    x, _ = _data(i, o, n, seed=8)
+    y_tc = net.predict(x)
+    monkeypatch.setenv("EVOC_MLP_GEMM", "mma")
+    y_mma = net.predict(x)
+    monkeypatch.delenv("EVOC_MLP_GEMM")
+    want = M.forward(M.unpack(net.get_params(), i, h, o), x)["y"]
+    _close(y_tc, want, "tcgen05 prediction")
+    _close(y_mma, want, "mma.sync prediction")
+    rel = np.linalg.norm(y_tc - y_mma) / np.linalg.norm(y_mma)
+    assert rel <= 2e-3, rel
+
+
+def test_tcgen05_prediction_over_chunks(ctx):
+    """Rows beyond the 262,144-row prediction chunk and a ragged last tile."""
+    net = _net(ctx, 64, 256, 8)
+    x, _ = _data(64, 8, 262_144 + 1_001, seed=9)
+    y = net.predict(x)
+    for sl in (slice(0, 300), slice(262_000, 262_400), slice(-77, None)):
+        want = M.forward(M.unpack(net.get_params(), 64, 256, 8), x[sl])["y"]
+        _close(y[sl], want, f"rows {sl}")
+
+
 def test_gradients_are_reproducible(ctx):
     net = _net(ctx, 768, 512, 8)
     x, t = _data(768, 8, 1000, seed=6)
@@ -87,7 +114,7 @@ def test_gradients_are_reproducible(ctx):
 def test_predict_device_equals_host(ctx):
     import torch
     net = _net(ctx, 768, 512, 8)
-    x, _ = _data(768, 8, 70_001, seed=7)  # more than one prediction chunk
+    x, _ = _data(768, 8, 70_001, seed=7)  # a ragged last row tile
     want = net.predict(x)
     xd = torch.from_numpy(x).cuda()
     xb = torch.empty(xd.shape, dtype=torch.bfloat16, device="cuda")
