@@ -82,12 +82,28 @@ struct GemmArgs {
   float* outf;         // EPI_PARTIAL: [splits][M][N]
 };
 
+// erf by Abramowitz & Stegun, Handbook of Mathematical Functions, 7.1.26:
+// erf(x) = 1 - (a1 t + a2 t^2 + a3 t^3 + a4 t^4 + a5 t^5) exp(-x^2),
+// t = 1 / (1 + p x) for x >= 0, odd in x; |error| <= 1.5e-7, far below the
+// BF16 rounding that follows every activation. Branch-free: one reciprocal
+// and one exponential.
+__device__ __forceinline__ float erf_as(float x) {
+  const float ax = fabsf(x);
+  const float t = __fdividef(1.0f, fmaf(0.3275911f, ax, 1.0f));
+  float q = fmaf(1.061405429f, t, -1.453152027f);
+  q = fmaf(q, t, 1.421413741f);
+  q = fmaf(q, t, -0.284496736f);
+  q = fmaf(q, t, 0.254829592f);
+  const float r = 1.0f - q * t * __expf(-ax * ax);
+  return copysignf(r, x);
+}
+// GELU(x) = x Phi(x) with the normal CDF Phi(x) = (1 + erf(x / sqrt 2)) / 2.
 __device__ __forceinline__ float gelu(float x) {
-  return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f));
+  return 0.5f * x * (1.0f + erf_as(x * 0.70710678118654752f));
 }
 __device__ __forceinline__ float gelu_grad(float x) {
-  const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
-  const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
+  const float cdf = 0.5f * (1.0f + erf_as(x * 0.70710678118654752f));
+  const float pdf = 0.39894228040143268f * __expf(-0.5f * x * x);
   return cdf + x * pdf;
 }
 
@@ -269,14 +285,35 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm(GemmArgs g) {
 //
 // Epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. +31 (its rows) and
 // columns 128 (w / 4) .. +127 with tcgen05.ld, adds the bias, applies GELU
-// and stores BF16 (and the FP32 pre-activation when asked).
+// and stores BF16 (and the FP32 pre-activation when asked). With HEAD (the
+// second hidden layer at inference) the activations are not stored: each
+// thread multiplies its row's BF16-rounded activations by the matching
+// columns of the output layer W3 (staged in shared memory, read by
+// broadcast), the two column halves are added through shared memory, and the
+// CTA writes one partial output per row and column tile; k_head_combine adds
+// the tiles in order and the bias b3.
+//
+// Two stages of 48 KB let two CTAs share an SM (2 x 256 tensor-memory
+// columns), so one CTA's epilogue overlaps the other's mainloop.
 // ---------------------------------------------------------------------------
-constexpr int TC_BM = 128, TC_BN = 256, TC_BK = 64, TC_STAGES = 4, TC_THREADS = 256;
+constexpr int TC_BM = 128, TC_BN = 256, TC_BK = 64, TC_THREADS = 256;
 constexpr int TC_A_BYTES = TC_BM * TC_BK * 2;
 constexpr int TC_B_BYTES = TC_BN * TC_BK * 2;
 constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
-constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024;  // + alignment slack
 constexpr uint32_t TC_TMEM_COLS = 256;
+
+struct HeadArgs {
+  const bf16* w3;  // [out][N]
+  int out;         // output width (<= 16)
+  int outp;        // W3 row stride in shared memory: 8 or 16 floats
+  float* ypart;    // [column tiles][M][out]
+};
+
+// Dynamic shared memory of k_gemm_tc: the ring, 1 KB of alignment slack and,
+// with the fused head, W3's columns of the tile as f32 [TC_BN][outp].
+inline int tc_smem_bytes(int stages, int head_outp) {
+  return stages * TC_STAGE_BYTES + 1024 + TC_BN * head_outp * (int)sizeof(float);
+}
 constexpr unsigned long long TC_WAIT_NS = 2000000000ull;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -377,13 +414,15 @@ __device__ __forceinline__ void tc_load_stage(unsigned char* st, const GemmArgs&
   }
 }
 
-__global__ void __launch_bounds__(TC_THREADS, 1)
-    k_gemm_tc(GemmArgs g, int32_t* __restrict__ status) {
+template <int STAGES, bool HEAD>
+__global__ void __launch_bounds__(TC_THREADS, (STAGES <= 2 ? 2 : 1))
+    k_gemm_tc(GemmArgs g, HeadArgs h, int32_t* __restrict__ status) {
   extern __shared__ unsigned char tc_raw[];
-  __shared__ __align__(8) uint64_t mbar[TC_STAGES];
+  __shared__ __align__(8) uint64_t mbar[STAGES];
   __shared__ uint32_t tmem_slot;
   const uint32_t raw = smem_u32(tc_raw);
   unsigned char* ring = tc_raw + (((raw + 1023u) & ~1023u) - raw);
+  float* w3s = reinterpret_cast<float*>(ring + STAGES * TC_STAGE_BYTES);  // HEAD: [TC_BN][outp]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
   const int kt = (g.K + TC_BK - 1) / TC_BK;
@@ -397,8 +436,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    for (int s = 0; s < TC_STAGES; ++s) mbar_init(&mbar[s], 1);
+    for (int s = 0; s < STAGES; ++s) mbar_init(&mbar[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (HEAD) {  // W3 columns n0 .. n0 + 255 as f32, zero beyond N and beyond out
+    for (int i = tid; i < TC_BN * h.outp; i += TC_THREADS) {
+      const int col = i / h.outp, o = i - col * h.outp, n = n0 + col;
+      w3s[i] = (n < g.N && o < h.out) ? __bfloat162float(h.w3[(int64_t)o * g.N + n]) : 0.0f;
+    }
   }
   tc_fence_before();
   __syncthreads();
@@ -406,15 +451,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const uint32_t tmem = tmem_slot;
 
 #pragma unroll
-  for (int s = 0; s < TC_STAGES - 1; ++s) {
+  for (int s = 0; s < STAGES - 1; ++s) {
     if (s < kt) tc_load_stage(ring + s * TC_STAGE_BYTES, g, m0, n0, s * TC_BK, tid);
     cp_async_commit();
   }
   constexpr uint32_t idesc = tc_idesc(TC_BM, TC_BN);
   bool ok = true;
   for (int t = 0; t < kt; ++t) {
-    const int st = t % TC_STAGES;
-    cp_async_wait<TC_STAGES - 2>();
+    const int st = t % STAGES;
+    cp_async_wait<STAGES - 2>();
     fence_async_smem();  // this thread's copies -> visible to the tensor cores
     // barrier + block-wide vote: every thread leaves the loop together
     if (!__syncthreads_and(ok ? 1 : 0)) {
@@ -431,16 +476,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                (t > 0 || k > 0) ? 1u : 0u);
       tc_commit(&mbar[st]);
     }
-    const int tn = t + TC_STAGES - 1;  // refill the slot read by tile t - 1
+    const int tn = t + STAGES - 1;  // refill the slot read by tile t - 1
     if (tn < kt) {
-      const int sn = tn % TC_STAGES;
-      if (t >= 1) ok = mbar_wait(&mbar[sn], (uint32_t)(((t - 1) / TC_STAGES) & 1), t0);
+      const int sn = tn % STAGES;
+      if (t >= 1) ok = mbar_wait(&mbar[sn], (uint32_t)(((t - 1) / STAGES) & 1), t0);
       if (ok) tc_load_stage(ring + sn * TC_STAGE_BYTES, g, m0, n0, tn * TC_BK, tid);
     }
     cp_async_commit();
   }
   cp_async_wait<0>();
-  if (ok) ok = mbar_wait(&mbar[(kt - 1) % TC_STAGES], (uint32_t)(((kt - 1) / TC_STAGES) & 1), t0);
+  if (ok) ok = mbar_wait(&mbar[(kt - 1) % STAGES], (uint32_t)(((kt - 1) / STAGES) & 1), t0);
   // every thread agrees on success before any tensor-memory read
   ok = __syncthreads_and(ok ? 1 : 0) != 0;
   tc_fence_after();
@@ -449,37 +494,89 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   } else {
     const int lg = warp & 3, half = warp >> 2;
     const int row = m0 + lg * 32 + lane;
+    float yp[16];
+#pragma unroll
+    for (int o = 0; o < 16; ++o) yp[o] = 0.0f;
 #pragma unroll 1
     for (int c = 0; c < TC_BN / 2; c += 16) {
       const int col = half * (TC_BN / 2) + c;
       uint32_t v[16];
       tc_ld16(tmem + ((uint32_t)(lg * 32) << 16) + (uint32_t)col, v);
       const int n = n0 + col;
-      if (row < g.M && n < g.N) {
-        float p[16];
+      if (n >= g.N) continue;  // uniform across the warp
+      const bool full = n + 16 <= g.N;
+      float p[16];
+      if (full) {
+        const float4* b4 = reinterpret_cast<const float4*>(g.bias + n);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const float4 b = __ldg(b4 + q);
+          p[4 * q] = __uint_as_float(v[4 * q]) + b.x;
+          p[4 * q + 1] = __uint_as_float(v[4 * q + 1]) + b.y;
+          p[4 * q + 2] = __uint_as_float(v[4 * q + 2]) + b.z;
+          p[4 * q + 3] = __uint_as_float(v[4 * q + 3]) + b.w;
+        }
+      } else {
 #pragma unroll
         for (int j = 0; j < 16; ++j)
           p[j] = __uint_as_float(v[j]) + (n + j < g.N ? g.bias[n + j] : 0.0f);
-        const int64_t o = (int64_t)row * g.N + n;
-        if (n + 16 <= g.N) {
-          __align__(16) bf16 hb[16];
+      }
+      __align__(16) bf16 hb[16];
 #pragma unroll
-          for (int j = 0; j < 16; ++j) hb[j] = __float2bfloat16_rn(gelu(p[j]));
+      for (int j = 0; j < 16; ++j) hb[j] = __float2bfloat16_rn(gelu(p[j]));
+      if (HEAD) {
+        // columns beyond N have zero rows in w3s
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const float a = __bfloat162float(hb[j]);
+          const float* w = w3s + (col + j) * h.outp;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            if (4 * q < h.outp) {
+              const float4 wq = *reinterpret_cast<const float4*>(w + 4 * q);
+              yp[4 * q] += a * wq.x;
+              yp[4 * q + 1] += a * wq.y;
+              yp[4 * q + 2] += a * wq.z;
+              yp[4 * q + 3] += a * wq.w;
+            }
+          }
+        }
+      } else if (row < g.M) {
+        const int64_t o = (int64_t)row * g.N + n;
+        if (full) {
           uint4* dst = reinterpret_cast<uint4*>(g.outb + o);
           dst[0] = reinterpret_cast<const uint4*>(hb)[0];
           dst[1] = reinterpret_cast<const uint4*>(hb)[1];
           if (g.pre) {
             float4* pd = reinterpret_cast<float4*>(g.pre + o);
 #pragma unroll
-            for (int j = 0; j < 4; ++j)
-              pd[j] = make_float4(p[4 * j], p[4 * j + 1], p[4 * j + 2], p[4 * j + 3]);
+            for (int q = 0; q < 4; ++q)
+              pd[q] = make_float4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
           }
         } else {
-          for (int j = 0; j < 16 && n + j < g.N; ++j) {
-            g.outb[o + j] = __float2bfloat16_rn(gelu(p[j]));
-            if (g.pre) g.pre[o + j] = p[j];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            if (n + j < g.N) {
+              g.outb[o + j] = hb[j];
+              if (g.pre) g.pre[o + j] = p[j];
+            }
           }
         }
+      }
+    }
+    if (HEAD) {
+      // add the two column halves; the ring is free (all MMAs done, no copies in flight)
+      float* red = reinterpret_cast<float*>(ring);  // [TC_BM][16]
+      if (half == 1) {
+#pragma unroll
+        for (int o = 0; o < 16; ++o) red[(lg * 32 + lane) * 16 + o] = yp[o];
+      }
+      __syncthreads();
+      if (half == 0 && row < g.M) {
+        float* dst = h.ypart + ((int64_t)blockIdx.x * g.M + row) * h.out;
+#pragma unroll
+        for (int o = 0; o < 16; ++o)
+          if (o < h.out) dst[o] = yp[o] + red[(lg * 32 + lane) * 16 + o];
       }
     }
   }
@@ -491,6 +588,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                  "r"(TC_TMEM_COLS)
                  : "memory");
   }
+}
+
+// y[r][o] = sum over column tiles t (in order) of ypart[t][r][o], plus b3[o].
+__global__ void k_head_combine(const float* __restrict__ ypart, int tiles, int64_t rows, int out,
+                               const float* __restrict__ b3, float* __restrict__ y) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= rows * out) return;
+  const int o = (int)(i % out);
+  float s = 0.0f;
+  for (int t = 0; t < tiles; ++t) s += ypart[(int64_t)t * rows * out + i];
+  y[i] = s + b3[o];
 }
 
 // ---------------------------------------------------------------------------
@@ -722,16 +830,44 @@ bool use_tcgen05() {
   return !(e && std::strcmp(e, "mma") == 0);
 }
 
+// Ring depth of k_gemm_tc: 2 stages (two CTAs per SM) unless EVOC_TC_STAGES=4
+// (one CTA per SM, deeper prefetch).
+int tc_stages() {
+  const char* e = std::getenv("EVOC_TC_STAGES");
+  return (e && std::atoi(e) == 4) ? 4 : 2;
+}
+
+template <int S, bool HEAD>
+void launch_tc(const GemmArgs& ga, const HeadArgs& ha, evoc_ctx* ctx) {
+  const int smem = tc_smem_bytes(S, HEAD ? ha.outp : 0);
+  EVOC_CUDA(cudaFuncSetAttribute(k_gemm_tc<S, HEAD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem));
+  dim3 grid((unsigned)((ga.N + TC_BN - 1) / TC_BN), (unsigned)((ga.M + TC_BM - 1) / TC_BM));
+  k_gemm_tc<S, HEAD><<<grid, TC_THREADS, smem, ctx->stream>>>(ga, ha, ctx->status.get());
+  EVOC_CHECK_LAUNCH();
+}
+
 void launch_forward_gemm(const GemmArgs& ga, evoc_ctx* ctx) {
   if (!use_tcgen05()) {
     launch_gemm<true, true, EPI_BIAS_GELU>(ga, 1, ctx->stream);
     return;
   }
-  EVOC_CUDA(cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM));
-  dim3 grid((unsigned)((ga.N + TC_BN - 1) / TC_BN), (unsigned)((ga.M + TC_BM - 1) / TC_BM));
-  k_gemm_tc<<<grid, TC_THREADS, TC_SMEM, ctx->stream>>>(ga, ctx->status.get());
-  EVOC_CHECK_LAUNCH();
+  const HeadArgs none{};
+  if (tc_stages() == 4)
+    launch_tc<4, false>(ga, none, ctx);
+  else
+    launch_tc<2, false>(ga, none, ctx);
 }
+
+// Second hidden layer fused with the output layer (inference on tcgen05).
+void launch_forward_head(const GemmArgs& ga, const HeadArgs& ha, evoc_ctx* ctx) {
+  if (tc_stages() == 4)
+    launch_tc<4, true>(ga, ha, ctx);
+  else
+    launch_tc<2, true>(ga, ha, ctx);
+}
+
+int tc_col_tiles(int n) { return (n + TC_BN - 1) / TC_BN; }
 
 // Splits of the K dimension so that tiles x splits covers about two waves.
 void choose_splits(int M, int N, int K, int num_sms, int* splits, int* kchunk) {
@@ -747,7 +883,7 @@ void choose_splits(int M, int N, int K, int num_sms, int* splits, int* kchunk) {
 // Scratch of one forward/backward pass over `rows` rows.
 struct MlpScratch {
   DevBuf<bf16> x, a1, a2, dh1, dh2;
-  DevBuf<float> h1, h2, target, dy, part, loss_part, loss;
+  DevBuf<float> h1, h2, target, dy, part, loss_part, loss, ypart;
   DevBuf<uint32_t> rows;
   int64_t cap = 0;
   int head_grid = 0;
@@ -790,7 +926,10 @@ void alloc_scratch(const evoc_mlp* net, MlpScratch& sc, int64_t rows, bool train
   sc.a1.alloc((size_t)rows * net->hid, s);
   sc.a2.alloc((size_t)rows * net->hid, s);
   sc.head_grid = head_grid_for(net, rows);
-  if (!train) return;
+  if (!train) {
+    sc.ypart.alloc((size_t)tc_col_tiles(net->hid) * rows * net->out, s);
+    return;
+  }
   int s1, kc1, s2, kc2, s3;
   int64_t rps3;
   const int64_t pf = partial_floats(net, rows, &s1, &kc1, &s2, &kc2, &s3, &rps3);
@@ -826,6 +965,14 @@ void forward(const evoc_mlp* net, const bf16* x, int64_t rows, MlpScratch& sc, b
   g2.bias = mp + net->o_b2;
   g2.pre = train ? sc.h2.get() : nullptr;
   g2.outb = sc.a2.get();
+  if (!train && use_tcgen05()) {
+    const HeadArgs ha{wb + net->o_w3, net->out, net->out <= 8 ? 8 : 16, sc.ypart.get()};
+    launch_forward_head(g2, ha, net->ctx);
+    k_head_combine<<<blocks_for(rows * net->out, 256), 256, 0, s>>>(
+        sc.ypart.get(), tc_col_tiles(net->hid), rows, net->out, mp + net->o_b3, y);
+    EVOC_CHECK_LAUNCH();
+    return;
+  }
   launch_forward_gemm(g2, net->ctx);
   if (!train) {
     k_head<false><<<head_grid_for(net, rows), HEAD_THREADS, head_smem(net), s>>>(
