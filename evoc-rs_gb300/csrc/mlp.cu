@@ -21,7 +21,9 @@
 #include "evoc_internal.h"
 #include "evoc_device.cuh"
 
+#include <cuda.h>
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <cmath>
@@ -414,6 +416,101 @@ __device__ __forceinline__ void tc_load_stage(unsigned char* st, const GemmArgs&
   }
 }
 
+// Epilogue of the tcgen05 forward layers (after the accumulator is complete);
+// every thread of the CTA calls it.
+template <bool HEAD>
+__device__ __forceinline__ void tc_epilogue(const GemmArgs& g, const HeadArgs& h, uint32_t tmem,
+                                            unsigned char* ring, const float* w3s, int m0, int n0,
+                                            int warp, int lane) {
+  const int lg = warp & 3, half = warp >> 2;
+  const int row = m0 + lg * 32 + lane;
+  float yp[16];
+#pragma unroll
+  for (int o = 0; o < 16; ++o) yp[o] = 0.0f;
+#pragma unroll 1
+  for (int c = 0; c < TC_BN / 2; c += 16) {
+    const int col = half * (TC_BN / 2) + c;
+    uint32_t v[16];
+    tc_ld16(tmem + ((uint32_t)(lg * 32) << 16) + (uint32_t)col, v);
+    const int n = n0 + col;
+    if (n >= g.N) continue;  // uniform across the warp
+    const bool full = n + 16 <= g.N;
+    float p[16];
+    if (full) {
+      const float4* b4 = reinterpret_cast<const float4*>(g.bias + n);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const float4 b = __ldg(b4 + q);
+        p[4 * q] = __uint_as_float(v[4 * q]) + b.x;
+        p[4 * q + 1] = __uint_as_float(v[4 * q + 1]) + b.y;
+        p[4 * q + 2] = __uint_as_float(v[4 * q + 2]) + b.z;
+        p[4 * q + 3] = __uint_as_float(v[4 * q + 3]) + b.w;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 16; ++j)
+        p[j] = __uint_as_float(v[j]) + (n + j < g.N ? g.bias[n + j] : 0.0f);
+    }
+    __align__(16) bf16 hb[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) hb[j] = __float2bfloat16_rn(gelu(p[j]));
+    if (HEAD) {
+      // columns beyond N have zero rows in w3s
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const float a = __bfloat162float(hb[j]);
+        const float* w = w3s + (col + j) * h.outp;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          if (4 * q < h.outp) {
+            const float4 wq = *reinterpret_cast<const float4*>(w + 4 * q);
+            yp[4 * q] += a * wq.x;
+            yp[4 * q + 1] += a * wq.y;
+            yp[4 * q + 2] += a * wq.z;
+            yp[4 * q + 3] += a * wq.w;
+          }
+        }
+      }
+    } else if (row < g.M) {
+      const int64_t o = (int64_t)row * g.N + n;
+      if (full) {
+        uint4* dst = reinterpret_cast<uint4*>(g.outb + o);
+        dst[0] = reinterpret_cast<const uint4*>(hb)[0];
+        dst[1] = reinterpret_cast<const uint4*>(hb)[1];
+        if (g.pre) {
+          float4* pd = reinterpret_cast<float4*>(g.pre + o);
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            pd[q] = make_float4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          if (n + j < g.N) {
+            g.outb[o + j] = hb[j];
+            if (g.pre) g.pre[o + j] = p[j];
+          }
+        }
+      }
+    }
+  }
+  if (HEAD) {
+    // add the two column halves; the ring is free (all MMAs done, no copies in flight)
+    float* red = reinterpret_cast<float*>(ring);  // [TC_BM][16]
+    if (half == 1) {
+#pragma unroll
+      for (int o = 0; o < 16; ++o) red[(lg * 32 + lane) * 16 + o] = yp[o];
+    }
+    __syncthreads();
+    if (half == 0 && row < g.M) {
+      float* dst = h.ypart + ((int64_t)blockIdx.x * g.M + row) * h.out;
+#pragma unroll
+      for (int o = 0; o < 16; ++o)
+        if (o < h.out) dst[o] = yp[o] + red[(lg * 32 + lane) * 16 + o];
+    }
+  }
+}
+
 template <int STAGES, bool HEAD>
 __global__ void __launch_bounds__(TC_THREADS, (STAGES <= 2 ? 2 : 1))
     k_gemm_tc(GemmArgs g, HeadArgs h, int32_t* __restrict__ status) {
@@ -492,93 +589,150 @@ __global__ void __launch_bounds__(TC_THREADS, (STAGES <= 2 ? 2 : 1))
   if (!ok) {
     if (tid == 0) atomicOr(status, (int32_t)ST_WAIT_TIMEOUT);
   } else {
-    const int lg = warp & 3, half = warp >> 2;
-    const int row = m0 + lg * 32 + lane;
-    float yp[16];
-#pragma unroll
-    for (int o = 0; o < 16; ++o) yp[o] = 0.0f;
-#pragma unroll 1
-    for (int c = 0; c < TC_BN / 2; c += 16) {
-      const int col = half * (TC_BN / 2) + c;
-      uint32_t v[16];
-      tc_ld16(tmem + ((uint32_t)(lg * 32) << 16) + (uint32_t)col, v);
-      const int n = n0 + col;
-      if (n >= g.N) continue;  // uniform across the warp
-      const bool full = n + 16 <= g.N;
-      float p[16];
-      if (full) {
-        const float4* b4 = reinterpret_cast<const float4*>(g.bias + n);
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const float4 b = __ldg(b4 + q);
-          p[4 * q] = __uint_as_float(v[4 * q]) + b.x;
-          p[4 * q + 1] = __uint_as_float(v[4 * q + 1]) + b.y;
-          p[4 * q + 2] = __uint_as_float(v[4 * q + 2]) + b.z;
-          p[4 * q + 3] = __uint_as_float(v[4 * q + 3]) + b.w;
+    tc_epilogue<HEAD>(g, h, tmem, ring, w3s, m0, n0, warp, lane);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+  }
+}
+
+// ---------------------------------------------------------------------------
+// The same forward layer with its operands moved by the Tensor Memory
+// Accelerator: one thread (lane 0 of warp 0) runs the whole mainloop. For
+// each stage it arms the stage's "full" mbarrier with the stage's byte count
+// and issues two cp.async.bulk.tensor loads (A: 64 x 128 box at (k, m0);
+// W: 64 x 256 box at (k, n0)), which land 128-byte swizzled, rows outside the
+// matrices zero-filled; it waits for "full", issues the four MMAs and commits
+// them to the stage's "empty" mbarrier, and refills a slot once "empty"
+// reports its MMAs done. The other threads only wait for the final commit,
+// then run the shared epilogue. No thread spends issue slots on address
+// arithmetic or barriers during the mainloop.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, "
+      "{%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+template <int STAGES, bool HEAD>
+__global__ void __launch_bounds__(TC_THREADS, (STAGES <= 2 ? 2 : 1))
+    k_gemm_tma(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
+               GemmArgs g, HeadArgs h, int32_t* __restrict__ status) {
+  extern __shared__ unsigned char tc_raw[];
+  __shared__ __align__(8) uint64_t full[STAGES];
+  __shared__ __align__(8) uint64_t empty[STAGES];
+  __shared__ __align__(8) uint64_t done;
+  __shared__ uint32_t tmem_slot;
+  __shared__ int aborted;
+  const uint32_t raw = smem_u32(tc_raw);
+  unsigned char* ring = tc_raw + (((raw + 1023u) & ~1023u) - raw);
+  float* w3s = reinterpret_cast<float*>(ring + STAGES * TC_STAGE_BYTES);  // HEAD: [TC_BN][outp]
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
+  const int kt = (g.K + TC_BK - 1) / TC_BK;
+  const uint64_t t0 = global_ns();
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_slot)),
+                 "r"(TC_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(&done, 1);
+    aborted = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (HEAD) {  // W3 columns n0 .. n0 + 255 as f32, zero beyond N and beyond out
+    for (int i = tid; i < TC_BN * h.outp; i += TC_THREADS) {
+      const int col = i / h.outp, o = i - col * h.outp, n = n0 + col;
+      w3s[i] = (n < g.N && o < h.out) ? __bfloat162float(h.w3[(int64_t)o * g.N + n]) : 0.0f;
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      auto issue = [&](int slot, int tile) {
+        const uint32_t a_dst = smem_u32(ring + slot * TC_STAGE_BYTES);
+        mbar_expect_tx(&full[slot], (uint32_t)TC_STAGE_BYTES);
+        tma_load_2d(a_dst, &map_a, tile * TC_BK, m0, &full[slot]);
+        tma_load_2d(a_dst + TC_A_BYTES, &map_b, tile * TC_BK, n0, &full[slot]);
+      };
+      constexpr uint32_t idesc = tc_idesc(TC_BM, TC_BN);
+      int issued = 0, t = 0;
+      bool okp = true;
+      for (; issued < STAGES && issued < kt; ++issued) issue(issued, issued);
+      for (; t < kt; ++t) {
+        const int st = t % STAGES;
+        if (!mbar_wait(&full[st], (uint32_t)((t / STAGES) & 1), t0)) {
+          okp = false;
+          break;
         }
+        tc_fence_after();
+        const uint32_t a0 = smem_u32(ring + st * TC_STAGE_BYTES);
+        const uint32_t b0 = a0 + TC_A_BYTES;
+#pragma unroll
+        for (int k = 0; k < TC_BK / 16; ++k)
+          tc_mma(tmem, sw128_desc(a0 + k * 32), sw128_desc(b0 + k * 32), idesc,
+                 (t > 0 || k > 0) ? 1u : 0u);
+        tc_commit(&empty[st]);
+        // refill the slot of tile t - 1 once its MMAs are done (tile t's run meanwhile)
+        if (t >= 1 && issued < kt) {
+          const int sn = (t - 1) % STAGES;
+          if (!mbar_wait(&empty[sn], (uint32_t)(((t - 1) / STAGES) & 1), t0)) {
+            okp = false;
+            ++t;  // tile t was consumed
+            break;
+          }
+          issue(sn, issued);
+          ++issued;
+        }
+      }
+      if (okp) {
+        tc_commit(&done);
       } else {
-#pragma unroll
-        for (int j = 0; j < 16; ++j)
-          p[j] = __uint_as_float(v[j]) + (n + j < g.N ? g.bias[n + j] : 0.0f);
-      }
-      __align__(16) bf16 hb[16];
-#pragma unroll
-      for (int j = 0; j < 16; ++j) hb[j] = __float2bfloat16_rn(gelu(p[j]));
-      if (HEAD) {
-        // columns beyond N have zero rows in w3s
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const float a = __bfloat162float(hb[j]);
-          const float* w = w3s + (col + j) * h.outp;
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            if (4 * q < h.outp) {
-              const float4 wq = *reinterpret_cast<const float4*>(w + 4 * q);
-              yp[4 * q] += a * wq.x;
-              yp[4 * q + 1] += a * wq.y;
-              yp[4 * q + 2] += a * wq.z;
-              yp[4 * q + 3] += a * wq.w;
-            }
-          }
-        }
-      } else if (row < g.M) {
-        const int64_t o = (int64_t)row * g.N + n;
-        if (full) {
-          uint4* dst = reinterpret_cast<uint4*>(g.outb + o);
-          dst[0] = reinterpret_cast<const uint4*>(hb)[0];
-          dst[1] = reinterpret_cast<const uint4*>(hb)[1];
-          if (g.pre) {
-            float4* pd = reinterpret_cast<float4*>(g.pre + o);
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-              pd[q] = make_float4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
-          }
-        } else {
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            if (n + j < g.N) {
-              g.outb[o + j] = hb[j];
-              if (g.pre) g.pre[o + j] = p[j];
-            }
-          }
-        }
+        aborted = 1;
+        const uint64_t t1 = global_ns();  // drain the loads still in flight, bounded
+        for (int u = t; u < issued; ++u)
+          if (!mbar_wait(&full[u % STAGES], (uint32_t)((u / STAGES) & 1), t1)) break;
+        mbar_arrive(&done);
       }
     }
-    if (HEAD) {
-      // add the two column halves; the ring is free (all MMAs done, no copies in flight)
-      float* red = reinterpret_cast<float*>(ring);  // [TC_BM][16]
-      if (half == 1) {
-#pragma unroll
-        for (int o = 0; o < 16; ++o) red[(lg * 32 + lane) * 16 + o] = yp[o];
-      }
-      __syncthreads();
-      if (half == 0 && row < g.M) {
-        float* dst = h.ypart + ((int64_t)blockIdx.x * g.M + row) * h.out;
-#pragma unroll
-        for (int o = 0; o < 16; ++o)
-          if (o < h.out) dst[o] = yp[o] + red[(lg * 32 + lane) * 16 + o];
-      }
-    }
+    __syncwarp();
+  }
+  bool ok = mbar_wait(&done, 0u, t0);
+  ok = __syncthreads_and(ok ? 1 : 0) != 0;
+  ok = ok && !aborted;
+  tc_fence_after();
+  if (!ok) {
+    if (tid == 0) atomicOr(status, (int32_t)ST_WAIT_TIMEOUT);
+  } else {
+    tc_epilogue<HEAD>(g, h, tmem, ring, w3s, m0, n0, warp, lane);
   }
   tc_fence_before();
   __syncthreads();
@@ -823,11 +977,52 @@ void launch_gemm(const GemmArgs& ga, int splits, cudaStream_t s) {
   EVOC_CHECK_LAUNCH();
 }
 
-// Forward layers run on tcgen05 unless EVOC_MLP_GEMM=mma selects the
-// mma.sync kernel (the cross-check of the two paths).
-bool use_tcgen05() {
+// Forward-layer kernel: tcgen05 with TMA loads (default); EVOC_MLP_GEMM=cpasync
+// selects tcgen05 with cp.async loads, EVOC_MLP_GEMM=mma the mma.sync kernel
+// (the cross-checks of the three paths).
+enum class FwdPath { kTma, kCpAsync, kMma };
+FwdPath forward_path() {
   const char* e = std::getenv("EVOC_MLP_GEMM");
-  return !(e && std::strcmp(e, "mma") == 0);
+  if (e && std::strcmp(e, "mma") == 0) return FwdPath::kMma;
+  if (e && std::strcmp(e, "cpasync") == 0) return FwdPath::kCpAsync;
+  return FwdPath::kTma;
+}
+bool use_tcgen05() { return forward_path() != FwdPath::kMma; }
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library).
+PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    EVOC_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                               cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !p)
+      throw Error(EVOC_ERR_CUDA, "cuTensorMapEncodeTiled is not available");
+    fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// Tensor map of a K-major BF16 matrix [rows][k] (row stride ld elements):
+// 64 x box_rows boxes, 128-byte swizzle, zero fill outside the matrix.
+CUtensorMap tmap_kmajor(const bf16* base, int64_t rows, int64_t k, int64_t ld, int box_rows) {
+  if ((reinterpret_cast<uintptr_t>(base) & 15) != 0 || (ld * 2) % 16 != 0)
+    throw Error(EVOC_ERR_INVALID_ARGUMENT, "tensor-map operand not 16-byte aligned");
+  CUtensorMap m;
+  const cuuint64_t dims[2] = {(cuuint64_t)k, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)TC_BK, (cuuint32_t)box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = tmap_encoder()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                                    const_cast<bf16*>(base), dims, strides, box, estr,
+                                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS)
+    throw Error(EVOC_ERR_CUDA, "cuTensorMapEncodeTiled failed with code " + std::to_string((int)r));
+  return m;
 }
 
 // Ring depth of k_gemm_tc: 2 stages (two CTAs per SM) unless EVOC_TC_STAGES=4
@@ -840,10 +1035,19 @@ int tc_stages() {
 template <int S, bool HEAD>
 void launch_tc(const GemmArgs& ga, const HeadArgs& ha, evoc_ctx* ctx) {
   const int smem = tc_smem_bytes(S, HEAD ? ha.outp : 0);
-  EVOC_CUDA(cudaFuncSetAttribute(k_gemm_tc<S, HEAD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 smem));
   dim3 grid((unsigned)((ga.N + TC_BN - 1) / TC_BN), (unsigned)((ga.M + TC_BM - 1) / TC_BM));
-  k_gemm_tc<S, HEAD><<<grid, TC_THREADS, smem, ctx->stream>>>(ga, ha, ctx->status.get());
+  if (forward_path() == FwdPath::kCpAsync) {
+    EVOC_CUDA(cudaFuncSetAttribute(k_gemm_tc<S, HEAD>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    k_gemm_tc<S, HEAD><<<grid, TC_THREADS, smem, ctx->stream>>>(ga, ha, ctx->status.get());
+  } else {
+    const CUtensorMap ma = tmap_kmajor(ga.a, ga.M, ga.K, ga.lda, TC_BM);
+    const CUtensorMap mb = tmap_kmajor(ga.b, ga.N, ga.K, ga.ldb, TC_BN);
+    EVOC_CUDA(cudaFuncSetAttribute(k_gemm_tma<S, HEAD>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    k_gemm_tma<S, HEAD><<<grid, TC_THREADS, smem, ctx->stream>>>(ma, mb, ga, ha,
+                                                                 ctx->status.get());
+  }
   EVOC_CHECK_LAUNCH();
 }
 
