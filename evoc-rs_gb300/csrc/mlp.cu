@@ -84,29 +84,27 @@ struct GemmArgs {
   float* outf;         // EPI_PARTIAL: [splits][M][N]
 };
 
-// erf by Abramowitz & Stegun, Handbook of Mathematical Functions, 7.1.26:
-// erf(x) = 1 - (a1 t + a2 t^2 + a3 t^3 + a4 t^4 + a5 t^5) exp(-x^2),
-// t = 1 / (1 + p x) for x >= 0, odd in x; |error| <= 1.5e-7, far below the
-// BF16 rounding that follows every activation. Branch-free: one reciprocal
-// and one exponential.
-__device__ __forceinline__ float erf_as(float x) {
-  const float ax = fabsf(x);
-  const float t = __fdividef(1.0f, fmaf(0.3275911f, ax, 1.0f));
-  float q = fmaf(1.061405429f, t, -1.453152027f);
-  q = fmaf(q, t, 1.421413741f);
-  q = fmaf(q, t, -0.284496736f);
-  q = fmaf(q, t, 0.254829592f);
-  const float r = 1.0f - q * t * __expf(-ax * ax);
-  return copysignf(r, x);
+// GELU in its tanh form (Hendrycks & Gimpel, 2016):
+//   gelu(x) = x/2 (1 + tanh(c (x + a x^3))),  c = sqrt(2/pi), a = 0.044715,
+//   gelu'(x) = (1 + t)/2 + x/2 (1 - t^2) c (1 + 3 a x^2),  t = tanh(c (x + a x^3)),
+// with the hardware tanh (tanh.approx.f32, relative error about 2^-11, below
+// the BF16 rounding that follows every activation).
+__device__ __forceinline__ float tanh_approx(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
 }
-// GELU(x) = x Phi(x) with the normal CDF Phi(x) = (1 + erf(x / sqrt 2)) / 2.
+constexpr float GELU_C = 0.7978845608028654f;
+constexpr float GELU_A = 0.044715f;
 __device__ __forceinline__ float gelu(float x) {
-  return 0.5f * x * (1.0f + erf_as(x * 0.70710678118654752f));
+  const float t = tanh_approx(GELU_C * x * fmaf(GELU_A, x * x, 1.0f));
+  const float hx = 0.5f * x;
+  return fmaf(hx, t, hx);
 }
 __device__ __forceinline__ float gelu_grad(float x) {
-  const float cdf = 0.5f * (1.0f + erf_as(x * 0.70710678118654752f));
-  const float pdf = 0.39894228040143268f * __expf(-0.5f * x * x);
-  return cdf + x * pdf;
+  const float x2 = x * x;
+  const float t = tanh_approx(GELU_C * x * fmaf(GELU_A, x2, 1.0f));
+  return 0.5f * (1.0f + t) + 0.5f * x * (1.0f - t * t) * GELU_C * fmaf(3.0f * GELU_A, x2, 1.0f);
 }
 
 __device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
@@ -288,12 +286,10 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm(GemmArgs g) {
 // Epilogue: warp w reads tensor-memory lanes 32 (w % 4) .. +31 (its rows) and
 // columns 128 (w / 4) .. +127 with tcgen05.ld, adds the bias, applies GELU
 // and stores BF16 (and the FP32 pre-activation when asked). With HEAD (the
-// second hidden layer at inference) the activations are not stored: each
-// thread multiplies its row's BF16-rounded activations by the matching
-// columns of the output layer W3 (staged in shared memory, read by
-// broadcast), the two column halves are added through shared memory, and the
-// CTA writes one partial output per row and column tile; k_head_combine adds
-// the tiles in order and the bias b3.
+// second hidden layer at inference) the activations stay on chip: they feed
+// a second tcgen05 MMA chain against the output layer's weights (see
+// tc_epilogue), the CTA writes one partial output per row and column tile,
+// and k_head_combine adds the tiles in order and the bias b3.
 //
 // Two stages of 48 KB let two CTAs share an SM (2 x 256 tensor-memory
 // columns), so one CTA's epilogue overlaps the other's mainloop.
@@ -307,14 +303,17 @@ constexpr uint32_t TC_TMEM_COLS = 256;
 struct HeadArgs {
   const bf16* w3;  // [out][N]
   int out;         // output width (<= 16)
-  int outp;        // W3 row stride in shared memory: 8 or 16 floats
   float* ypart;    // [column tiles][M][out]
 };
 
-// Dynamic shared memory of k_gemm_tc: the ring, 1 KB of alignment slack and,
-// with the fused head, W3's columns of the tile as f32 [TC_BN][outp].
-inline int tc_smem_bytes(int stages, int head_outp) {
-  return stages * TC_STAGE_BYTES + 1024 + TC_BN * head_outp * (int)sizeof(float);
+// W3's columns of a tile for the head MMA: 16 rows (zero beyond out) x 256
+// columns, K-major BF16 in four 128-byte swizzle atoms of 2 KB.
+constexpr int TC_W3_BYTES = 16 * TC_BN * 2;
+
+// Dynamic shared memory of the tcgen05 kernels: the ring (1024-byte aligned,
+// 1 KB of slack), then with the head the W3 tile, then the tile's bias as f32.
+inline int tc_smem_bytes(int stages, bool head) {
+  return stages * TC_STAGE_BYTES + 1024 + (head ? TC_W3_BYTES : 0) + TC_BN * (int)sizeof(float);
 }
 constexpr unsigned long long TC_WAIT_NS = 2000000000ull;
 
@@ -416,99 +415,137 @@ __device__ __forceinline__ void tc_load_stage(unsigned char* st, const GemmArgs&
   }
 }
 
-// Epilogue of the tcgen05 forward layers (after the accumulator is complete);
-// every thread of the CTA calls it.
+// Per-CTA constants of the tcgen05 forward layers, staged before the
+// mainloop: the bias of the tile's columns (zero beyond N) and, with the head,
+// W3's columns of the tile as the B operand of the head MMA (16 rows, zero
+// beyond out and beyond N; K-major, 128-byte swizzle).
 template <bool HEAD>
-__device__ __forceinline__ void tc_epilogue(const GemmArgs& g, const HeadArgs& h, uint32_t tmem,
-                                            unsigned char* ring, const float* w3s, int m0, int n0,
-                                            int warp, int lane) {
-  const int lg = warp & 3, half = warp >> 2;
-  const int row = m0 + lg * 32 + lane;
-  float yp[16];
-#pragma unroll
-  for (int o = 0; o < 16; ++o) yp[o] = 0.0f;
-#pragma unroll 1
-  for (int c = 0; c < TC_BN / 2; c += 16) {
-    const int col = half * (TC_BN / 2) + c;
-    uint32_t v[16];
-    tc_ld16(tmem + ((uint32_t)(lg * 32) << 16) + (uint32_t)col, v);
-    const int n = n0 + col;
-    if (n >= g.N) continue;  // uniform across the warp
-    const bool full = n + 16 <= g.N;
-    float p[16];
-    if (full) {
-      const float4* b4 = reinterpret_cast<const float4*>(g.bias + n);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const float4 b = __ldg(b4 + q);
-        p[4 * q] = __uint_as_float(v[4 * q]) + b.x;
-        p[4 * q + 1] = __uint_as_float(v[4 * q + 1]) + b.y;
-        p[4 * q + 2] = __uint_as_float(v[4 * q + 2]) + b.z;
-        p[4 * q + 3] = __uint_as_float(v[4 * q + 3]) + b.w;
-      }
-    } else {
-#pragma unroll
-      for (int j = 0; j < 16; ++j)
-        p[j] = __uint_as_float(v[j]) + (n + j < g.N ? g.bias[n + j] : 0.0f);
+__device__ __forceinline__ void tc_stage_constants(const GemmArgs& g, const HeadArgs& h,
+                                                   unsigned char* w3b, float* bias_s, int n0,
+                                                   int tid) {
+  for (int j = tid; j < TC_BN; j += TC_THREADS)
+    bias_s[j] = n0 + j < g.N ? g.bias[n0 + j] : 0.0f;
+  if (HEAD) {
+    for (int i = tid; i < 16 * TC_BN; i += TC_THREADS) {
+      const int o = i / TC_BN, j = i - o * TC_BN, n = n0 + j;
+      const bf16 w = (o < h.out && n < g.N) ? h.w3[(int64_t)o * g.N + n] : __float2bfloat16_rn(0.0f);
+      const int atom = j >> 6, ch = (j & 63) >> 3;
+      *reinterpret_cast<bf16*>(w3b + atom * 2048 + o * 128 + ((ch ^ (o & 7)) << 4) + (j & 7) * 2) = w;
     }
-    __align__(16) bf16 hb[16];
+  }
+}
+
+__device__ __forceinline__ void tc_ld16_nowait(uint32_t taddr, uint32_t* v) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]),
+        "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr));
+}
+
+// Epilogue of the tcgen05 forward layers (after the accumulator is complete);
+// every thread of the CTA calls it. Returns false if the head MMA's bounded
+// wait gave up.
+//
+// Without HEAD: bias + GELU, BF16 activations (and FP32 pre-activations) to
+// global memory. With HEAD: the BF16 activations of the tile are written to
+// the (now idle) ring as a K-major, 128-byte swizzled A operand
+// (4 atoms of 128 rows x 64 columns), and one thread issues the output-layer
+// MMA chain M = 128, N = 16, K = 256 against the staged W3 tile into tensor
+// memory columns 0..15 (all accumulator reads are complete by then); the
+// first four warps read the 16 results per row and store the out_dim partial
+// outputs of this column tile.
+template <bool HEAD>
+__device__ __forceinline__ bool tc_epilogue(const GemmArgs& g, const HeadArgs& h, uint32_t tmem,
+                                            unsigned char* ring, const unsigned char* w3b,
+                                            const float* bias_s, uint64_t* hbar, uint64_t t0,
+                                            int m0, int n0, int warp, int lane) {
+  const int lg = warp & 3, half = warp >> 2;
+  const int r = lg * 32 + lane;  // row within the tile = tensor-memory lane
+  const int row = m0 + r;
+  const uint32_t tl = tmem + ((uint32_t)(lg * 32) << 16);
+#pragma unroll 1
+  for (int c = 0; c < TC_BN / 2; c += 32) {
+    const int col0 = half * (TC_BN / 2) + c;
+    uint32_t v[32];
+    tc_ld16_nowait(tl + (uint32_t)col0, v);
+    tc_ld16_nowait(tl + (uint32_t)col0 + 16u, v + 16);
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-    for (int j = 0; j < 16; ++j) hb[j] = __float2bfloat16_rn(gelu(p[j]));
-    if (HEAD) {
-      // columns beyond N have zero rows in w3s
+    for (int hh = 0; hh < 2; ++hh) {
+      const int col = col0 + 16 * hh, n = n0 + col;
+      float p[16];
+      __align__(16) bf16 hb[16];
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
-        const float a = __bfloat162float(hb[j]);
-        const float* w = w3s + (col + j) * h.outp;
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          if (4 * q < h.outp) {
-            const float4 wq = *reinterpret_cast<const float4*>(w + 4 * q);
-            yp[4 * q] += a * wq.x;
-            yp[4 * q + 1] += a * wq.y;
-            yp[4 * q + 2] += a * wq.z;
-            yp[4 * q + 3] += a * wq.w;
-          }
-        }
+        p[j] = __uint_as_float(v[16 * hh + j]) + bias_s[col + j];
+        hb[j] = __float2bfloat16_rn(gelu(p[j]));
       }
-    } else if (row < g.M) {
-      const int64_t o = (int64_t)row * g.N + n;
-      if (full) {
-        uint4* dst = reinterpret_cast<uint4*>(g.outb + o);
-        dst[0] = reinterpret_cast<const uint4*>(hb)[0];
-        dst[1] = reinterpret_cast<const uint4*>(hb)[1];
-        if (g.pre) {
-          float4* pd = reinterpret_cast<float4*>(g.pre + o);
+      if (HEAD) {
+        // columns beyond N hold gelu(0) = 0
+        const int atom = col >> 6, ch = (col & 63) >> 3;
+        unsigned char* base = ring + atom * 16384 + r * 128;
+        *reinterpret_cast<uint4*>(base + ((ch ^ (r & 7)) << 4)) =
+            reinterpret_cast<const uint4*>(hb)[0];
+        *reinterpret_cast<uint4*>(base + (((ch + 1) ^ (r & 7)) << 4)) =
+            reinterpret_cast<const uint4*>(hb)[1];
+      } else if (row < g.M && n < g.N) {
+        const int64_t o = (int64_t)row * g.N + n;
+        if (n + 16 <= g.N) {
+          uint4* dst = reinterpret_cast<uint4*>(g.outb + o);
+          dst[0] = reinterpret_cast<const uint4*>(hb)[0];
+          dst[1] = reinterpret_cast<const uint4*>(hb)[1];
+          if (g.pre) {
+            float4* pd = reinterpret_cast<float4*>(g.pre + o);
 #pragma unroll
-          for (int q = 0; q < 4; ++q)
-            pd[q] = make_float4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
-        }
-      } else {
+            for (int q = 0; q < 4; ++q)
+              pd[q] = make_float4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
+          }
+        } else {
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          if (n + j < g.N) {
-            g.outb[o + j] = hb[j];
-            if (g.pre) g.pre[o + j] = p[j];
+          for (int j = 0; j < 16; ++j) {
+            if (n + j < g.N) {
+              g.outb[o + j] = hb[j];
+              if (g.pre) g.pre[o + j] = p[j];
+            }
           }
         }
       }
     }
   }
-  if (HEAD) {
-    // add the two column halves; the ring is free (all MMAs done, no copies in flight)
-    float* red = reinterpret_cast<float*>(ring);  // [TC_BM][16]
-    if (half == 1) {
+  if (!HEAD) return true;
+  fence_async_smem();  // the activation tile -> visible to the tensor cores
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tc_fence_after();
+    const uint32_t a0 = smem_u32(ring), b0 = smem_u32(w3b);
+    constexpr uint32_t idesc16 = tc_idesc(TC_BM, 16);
 #pragma unroll
-      for (int o = 0; o < 16; ++o) red[(lg * 32 + lane) * 16 + o] = yp[o];
+    for (int k = 0; k < TC_BN / 16; ++k) {
+      const int atom = k >> 2, off = (k & 3) * 32;
+      tc_mma(tmem, sw128_desc(a0 + atom * 16384 + off), sw128_desc(b0 + atom * 2048 + off),
+             idesc16, k > 0 ? 1u : 0u);
     }
-    __syncthreads();
-    if (half == 0 && row < g.M) {
+    tc_commit(hbar);
+  }
+  bool hok = mbar_wait(hbar, 0u, t0);
+  hok = __syncthreads_and(hok ? 1 : 0) != 0;
+  tc_fence_after();
+  if (!hok) return false;
+  if (half == 0) {
+    uint32_t y[16];
+    tc_ld16(tl, y);
+    if (row < g.M) {
       float* dst = h.ypart + ((int64_t)blockIdx.x * g.M + row) * h.out;
 #pragma unroll
       for (int o = 0; o < 16; ++o)
-        if (o < h.out) dst[o] = yp[o] + red[(lg * 32 + lane) * 16 + o];
+        if (o < h.out) dst[o] = __uint_as_float(y[o]);
     }
   }
+  return true;
 }
 
 template <int STAGES, bool HEAD>
@@ -516,10 +553,12 @@ __global__ void __launch_bounds__(TC_THREADS, (STAGES <= 2 ? 2 : 1))
     k_gemm_tc(GemmArgs g, HeadArgs h, int32_t* __restrict__ status) {
   extern __shared__ unsigned char tc_raw[];
   __shared__ __align__(8) uint64_t mbar[STAGES];
+  __shared__ __align__(8) uint64_t hbar;
   __shared__ uint32_t tmem_slot;
   const uint32_t raw = smem_u32(tc_raw);
   unsigned char* ring = tc_raw + (((raw + 1023u) & ~1023u) - raw);
-  float* w3s = reinterpret_cast<float*>(ring + STAGES * TC_STAGE_BYTES);  // HEAD: [TC_BN][outp]
+  unsigned char* w3b = ring + STAGES * TC_STAGE_BYTES;  // HEAD: W3 tile
+  float* bias_s = reinterpret_cast<float*>(w3b + (HEAD ? TC_W3_BYTES : 0));
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
   const int kt = (g.K + TC_BK - 1) / TC_BK;
@@ -534,14 +573,10 @@ __global__ void __launch_bounds__(TC_THREADS, (STAGES <= 2 ? 2 : 1))
   }
   if (tid == 0) {
     for (int s = 0; s < STAGES; ++s) mbar_init(&mbar[s], 1);
+    mbar_init(&hbar, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (HEAD) {  // W3 columns n0 .. n0 + 255 as f32, zero beyond N and beyond out
-    for (int i = tid; i < TC_BN * h.outp; i += TC_THREADS) {
-      const int col = i / h.outp, o = i - col * h.outp, n = n0 + col;
-      w3s[i] = (n < g.N && o < h.out) ? __bfloat162float(h.w3[(int64_t)o * g.N + n]) : 0.0f;
-    }
-  }
+  tc_stage_constants<HEAD>(g, h, w3b, bias_s, n0, tid);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -588,8 +623,8 @@ __global__ void __launch_bounds__(TC_THREADS, (STAGES <= 2 ? 2 : 1))
   tc_fence_after();
   if (!ok) {
     if (tid == 0) atomicOr(status, (int32_t)ST_WAIT_TIMEOUT);
-  } else {
-    tc_epilogue<HEAD>(g, h, tmem, ring, w3s, m0, n0, warp, lane);
+  } else if (!tc_epilogue<HEAD>(g, h, tmem, ring, w3b, bias_s, &hbar, t0, m0, n0, warp, lane)) {
+    if (tid == 0) atomicOr(status, (int32_t)ST_WAIT_TIMEOUT);
   }
   tc_fence_before();
   __syncthreads();
@@ -638,11 +673,13 @@ __global__ void __launch_bounds__(TC_THREADS, (STAGES <= 2 ? 2 : 1))
   __shared__ __align__(8) uint64_t full[STAGES];
   __shared__ __align__(8) uint64_t empty[STAGES];
   __shared__ __align__(8) uint64_t done;
+  __shared__ __align__(8) uint64_t hbar;
   __shared__ uint32_t tmem_slot;
   __shared__ int aborted;
   const uint32_t raw = smem_u32(tc_raw);
   unsigned char* ring = tc_raw + (((raw + 1023u) & ~1023u) - raw);
-  float* w3s = reinterpret_cast<float*>(ring + STAGES * TC_STAGE_BYTES);  // HEAD: [TC_BN][outp]
+  unsigned char* w3b = ring + STAGES * TC_STAGE_BYTES;  // HEAD: W3 tile
+  float* bias_s = reinterpret_cast<float*>(w3b + (HEAD ? TC_W3_BYTES : 0));
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
   const int kt = (g.K + TC_BK - 1) / TC_BK;
@@ -661,15 +698,11 @@ __global__ void __launch_bounds__(TC_THREADS, (STAGES <= 2 ? 2 : 1))
       mbar_init(&empty[s], 1);
     }
     mbar_init(&done, 1);
+    mbar_init(&hbar, 1);
     aborted = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (HEAD) {  // W3 columns n0 .. n0 + 255 as f32, zero beyond N and beyond out
-    for (int i = tid; i < TC_BN * h.outp; i += TC_THREADS) {
-      const int col = i / h.outp, o = i - col * h.outp, n = n0 + col;
-      w3s[i] = (n < g.N && o < h.out) ? __bfloat162float(h.w3[(int64_t)o * g.N + n]) : 0.0f;
-    }
-  }
+  tc_stage_constants<HEAD>(g, h, w3b, bias_s, n0, tid);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -731,8 +764,8 @@ __global__ void __launch_bounds__(TC_THREADS, (STAGES <= 2 ? 2 : 1))
   tc_fence_after();
   if (!ok) {
     if (tid == 0) atomicOr(status, (int32_t)ST_WAIT_TIMEOUT);
-  } else {
-    tc_epilogue<HEAD>(g, h, tmem, ring, w3s, m0, n0, warp, lane);
+  } else if (!tc_epilogue<HEAD>(g, h, tmem, ring, w3b, bias_s, &hbar, t0, m0, n0, warp, lane)) {
+    if (tid == 0) atomicOr(status, (int32_t)ST_WAIT_TIMEOUT);
   }
   tc_fence_before();
   __syncthreads();
@@ -1034,7 +1067,7 @@ int tc_stages() {
 
 template <int S, bool HEAD>
 void launch_tc(const GemmArgs& ga, const HeadArgs& ha, evoc_ctx* ctx) {
-  const int smem = tc_smem_bytes(S, HEAD ? ha.outp : 0);
+  const int smem = tc_smem_bytes(S, HEAD);
   dim3 grid((unsigned)((ga.N + TC_BN - 1) / TC_BN), (unsigned)((ga.M + TC_BM - 1) / TC_BM));
   if (forward_path() == FwdPath::kCpAsync) {
     EVOC_CUDA(cudaFuncSetAttribute(k_gemm_tc<S, HEAD>,
@@ -1170,7 +1203,7 @@ void forward(const evoc_mlp* net, const bf16* x, int64_t rows, MlpScratch& sc, b
   g2.pre = train ? sc.h2.get() : nullptr;
   g2.outb = sc.a2.get();
   if (!train && use_tcgen05()) {
-    const HeadArgs ha{wb + net->o_w3, net->out, net->out <= 8 ? 8 : 16, sc.ypart.get()};
+    const HeadArgs ha{wb + net->o_w3, net->out, sc.ypart.get()};
     launch_forward_head(g2, ha, net->ctx);
     k_head_combine<<<blocks_for(rows * net->out, 256), 256, 0, s>>>(
         sc.ypart.get(), tc_col_tiles(net->hid), rows, net->out, mp + net->o_b3, y);

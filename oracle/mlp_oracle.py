@@ -9,8 +9,8 @@ the warm-start form that sits beside the plain method. The oracle restates
 the published algorithm the library implements:
 
   * a multilayer perceptron  x -> GELU(x W1^T + b1) -> GELU(. W2^T + b2)
-    -> . W3^T + b3, GELU(x) = x * Phi(x) with the exact normal CDF
-    (Hendrycks & Gimpel, 2016);
+    -> . W3^T + b3, GELU in its tanh form x/2 (1 + tanh(sqrt(2/pi)
+    (x + 0.044715 x^3))) (Hendrycks & Gimpel, 2016);
   * mean squared error L = mean((y - t)^2) over all n * out_dim entries;
   * its gradients by back-propagation;
   * Adam with bias correction (Kingma & Ba, 2015);
@@ -30,10 +30,6 @@ import math
 
 import numpy as np
 
-_SQRT_HALF = 1.0 / math.sqrt(2.0)
-_INV_SQRT_2PI = 1.0 / math.sqrt(2.0 * math.pi)
-_erf = np.vectorize(math.erf, otypes=[np.float64])
-
 
 def bf16(x) -> np.ndarray:
     """Round float32 values to the nearest BF16 (ties to even), as float64."""
@@ -43,12 +39,18 @@ def bf16(x) -> np.ndarray:
     return u.astype(np.uint32).view(np.float32).astype(np.float64)
 
 
+_GELU_C = math.sqrt(2.0 / math.pi)
+_GELU_A = 0.044715
+
+
 def gelu(x: np.ndarray) -> np.ndarray:
-    return 0.5 * x * (1.0 + _erf(x * _SQRT_HALF))
+    """GELU, tanh form: x/2 (1 + tanh(c (x + a x^3)))."""
+    return 0.5 * x * (1.0 + np.tanh(_GELU_C * (x + _GELU_A * x ** 3)))
 
 
 def gelu_grad(x: np.ndarray) -> np.ndarray:
-    return 0.5 * (1.0 + _erf(x * _SQRT_HALF)) + x * _INV_SQRT_2PI * np.exp(-0.5 * x * x)
+    t = np.tanh(_GELU_C * (x + _GELU_A * x ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * x * (1.0 - t * t) * _GELU_C * (1.0 + 3.0 * _GELU_A * x * x)
 
 
 def unpack(flat: np.ndarray, in_dim: int, hidden: int, out_dim: int) -> dict:
