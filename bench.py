@@ -69,7 +69,10 @@ WORKLOADS = {
     # n = points of the fresh evaluation instance
     "warm_start_c5": dict(n=1_000_000, d=768, k=30, dim=8, seed=777, hidden=512,
                           train_n=2_000_000, train_instances=20, train_seed=100),
+    # the warm-start network's forward pass alone (n = rows)
+    "mlp_forward": dict(n=1_000_000, d=768, k=0, dim=8, seed=777, hidden=512),
 }
+METRIC_MLP = "warm-start network forward TFLOP/s (768->512->512->8, BF16 tensor cores)"
 METRIC_C4 = "edge-updates/s, 256 batched problems (EVoC node embedding, 50 epochs)"
 METRIC_C5 = ("time-to-embedding speed-up at 1M pts, learned warm start vs plain "
              "(equal trustworthiness@15 and kNN label accuracy)")
@@ -539,7 +542,7 @@ def run_warm_start(args) -> dict:
         if (ROOT / "MEASURED_PEAKS.json").exists() else {"bf16_tflops": 1900.0}
     peak = float(pk["bf16_tflops"])
     value = (t_plain / (chosen["warm_ms"] / 1e3)) if chosen else None
-    chunks = (n + 65535) // 65536
+    chunks = (n + 262143) // 262144
     return {
         "metric": METRIC_C5, "value": value, "unit": "x", "n_gpus": 1,
         "steps": args.c5_reps, "warmup": 0, "ms_per_step": chosen["warm_ms"] if chosen else None,
@@ -565,13 +568,80 @@ def run_warm_start(args) -> dict:
         "warm": rows, "chosen_epochs": chosen["epochs"] if chosen else None,
         "e2e": None,
         "gpu_launches": int(3 * chunks * (1 + args.c5_reps) + (chosen["epochs"] + 2 if chosen else 0)),
-        "gpu_launches_note": "network forward (3 per 65,536-row chunk) and epoch loop of the "
+        "gpu_launches_note": "network forward (3 per 262,144-row chunk) and epoch loop of the "
                              "chosen warm run; fuzzy-set and set-up kernels not counted",
-        "roofline": {"bound": "tensor", "kernel": "k_gemm (network forward, 1M rows)",
+        "roofline": {"bound": "tensor", "kernel": "k_gemm_tma (network forward, 1M rows)",
                      "achieved": round(tflops, 1), "peak": peak, "unit": "TFLOP/s",
                      "frac": round(tflops / peak, 4), "traffic": None,
                      "peak_src": "measured (cuBLAS bf16 burst)" if "hbm_gbs" in pk else "fallback",
                      "predict_ms": round(predict_ms, 3)},
+        "clocks": clk.summary(),
+    }
+
+
+def run_mlp_forward(args) -> dict:
+    """The network's forward pass (two tcgen05 GEMM launches with TMA loads,
+    the output layer fused into the second, and one combine launch per 262,144
+    rows) over random unit-norm points, device-resident (value) and through
+    the host-buffer C ABI (e2e)."""
+    import torch
+    import evoc_gb300 as E
+    torch.cuda.init()
+    cfg = WORKLOADS["mlp_forward"]
+    n = args.n or cfg["n"]
+    d, hid, dim = cfg["d"], cfg["hidden"], cfg["dim"]
+    ctx = E.Context(0)
+    net = ctx.mlp(d, hid, dim, seed=1)
+    g = torch.Generator(device="cuda").manual_seed(cfg["seed"])
+    x = torch.randn(n, d, device="cuda", generator=g)
+    x /= x.norm(dim=1, keepdim=True)
+    xb = torch.empty(n, d, dtype=torch.bfloat16, device="cuda")
+    torch.cuda.synchronize()
+    ctx.to_bf16_device(x.data_ptr(), n * d, xb.data_ptr())
+    out = torch.empty(n, dim, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    flops = 2.0 * n * (d * hid + hid * hid + hid * dim)
+    for _ in range(args.warmup):
+        net.predict_device(xb.data_ptr(), n, out.data_ptr())
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler() as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            net.predict_device(xb.data_ptr(), n, out.data_ptr())
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        xh = torch.empty(n, d, dtype=torch.float32, pin_memory=True)
+        xh.copy_(x)
+        yh = np.empty((n, dim), dtype=np.float32)
+        xn = xh.numpy()
+        e2e_steps = max(1, min(args.steps, args.e2e_steps))
+        t = time.perf_counter()
+        for _ in range(e2e_steps):
+            yh = net.predict(xn)
+        e2e_ms = (time.perf_counter() - t) / e2e_steps * 1e3
+    pk = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) \
+        if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(pk.get("bf16_tflops", 1900.0))
+    tflops = flops / (ms / 1e3) / 1e12
+    chunks = (n + 262143) // 262144
+    return {
+        "metric": METRIC_MLP, "value": tflops, "unit": "TFLOP/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16 (f32 accumulate)", "data": "synthetic (seeded unit-norm points)",
+        "config": {"workload": "mlp_forward", "n": n, "mlp": f"{d}->{hid}->{hid}->{dim} GELU",
+                   "flop_per_step": flops,
+                   "l2": "inputs larger than L2 (1.5 GB of BF16 points)"},
+        "e2e": {"value": flops / (e2e_ms / 1e3) / 1e12, "unit": "TFLOP/s",
+                "ms_per_step": round(e2e_ms, 3), "h2d_bytes_per_step": int(n * d * 4),
+                "d2h_bytes_per_step": int(n * dim * 4)},
+        "gpu_launches": int(args.steps * 3 * chunks),
+        "roofline": {"bound": "tensor", "kernel": "k_gemm_tma", "achieved": round(tflops, 1),
+                     "peak": peak, "unit": "TFLOP/s", "frac": round(tflops / peak, 4),
+                     "traffic": None,
+                     "peak_src": "measured (cuBLAS bf16 burst)" if pk else "fallback"},
         "clocks": clk.summary(),
     }
 
@@ -656,6 +726,9 @@ def main() -> None:
         return
     if args.workload == "warm_start_c5":
         print(json.dumps(run_warm_start(args)))
+        return
+    if args.workload == "mlp_forward":
+        print(json.dumps(run_mlp_forward(args)))
         return
     print(json.dumps(run_batched(args) if args.workload == "batch_c4" else run_ours(args)))
 
