@@ -38,7 +38,8 @@ struct evoc_mlp {
   int64_t n_params = 0;
   int64_t o_w1 = 0, o_b1 = 0, o_w2 = 0, o_b2 = 0, o_w3 = 0, o_b3 = 0;
   evoc::DevBuf<float> master, adam_m, adam_v, grad;
-  evoc::DevBuf<bf16> wb;  // BF16 copy of `master`, same packing
+  evoc::DevBuf<bf16> wb;   // BF16 copy of `master`, same packing
+  evoc::DevBuf<bf16> w2t;  // BF16 W2 transposed ([in][out]), the K-major B operand of dH2 W2
   int64_t adam_steps = 0;
 };
 
@@ -300,6 +301,14 @@ constexpr int TC_B_BYTES = TC_BN * TC_BK * 2;
 constexpr int TC_STAGE_BYTES = TC_A_BYTES + TC_B_BYTES;
 constexpr uint32_t TC_TMEM_COLS = 256;
 
+// Epilogues of the tcgen05 kernels.
+enum TcEpi : int {
+  TC_GELU = 0,  // outb = bf16(gelu(acc + bias)), pre = acc + bias (optional)
+  TC_HEAD = 1,  // TC_GELU kept on chip, then the output layer (partials to ypart)
+  TC_GRAD = 2,  // outb = bf16(acc * gelu'(pre))
+  TC_F32 = 3,   // outf[split][m][n] = acc
+};
+
 struct HeadArgs {
   const bf16* w3;  // [out][N]
   int out;         // output width (<= 16)
@@ -424,7 +433,7 @@ __device__ __forceinline__ void tc_stage_constants(const GemmArgs& g, const Head
                                                    unsigned char* w3b, float* bias_s, int n0,
                                                    int tid) {
   for (int j = tid; j < TC_BN; j += TC_THREADS)
-    bias_s[j] = n0 + j < g.N ? g.bias[n0 + j] : 0.0f;
+    bias_s[j] = (g.bias && n0 + j < g.N) ? g.bias[n0 + j] : 0.0f;
   if (HEAD) {
     for (int i = tid; i < 16 * TC_BN; i += TC_THREADS) {
       const int o = i / TC_BN, j = i - o * TC_BN, n = n0 + j;
@@ -457,11 +466,12 @@ __device__ __forceinline__ void tc_ld16_nowait(uint32_t taddr, uint32_t* v) {
 // memory columns 0..15 (all accumulator reads are complete by then); the
 // first four warps read the 16 results per row and store the out_dim partial
 // outputs of this column tile.
-template <bool HEAD>
+template <int EPI>
 __device__ __forceinline__ bool tc_epilogue(const GemmArgs& g, const HeadArgs& h, uint32_t tmem,
                                             unsigned char* ring, const unsigned char* w3b,
                                             const float* bias_s, uint64_t* hbar, uint64_t t0,
                                             int m0, int n0, int warp, int lane) {
+  constexpr bool HEAD = EPI == TC_HEAD;
   const int lg = warp & 3, half = warp >> 2;
   const int r = lg * 32 + lane;  // row within the tile = tensor-memory lane
   const int row = m0 + r;
@@ -476,46 +486,88 @@ __device__ __forceinline__ bool tc_epilogue(const GemmArgs& g, const HeadArgs& h
 #pragma unroll
     for (int hh = 0; hh < 2; ++hh) {
       const int col = col0 + 16 * hh, n = n0 + col;
-      float p[16];
-      __align__(16) bf16 hb[16];
-#pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        p[j] = __uint_as_float(v[16 * hh + j]) + bias_s[col + j];
-        hb[j] = __float2bfloat16_rn(gelu(p[j]));
-      }
-      if (HEAD) {
-        // columns beyond N hold gelu(0) = 0
-        const int atom = col >> 6, ch = (col & 63) >> 3;
-        unsigned char* base = ring + atom * 16384 + r * 128;
-        *reinterpret_cast<uint4*>(base + ((ch ^ (r & 7)) << 4)) =
-            reinterpret_cast<const uint4*>(hb)[0];
-        *reinterpret_cast<uint4*>(base + (((ch + 1) ^ (r & 7)) << 4)) =
-            reinterpret_cast<const uint4*>(hb)[1];
-      } else if (row < g.M && n < g.N) {
+      if constexpr (EPI == TC_F32 || EPI == TC_GRAD) {
+        if (row >= g.M || n >= g.N) continue;
         const int64_t o = (int64_t)row * g.N + n;
-        if (n + 16 <= g.N) {
-          uint4* dst = reinterpret_cast<uint4*>(g.outb + o);
-          dst[0] = reinterpret_cast<const uint4*>(hb)[0];
-          dst[1] = reinterpret_cast<const uint4*>(hb)[1];
-          if (g.pre) {
-            float4* pd = reinterpret_cast<float4*>(g.pre + o);
+        const bool full = n + 16 <= g.N;
+        if (EPI == TC_F32) {
+          float* dst = g.outf + (int64_t)blockIdx.z * g.M * g.N + o;
+          if (full) {
 #pragma unroll
             for (int q = 0; q < 4; ++q)
-              pd[q] = make_float4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
+              reinterpret_cast<float4*>(dst)[q] =
+                  make_float4(__uint_as_float(v[16 * hh + 4 * q]), __uint_as_float(v[16 * hh + 4 * q + 1]),
+                              __uint_as_float(v[16 * hh + 4 * q + 2]), __uint_as_float(v[16 * hh + 4 * q + 3]));
+          } else {
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+              if (n + j < g.N) dst[j] = __uint_as_float(v[16 * hh + j]);
           }
         } else {
+          __align__(16) bf16 gb[16];
+          if (full) {
+            const float4* pr = reinterpret_cast<const float4*>(g.pre + o);
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            if (n + j < g.N) {
-              g.outb[o + j] = hb[j];
-              if (g.pre) g.pre[o + j] = p[j];
+            for (int q = 0; q < 4; ++q) {
+              const float4 pq = pr[q];
+              gb[4 * q] = __float2bfloat16_rn(__uint_as_float(v[16 * hh + 4 * q]) * gelu_grad(pq.x));
+              gb[4 * q + 1] = __float2bfloat16_rn(__uint_as_float(v[16 * hh + 4 * q + 1]) * gelu_grad(pq.y));
+              gb[4 * q + 2] = __float2bfloat16_rn(__uint_as_float(v[16 * hh + 4 * q + 2]) * gelu_grad(pq.z));
+              gb[4 * q + 3] = __float2bfloat16_rn(__uint_as_float(v[16 * hh + 4 * q + 3]) * gelu_grad(pq.w));
+            }
+            uint4* dst = reinterpret_cast<uint4*>(g.outb + o);
+            dst[0] = reinterpret_cast<const uint4*>(gb)[0];
+            dst[1] = reinterpret_cast<const uint4*>(gb)[1];
+          } else {
+#pragma unroll
+            for (int j = 0; j < 16; ++j)
+              if (n + j < g.N)
+                g.outb[o + j] =
+                    __float2bfloat16_rn(__uint_as_float(v[16 * hh + j]) * gelu_grad(g.pre[o + j]));
+          }
+        }
+      } else {
+        float p[16];
+        __align__(16) bf16 hb[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          p[j] = __uint_as_float(v[16 * hh + j]) + bias_s[col + j];
+          hb[j] = __float2bfloat16_rn(gelu(p[j]));
+        }
+        if (HEAD) {
+          // columns beyond N hold gelu(0) = 0
+          const int atom = col >> 6, ch = (col & 63) >> 3;
+          unsigned char* base = ring + atom * 16384 + r * 128;
+          *reinterpret_cast<uint4*>(base + ((ch ^ (r & 7)) << 4)) =
+              reinterpret_cast<const uint4*>(hb)[0];
+          *reinterpret_cast<uint4*>(base + (((ch + 1) ^ (r & 7)) << 4)) =
+              reinterpret_cast<const uint4*>(hb)[1];
+        } else if (row < g.M && n < g.N) {
+          const int64_t o = (int64_t)row * g.N + n;
+          if (n + 16 <= g.N) {
+            uint4* dst = reinterpret_cast<uint4*>(g.outb + o);
+            dst[0] = reinterpret_cast<const uint4*>(hb)[0];
+            dst[1] = reinterpret_cast<const uint4*>(hb)[1];
+            if (g.pre) {
+              float4* pd = reinterpret_cast<float4*>(g.pre + o);
+#pragma unroll
+              for (int q = 0; q < 4; ++q)
+                pd[q] = make_float4(p[4 * q], p[4 * q + 1], p[4 * q + 2], p[4 * q + 3]);
+            }
+          } else {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              if (n + j < g.N) {
+                g.outb[o + j] = hb[j];
+                if (g.pre) g.pre[o + j] = p[j];
+              }
             }
           }
         }
       }
     }
   }
-  if (!HEAD) return true;
+  if constexpr (!HEAD) return true;
   fence_async_smem();  // the activation tile -> visible to the tensor cores
   tc_fence_before();
   __syncthreads();
@@ -623,7 +675,8 @@ __global__ void __launch_bounds__(TC_THREADS, (STAGES <= 2 ? 2 : 1))
   tc_fence_after();
   if (!ok) {
     if (tid == 0) atomicOr(status, (int32_t)ST_WAIT_TIMEOUT);
-  } else if (!tc_epilogue<HEAD>(g, h, tmem, ring, w3b, bias_s, &hbar, t0, m0, n0, warp, lane)) {
+  } else if (!tc_epilogue<HEAD ? TC_HEAD : TC_GELU>(g, h, tmem, ring, w3b, bias_s, &hbar, t0,
+                                                  m0, n0, warp, lane)) {
     if (tid == 0) atomicOr(status, (int32_t)ST_WAIT_TIMEOUT);
   }
   tc_fence_before();
@@ -665,10 +718,11 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
-template <int STAGES, bool HEAD>
+template <int STAGES, int EPI>
 __global__ void __launch_bounds__(TC_THREADS, (STAGES <= 2 ? 2 : 1))
     k_gemm_tma(const __grid_constant__ CUtensorMap map_a, const __grid_constant__ CUtensorMap map_b,
                GemmArgs g, HeadArgs h, int32_t* __restrict__ status) {
+  constexpr bool HEAD = EPI == TC_HEAD;
   extern __shared__ unsigned char tc_raw[];
   __shared__ __align__(8) uint64_t full[STAGES];
   __shared__ __align__(8) uint64_t empty[STAGES];
@@ -682,7 +736,10 @@ __global__ void __launch_bounds__(TC_THREADS, (STAGES <= 2 ? 2 : 1))
   float* bias_s = reinterpret_cast<float*>(w3b + (HEAD ? TC_W3_BYTES : 0));
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int m0 = blockIdx.y * TC_BM, n0 = blockIdx.x * TC_BN;
-  const int kt = (g.K + TC_BK - 1) / TC_BK;
+  // this CTA's K range (split-K over blockIdx.z; kchunk is a multiple of TC_BK)
+  const int kbeg = blockIdx.z * g.kchunk;
+  const int kend = min(g.K, kbeg + g.kchunk);
+  const int kt = kend > kbeg ? (kend - kbeg + TC_BK - 1) / TC_BK : 0;
   const uint64_t t0 = global_ns();
 
   if (warp == 0) {
@@ -713,8 +770,8 @@ __global__ void __launch_bounds__(TC_THREADS, (STAGES <= 2 ? 2 : 1))
       auto issue = [&](int slot, int tile) {
         const uint32_t a_dst = smem_u32(ring + slot * TC_STAGE_BYTES);
         mbar_expect_tx(&full[slot], (uint32_t)TC_STAGE_BYTES);
-        tma_load_2d(a_dst, &map_a, tile * TC_BK, m0, &full[slot]);
-        tma_load_2d(a_dst + TC_A_BYTES, &map_b, tile * TC_BK, n0, &full[slot]);
+        tma_load_2d(a_dst, &map_a, kbeg + tile * TC_BK, m0, &full[slot]);
+        tma_load_2d(a_dst + TC_A_BYTES, &map_b, kbeg + tile * TC_BK, n0, &full[slot]);
       };
       constexpr uint32_t idesc = tc_idesc(TC_BM, TC_BN);
       int issued = 0, t = 0;
@@ -764,7 +821,7 @@ __global__ void __launch_bounds__(TC_THREADS, (STAGES <= 2 ? 2 : 1))
   tc_fence_after();
   if (!ok) {
     if (tid == 0) atomicOr(status, (int32_t)ST_WAIT_TIMEOUT);
-  } else if (!tc_epilogue<HEAD>(g, h, tmem, ring, w3b, bias_s, &hbar, t0, m0, n0, warp, lane)) {
+  } else if (!tc_epilogue<EPI>(g, h, tmem, ring, w3b, bias_s, &hbar, t0, m0, n0, warp, lane)) {
     if (tid == 0) atomicOr(status, (int32_t)ST_WAIT_TIMEOUT);
   }
   tc_fence_before();
@@ -947,6 +1004,25 @@ __global__ void k_to_bf16(const float* __restrict__ x, int64_t count, bf16* __re
   if (i < count) y[i] = __float2bfloat16_rn(x[i]);
 }
 
+// dst[c][r] = src[r][c] for a rows x cols BF16 matrix (row strides lds, ldd),
+// through 64 x 64 shared-memory tiles; coalesced on both sides.
+__global__ void __launch_bounds__(256) k_transpose_bf16(const bf16* __restrict__ src, int64_t lds,
+                                                        int rows, int cols, bf16* __restrict__ dst,
+                                                        int64_t ldd) {
+  __shared__ bf16 tile[64][66];
+  const int r0 = blockIdx.y * 64, c0 = blockIdx.x * 64;
+  const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;  // 64 x 4
+  for (int i = ty; i < 64; i += 4) {
+    const int r = r0 + i, c = c0 + tx;
+    tile[i][tx] = (r < rows && c < cols) ? src[(int64_t)r * lds + c] : __float2bfloat16_rn(0.0f);
+  }
+  __syncthreads();
+  for (int i = ty; i < 64; i += 4) {
+    const int c = c0 + i, r = r0 + tx;
+    if (c < cols && r < rows) dst[(int64_t)c * ldd + r] = tile[tx][i];
+  }
+}
+
 // Row indices drawn uniformly with replacement from [0, n), keyed by (seed, draw).
 __global__ void k_sample_rows(uint32_t* __restrict__ rows, int64_t count, uint32_t n,
                               uint64_t seed, uint32_t draw) {
@@ -1065,23 +1141,39 @@ int tc_stages() {
   return (e && std::atoi(e) == 4) ? 4 : 2;
 }
 
-template <int S, bool HEAD>
-void launch_tc(const GemmArgs& ga, const HeadArgs& ha, evoc_ctx* ctx) {
+template <int S, int EPI>
+void launch_tc(const GemmArgs& ga, const HeadArgs& ha, evoc_ctx* ctx, int splits = 1) {
+  constexpr bool HEAD = EPI == TC_HEAD;
   const int smem = tc_smem_bytes(S, HEAD);
-  dim3 grid((unsigned)((ga.N + TC_BN - 1) / TC_BN), (unsigned)((ga.M + TC_BM - 1) / TC_BM));
-  if (forward_path() == FwdPath::kCpAsync) {
-    EVOC_CUDA(cudaFuncSetAttribute(k_gemm_tc<S, HEAD>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    k_gemm_tc<S, HEAD><<<grid, TC_THREADS, smem, ctx->stream>>>(ga, ha, ctx->status.get());
-  } else {
-    const CUtensorMap ma = tmap_kmajor(ga.a, ga.M, ga.K, ga.lda, TC_BM);
-    const CUtensorMap mb = tmap_kmajor(ga.b, ga.N, ga.K, ga.ldb, TC_BN);
-    EVOC_CUDA(cudaFuncSetAttribute(k_gemm_tma<S, HEAD>,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    k_gemm_tma<S, HEAD><<<grid, TC_THREADS, smem, ctx->stream>>>(ma, mb, ga, ha,
-                                                                 ctx->status.get());
+  dim3 grid((unsigned)((ga.N + TC_BN - 1) / TC_BN), (unsigned)((ga.M + TC_BM - 1) / TC_BM),
+            (unsigned)splits);
+  if constexpr (EPI == TC_GELU || EPI == TC_HEAD) {
+    if (forward_path() == FwdPath::kCpAsync) {
+      EVOC_CUDA(cudaFuncSetAttribute(k_gemm_tc<S, HEAD>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+      k_gemm_tc<S, HEAD><<<grid, TC_THREADS, smem, ctx->stream>>>(ga, ha, ctx->status.get());
+      EVOC_CHECK_LAUNCH();
+      return;
+    }
   }
+  const CUtensorMap ma = tmap_kmajor(ga.a, ga.M, ga.K, ga.lda, TC_BM);
+  const CUtensorMap mb = tmap_kmajor(ga.b, ga.N, ga.K, ga.ldb, TC_BN);
+  EVOC_CUDA(cudaFuncSetAttribute(k_gemm_tma<S, EPI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem));
+  k_gemm_tma<S, EPI><<<grid, TC_THREADS, smem, ctx->stream>>>(ma, mb, ga, ha, ctx->status.get());
   EVOC_CHECK_LAUNCH();
+}
+
+// Splits of K (multiples of TC_BK) so that tiles x splits covers about two
+// CTAs per SM.
+void choose_splits_tc(int M, int N, int K, int num_sms, int* splits, int* kchunk) {
+  const int tiles = ((M + TC_BM - 1) / TC_BM) * ((N + TC_BN - 1) / TC_BN);
+  const int ktiles = std::max(1, (K + TC_BK - 1) / TC_BK);
+  int want = std::max(1, (2 * num_sms) / tiles);
+  want = std::min(want, ktiles);
+  const int per = (ktiles + want - 1) / want;
+  *kchunk = per * TC_BK;
+  *splits = std::max(1, (K + *kchunk - 1) / *kchunk);
 }
 
 void launch_forward_gemm(const GemmArgs& ga, evoc_ctx* ctx) {
@@ -1091,20 +1183,31 @@ void launch_forward_gemm(const GemmArgs& ga, evoc_ctx* ctx) {
   }
   const HeadArgs none{};
   if (tc_stages() == 4)
-    launch_tc<4, false>(ga, none, ctx);
+    launch_tc<4, TC_GELU>(ga, none, ctx);
   else
-    launch_tc<2, false>(ga, none, ctx);
+    launch_tc<2, TC_GELU>(ga, none, ctx);
 }
 
 // Second hidden layer fused with the output layer (inference on tcgen05).
 void launch_forward_head(const GemmArgs& ga, const HeadArgs& ha, evoc_ctx* ctx) {
   if (tc_stages() == 4)
-    launch_tc<4, true>(ga, ha, ctx);
+    launch_tc<4, TC_HEAD>(ga, ha, ctx);
   else
-    launch_tc<2, true>(ga, ha, ctx);
+    launch_tc<2, TC_HEAD>(ga, ha, ctx);
 }
 
 int tc_col_tiles(int n) { return (n + TC_BN - 1) / TC_BN; }
+
+void transpose_bf16(const bf16* src, int64_t lds, int rows, int cols, bf16* dst, int64_t ldd,
+                    cudaStream_t s) {
+  dim3 grid((unsigned)((cols + 63) / 64), (unsigned)((rows + 63) / 64));
+  k_transpose_bf16<<<grid, 256, 0, s>>>(src, lds, rows, cols, dst, ldd);
+  EVOC_CHECK_LAUNCH();
+}
+
+// Row stride (elements) of a transposed [cols][rows] copy: rows rounded up
+// to 8, so every row starts 16-byte aligned (a TMA requirement).
+int64_t transposed_ld(int64_t rows) { return (rows + 7) / 8 * 8; }
 
 // Splits of the K dimension so that tiles x splits covers about two waves.
 void choose_splits(int M, int N, int K, int num_sms, int* splits, int* kchunk) {
@@ -1120,6 +1223,7 @@ void choose_splits(int M, int N, int K, int num_sms, int* splits, int* kchunk) {
 // Scratch of one forward/backward pass over `rows` rows.
 struct MlpScratch {
   DevBuf<bf16> x, a1, a2, dh1, dh2;
+  DevBuf<bf16> xt, a1t, dh1t, dh2t;  // [features][batch] copies for the weight gradients
   DevBuf<float> h1, h2, target, dy, part, loss_part, loss, ypart;
   DevBuf<uint32_t> rows;
   int64_t cap = 0;
@@ -1150,8 +1254,11 @@ int64_t partial_floats(const evoc_mlp* net, int64_t rows, int* s1, int* kc1, int
   int want3 = std::max(1, (2 * sms + colblocks - 1) / colblocks);
   *rps3 = std::max<int64_t>(1, (rows + want3 - 1) / want3);
   *s3 = (int)((rows + *rps3 - 1) / *rps3);
-  const int64_t p1 = (int64_t)*s1 * net->hid * net->in;
-  const int64_t p2 = (int64_t)*s2 * net->hid * net->hid;
+  int t1, tk1, t2, tk2;  // the tcgen05 weight-gradient splits
+  choose_splits_tc(net->hid, net->in, (int)rows, sms, &t1, &tk1);
+  choose_splits_tc(net->hid, net->hid, (int)rows, sms, &t2, &tk2);
+  const int64_t p1 = (int64_t)std::max(*s1, t1) * net->hid * net->in;
+  const int64_t p2 = (int64_t)std::max(*s2, t2) * net->hid * net->hid;
   const int64_t p3 = (int64_t)*s3 * ((int64_t)net->out * net->hid + 2 * net->hid + net->out);
   return std::max(p1, std::max(p2, p3));
 }
@@ -1178,6 +1285,13 @@ void alloc_scratch(const evoc_mlp* net, MlpScratch& sc, int64_t rows, bool train
   sc.dy.alloc((size_t)rows * net->out, s);
   sc.part.alloc((size_t)pf, s);
   sc.loss_part.alloc((size_t)sc.head_grid, s);
+  if (use_tcgen05()) {
+    const int64_t ldt = transposed_ld(rows);
+    sc.xt.alloc((size_t)net->in * ldt, s);
+    sc.a1t.alloc((size_t)net->hid * ldt, s);
+    sc.dh1t.alloc((size_t)net->hid * ldt, s);
+    sc.dh2t.alloc((size_t)net->hid * ldt, s);
+  }
   sc.rows.alloc((size_t)rows, s);
 }
 
@@ -1234,39 +1348,76 @@ void forward_backward(evoc_mlp* net, int64_t rows, MlpScratch& sc, float* loss_d
   EVOC_CHECK_LAUNCH();
   k_loss_total<<<1, 32, 0, s>>>(sc.loss_part.get(), hg, scale, loss_dst);
   EVOC_CHECK_LAUNCH();
-  // dH1 = (dH2 W2) * gelu'(H1): W2 is [out][in] = [K][N], read MN-major.
-  GemmArgs gd{};
-  gd.a = sc.dh2.get(); gd.lda = net->hid;
-  gd.b = wb + net->o_w2; gd.ldb = net->hid;
-  gd.M = (int)rows; gd.N = net->hid; gd.K = net->hid; gd.kchunk = ((net->hid + GBK - 1) / GBK) * GBK;
-  gd.pre = sc.h1.get();
-  gd.outb = sc.dh1.get();
-  launch_gemm<true, false, EPI_GELU_GRAD>(gd, 1, s);
-
   int s1, kc1, s2, kc2, s3;
   int64_t rps3;
   partial_floats(net, rows, &s1, &kc1, &s2, &kc2, &s3, &rps3);
   float* grad = net->grad.get();
-  // dW2 = dH2^T A1 (both [batch][hidden]: MN-major with the batch as K).
-  GemmArgs gw2{};
-  gw2.a = sc.dh2.get(); gw2.lda = net->hid;
-  gw2.b = sc.a1.get(); gw2.ldb = net->hid;
-  gw2.M = net->hid; gw2.N = net->hid; gw2.K = (int)rows; gw2.kchunk = kc2;
-  gw2.outf = sc.part.get();
-  launch_gemm<false, false, EPI_PARTIAL>(gw2, s2, s);
-  const int64_t cw2 = (int64_t)net->hid * net->hid;
-  k_sum_splits<<<blocks_for(cw2, 256), 256, 0, s>>>(sc.part.get(), s2, cw2, grad + net->o_w2);
-  EVOC_CHECK_LAUNCH();
-  // dW1 = dH1^T X.
-  GemmArgs gw1{};
-  gw1.a = sc.dh1.get(); gw1.lda = net->hid;
-  gw1.b = sc.x.get(); gw1.ldb = net->in;
-  gw1.M = net->hid; gw1.N = net->in; gw1.K = (int)rows; gw1.kchunk = kc1;
-  gw1.outf = sc.part.get();
-  launch_gemm<false, false, EPI_PARTIAL>(gw1, s1, s);
-  const int64_t cw1 = (int64_t)net->hid * net->in;
-  k_sum_splits<<<blocks_for(cw1, 256), 256, 0, s>>>(sc.part.get(), s1, cw1, grad + net->o_w1);
-  EVOC_CHECK_LAUNCH();
+  const int64_t cw1 = (int64_t)net->hid * net->in, cw2 = (int64_t)net->hid * net->hid;
+  if (use_tcgen05()) {
+    // dH1 = (dH2 W2) * gelu'(H1) with W2^T as the K-major B operand.
+    const HeadArgs none{};
+    GemmArgs gd{};
+    gd.a = sc.dh2.get(); gd.lda = net->hid;
+    gd.b = net->w2t.get(); gd.ldb = net->hid;
+    gd.M = (int)rows; gd.N = net->hid; gd.K = net->hid;
+    gd.kchunk = (net->hid + TC_BK - 1) / TC_BK * TC_BK;
+    gd.pre = sc.h1.get();
+    gd.outb = sc.dh1.get();
+    launch_tc<2, TC_GRAD>(gd, none, net->ctx);
+    // Weight gradients over the batch: K-major copies [features][batch].
+    const int64_t ldt = transposed_ld(rows);
+    transpose_bf16(sc.dh2.get(), net->hid, (int)rows, net->hid, sc.dh2t.get(), ldt, s);
+    transpose_bf16(sc.a1.get(), net->hid, (int)rows, net->hid, sc.a1t.get(), ldt, s);
+    transpose_bf16(sc.dh1.get(), net->hid, (int)rows, net->hid, sc.dh1t.get(), ldt, s);
+    transpose_bf16(sc.x.get(), net->in, (int)rows, net->in, sc.xt.get(), ldt, s);
+    int t2, tk2, t1, tk1;
+    choose_splits_tc(net->hid, net->hid, (int)rows, net->ctx->num_sms, &t2, &tk2);
+    choose_splits_tc(net->hid, net->in, (int)rows, net->ctx->num_sms, &t1, &tk1);
+    GemmArgs gw2{};  // dW2 = dH2^T A1
+    gw2.a = sc.dh2t.get(); gw2.lda = ldt;
+    gw2.b = sc.a1t.get(); gw2.ldb = ldt;
+    gw2.M = net->hid; gw2.N = net->hid; gw2.K = (int)rows; gw2.kchunk = tk2;
+    gw2.outf = sc.part.get();
+    launch_tc<2, TC_F32>(gw2, none, net->ctx, t2);
+    k_sum_splits<<<blocks_for(cw2, 256), 256, 0, s>>>(sc.part.get(), t2, cw2, grad + net->o_w2);
+    EVOC_CHECK_LAUNCH();
+    GemmArgs gw1{};  // dW1 = dH1^T X
+    gw1.a = sc.dh1t.get(); gw1.lda = ldt;
+    gw1.b = sc.xt.get(); gw1.ldb = ldt;
+    gw1.M = net->hid; gw1.N = net->in; gw1.K = (int)rows; gw1.kchunk = tk1;
+    gw1.outf = sc.part.get();
+    launch_tc<2, TC_F32>(gw1, none, net->ctx, t1);
+    k_sum_splits<<<blocks_for(cw1, 256), 256, 0, s>>>(sc.part.get(), t1, cw1, grad + net->o_w1);
+    EVOC_CHECK_LAUNCH();
+  } else {
+    // dH1 = (dH2 W2) * gelu'(H1): W2 is [out][in] = [K][N], read MN-major.
+    GemmArgs gd{};
+    gd.a = sc.dh2.get(); gd.lda = net->hid;
+    gd.b = wb + net->o_w2; gd.ldb = net->hid;
+    gd.M = (int)rows; gd.N = net->hid; gd.K = net->hid;
+    gd.kchunk = ((net->hid + GBK - 1) / GBK) * GBK;
+    gd.pre = sc.h1.get();
+    gd.outb = sc.dh1.get();
+    launch_gemm<true, false, EPI_GELU_GRAD>(gd, 1, s);
+    // dW2 = dH2^T A1 (both [batch][hidden]: MN-major with the batch as K).
+    GemmArgs gw2{};
+    gw2.a = sc.dh2.get(); gw2.lda = net->hid;
+    gw2.b = sc.a1.get(); gw2.ldb = net->hid;
+    gw2.M = net->hid; gw2.N = net->hid; gw2.K = (int)rows; gw2.kchunk = kc2;
+    gw2.outf = sc.part.get();
+    launch_gemm<false, false, EPI_PARTIAL>(gw2, s2, s);
+    k_sum_splits<<<blocks_for(cw2, 256), 256, 0, s>>>(sc.part.get(), s2, cw2, grad + net->o_w2);
+    EVOC_CHECK_LAUNCH();
+    // dW1 = dH1^T X.
+    GemmArgs gw1{};
+    gw1.a = sc.dh1.get(); gw1.lda = net->hid;
+    gw1.b = sc.x.get(); gw1.ldb = net->in;
+    gw1.M = net->hid; gw1.N = net->in; gw1.K = (int)rows; gw1.kchunk = kc1;
+    gw1.outf = sc.part.get();
+    launch_gemm<false, false, EPI_PARTIAL>(gw1, s1, s);
+    k_sum_splits<<<blocks_for(cw1, 256), 256, 0, s>>>(sc.part.get(), s1, cw1, grad + net->o_w1);
+    EVOC_CHECK_LAUNCH();
+  }
   // dW3, db2, db3 in one column pass; then db1.
   float* pw3 = sc.part.get();
   float* pb2 = pw3 + (int64_t)s3 * net->out * net->hid;
@@ -1287,6 +1438,11 @@ void forward_backward(evoc_mlp* net, int64_t rows, MlpScratch& sc, float* loss_d
   EVOC_CHECK_LAUNCH();
 }
 
+void refresh_w2t(evoc_mlp* net) {
+  transpose_bf16(net->wb.get() + net->o_w2, net->hid, net->hid, net->hid, net->w2t.get(),
+                 net->hid, net->ctx->stream);
+}
+
 void adam_step(evoc_mlp* net, float lr, float beta1, float beta2, float eps) {
   net->adam_steps += 1;
   const double t = (double)net->adam_steps;
@@ -1296,12 +1452,14 @@ void adam_step(evoc_mlp* net, float lr, float beta1, float beta2, float eps) {
       net->master.get(), net->adam_m.get(), net->adam_v.get(), net->grad.get(), net->wb.get(),
       net->n_params, lr, beta1, beta2, eps, bc1, bc2);
   EVOC_CHECK_LAUNCH();
+  refresh_w2t(net);
 }
 
 void refresh_bf16(evoc_mlp* net) {
   k_to_bf16<<<blocks_for(net->n_params, 256), 256, 0, net->ctx->stream>>>(
       net->master.get(), net->n_params, net->wb.get());
   EVOC_CHECK_LAUNCH();
+  refresh_w2t(net);
 }
 
 // splitmix64: the host-side generator of the initial weights.
@@ -1427,6 +1585,7 @@ evoc_mlp* mlp_create(evoc_ctx* ctx, int in, int hid, int out, uint64_t seed) {
   net->adam_v.alloc(np, s);
   net->grad.alloc(np, s);
   net->wb.alloc(np, s);
+  net->w2t.alloc((size_t)hid * hid, s);
   // Linear-layer initialisation: weights and biases uniform in
   // [-1/sqrt(fan_in), 1/sqrt(fan_in)).
   std::vector<float> h(np);
@@ -1463,6 +1622,7 @@ void mlp_free(evoc_mlp* net) {
   net->adam_v.release();
   net->grad.release();
   net->wb.release();
+  net->w2t.release();
   if (s) cudaStreamSynchronize(s);
   delete net;
 }

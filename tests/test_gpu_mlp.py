@@ -99,6 +99,25 @@ def test_tcgen05_forward_matches_mma_sync(ctx, i, h, o, n, stages, path, monkeyp
     assert rel <= 2e-3, rel
 
 
+@pytest.mark.parametrize("i,h,o,n", DIMS + [(768, 512, 8, 8192)])
+def test_tcgen05_gradients_match_mma_sync(ctx, i, h, o, n, monkeypatch):
+    """The tcgen05 backward (default: GELU' epilogue on a W2^T operand,
+    split-K weight gradients over transposed copies) and the mma.sync backward
+    give the same gradients up to accumulation order; both match the oracle."""
+    net = _net(ctx, i, h, o)
+    x, t = _data(i, o, n, seed=12)
+    l_tc, g_tc = net.gradients(x, t)
+    monkeypatch.setenv("EVOC_MLP_GEMM", "mma")
+    l_mma, g_mma = net.gradients(x, t)
+    monkeypatch.delenv("EVOC_MLP_GEMM")
+    want_loss, want = M.loss_and_gradients(M.unpack(net.get_params(), i, h, o), x, t)
+    assert l_tc == pytest.approx(want_loss, rel=1e-3) and l_mma == pytest.approx(want_loss, rel=1e-3)
+    a, b = net.unpack(g_tc), net.unpack(g_mma)
+    for name in ("w1", "b1", "w2", "b2", "w3", "b3"):
+        _close(a[name], want[name], "tcgen05 " + name)
+        _close(b[name], want[name], "mma.sync " + name)
+
+
 def test_tcgen05_prediction_over_chunks(ctx):
     """Rows beyond the 262,144-row prediction chunk and a ragged last tile."""
     net = _net(ctx, 64, 256, 8)
