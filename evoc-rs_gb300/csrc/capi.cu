@@ -151,6 +151,7 @@ void evoc_ctx_destroy(evoc_ctx_t* ctx) {
   cudaSetDevice(ctx->device);
   cudaStream_t s = ctx->stream;
   ctx->status.release();
+  ctx->slot_cache.release();
   if (s) {
     cudaStreamSynchronize(s);
     cudaStreamDestroy(s);

@@ -959,12 +959,15 @@ __device__ __forceinline__ int nth_set_bit(uint32_t m, int r) {
 // Fill pass from the planes (n_epochs <= 64, at most 3 negatives per edge and
 // epoch): warp per (tile, epoch), numbered tile-major: a hub tile's epochs
 // run in parallel, and the warps of one tile read its partner ids from L2
-// together. Lane l owns plane word l of each 32-word window of the tile's entries and
-// walks its fired bits in order; its slots (each attraction, then its
-// negatives) start at the prefix of the lower lanes' slot counts, so every
-// (epoch, tile) segment holds the terms in the order of the reference's
-// serial sum. Negative draws (Philox counter (j, epoch, edge)) are queued in
-// shared memory and drawn 32 at a time.
+// together. For each 32-word window of the tile's entries, a prefix sum of the
+// words' fired counts numbers the fired entries in incidence order; each
+// batch of 32 consecutive fired entries goes one per lane (the word by a
+// shuffle binary search, the bit by nth_set_bit), so every lane has work and
+// the batch's slots (each attraction, then its negatives, placed by a prefix
+// of the per-entry slot counts) land close together. Every (epoch, tile)
+// segment holds the terms in the order of the reference's serial sum.
+// Negative draws (Philox counter (j, epoch, edge)) are queued in shared memory
+// and drawn 32 at a time.
 constexpr int DRAW_Q = 160;  // >= 31 left over + 32 lanes x 3 negatives
 struct DrawJob {
   int64_t q;        // slot index
@@ -1030,38 +1033,55 @@ __global__ void __launch_bounds__(128) k_plane_fill(
   const int64_t po = (int64_t)t * W;
   int64_t cur = tile_off[(int64_t)t * ntiles + tile];
   int qn = 0;  // queued draws
+  int node = 0;  // node of this lane's current entry (a lane's entries only move forward)
   for (int64_t ws = wb; ws < we; ws += 32) {
     const int64_t w = ws + lane;
-    uint32_t x = tile_word(fplane + po, w, wb, we, lo_mask, hi_mask);
-    // negative bits are set only on fired entries: masking by x keeps the tile's
-    const uint32_t g0 = x ? nplane0[po + w] & x : 0u, g1 = x ? nplane1[po + w] & x : 0u;
-    const int cnt = __popc(x) + __popc(g0) + 2 * __popc(g1);
-    int incl = cnt;
+    const uint32_t xw = tile_word(fplane + po, w, wb, we, lo_mask, hi_mask);
+    // negative bits are set only on fired entries: masking by xw keeps the tile's
+    const uint32_t g0w = xw ? nplane0[po + w] & xw : 0u, g1w = xw ? nplane1[po + w] & xw : 0u;
+    int fincl = __popc(xw);  // fired entries up to and including this lane's word
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(FULL, incl, o);
-      if (lane >= o) incl += y;
+      const int y = __shfl_up_sync(FULL, fincl, o);
+      if (lane >= o) fincl += y;
     }
-    int64_t q = cur + incl - cnt;
-    cur += __shfl_sync(FULL, incl, 31);
-    const int iters = __reduce_max_sync(FULL, (unsigned)__popc(x));
-    int node = 0;  // node of this lane's current entry (entries only move forward)
-    for (int it = 0; it < iters; ++it) {
+    const int ftot = __shfl_sync(FULL, fincl, 31);
+    // batches of 32 consecutive fired entries (incidence order), one per lane
+    for (int k0 = 0; k0 < ftot; k0 += 32) {
+      const int k = k0 + lane;
+      int j = 0;  // the word (lane) holding fired entry k: first j with fincl[j] > k
+#pragma unroll
+      for (int step = 16; step >= 1; step >>= 1)
+        if (__shfl_sync(FULL, fincl, j + step - 1) <= k) j += step;
+      const uint32_t xj = __shfl_sync(FULL, xw, j);
+      const uint32_t g0j = __shfl_sync(FULL, g0w, j), g1j = __shfl_sync(FULL, g1w, j);
+      const int fex = __shfl_sync(FULL, fincl, j) - __popc(xj);
+      const bool valid = k < ftot;
       int nn = 0;
+      int64_t p = 0;
+      if (valid) {
+        const int b = nth_set_bit(xj, k - fex);
+        p = ((ws + j) << 5) + b;
+        nn = (int)(((g0j >> b) & 1u) | (((g1j >> b) & 1u) << 1));
+      }
+      const int cnt = valid ? 1 + nn : 0;  // this entry's slots: attraction + negatives
+      int cincl = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL, cincl, o);
+        if (lane >= o) cincl += y;
+      }
+      const int64_t q = cur + cincl - cnt;
+      cur += __shfl_sync(FULL, cincl, 31);
       uint32_t eidx = 0;
       int64_t q0 = 0;
-      if (x) {
-        const int b = __ffs(x) - 1;
-        x &= x - 1;
-        const int64_t p = (w << 5) + b;
+      if (valid) {
         while (node + 1 < nt && sm.pb[node + 1] <= p) ++node;
-        nn = (int)(((g0 >> b) & 1u) | (((g1 >> b) & 1u) << 1));
         slots[q] = make_uint2(inc_other[p], (uint32_t)node);
         q0 = q + 1;
-        q += 1 + nn;
         eidx = (uint32_t)(p + sm.eb[node]);
       }
-      // queue this iteration's draws, level by level (draw j of every lane with
+      // queue this batch's draws, level by level (draw j of every lane with
       // more than j negatives); their order in the queue does not matter
       const uint32_t lt = (1u << lane) - 1u;
       const uint32_t b1 = __ballot_sync(FULL, nn >= 1), b2 = __ballot_sync(FULL, nn >= 2),
@@ -1678,7 +1698,8 @@ static bool build_slots(evoc_plan* pl, const float* inc_ps, const uint8_t* inc_u
   size_t free_b = 0, total_b = 0;
   EVOC_CUDA(cudaMemGetInfo(&free_b, &total_b));
   const double need = (double)sizeof(uint2) * (double)total;
-  if (!force_slots && need > 0.5 * (double)free_b) return false;
+  const double avail = (double)free_b + (double)pl->ctx->slot_cache.bytes();  // the cache is reusable
+  if (!force_slots && need > 0.5 * avail) return false;
   pl->max_neg = maxneg;
   trace.mark("offset scan + sync");
   {
@@ -1694,7 +1715,12 @@ static bool build_slots(evoc_plan* pl, const float* inc_ps, const uint8_t* inc_u
     EVOC_CHECK_LAUNCH();
   }
   trace.mark("tile order");
-  pl->slots.alloc(total, s);
+  if (total > 0 && pl->ctx->slot_cache.count >= (size_t)total) {
+    pl->slots = std::move(pl->ctx->slot_cache);
+  } else {
+    pl->ctx->slot_cache.release();
+    pl->slots.alloc(total, s);
+  }
   trace.mark("alloc slots");
   const uint32_t* pon = pl->n_problems > 1 ? pl->prob_of_node.get() : nullptr;
   const ProbInfo* pinfo = pl->n_problems > 1 ? pl->prob.get() : nullptr;
@@ -2260,6 +2286,8 @@ void plan_upload_init_and_run(evoc_plan* pl, const float* const* h_inits,
 
 void plan_free(evoc_plan* pl) {
   if (!pl) return;
+  if (pl->ctx && pl->slots.count > pl->ctx->slot_cache.count)
+    pl->ctx->slot_cache = std::move(pl->slots);
   if (pl->graph_exec) cudaGraphExecDestroy(pl->graph_exec);
   if (pl->graph) cudaGraphDestroy(pl->graph);
   delete pl;

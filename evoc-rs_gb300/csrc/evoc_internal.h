@@ -141,6 +141,10 @@ struct evoc_ctx {
   cudaStream_t stream = nullptr;
   std::string last_error;
   evoc::DevBuf<int32_t> status;  // device status word
+  // The largest gradient-slot buffer of a freed plan, handed to the next plan
+  // that fits in it (stream order makes the reuse safe): repeated one-shot
+  // embeddings skip a multi-gigabyte allocation each.
+  evoc::DevBuf<uint2> slot_cache;
 };
 
 struct evoc_graph {
