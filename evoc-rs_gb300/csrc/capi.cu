@@ -571,6 +571,7 @@ void evoc_mlp_train_params_default(evoc_mlp_train_params_t* p) {
   p->beta1 = 0.9f;
   p->beta2 = 0.999f;
   p->eps = 1e-8f;
+  p->lr_end = 1e-4f;
   p->seed = 0;
 }
 

@@ -1709,7 +1709,8 @@ void mlp_gradients_host(evoc_mlp* net, const float* x, const float* target, int6
   check_status(net->ctx, "evoc_mlp_gradients");
 }
 
-// Training on layouts of several instances: every `align_every` steps each
+// Training on layouts of several instances (step size falling linearly from
+// lr to lr_end): every `align_every` steps each
 // instance's layout is re-aligned to the network's prediction on a fixed
 // sample of its rows (means removed, Procrustes rotation, prediction mean
 // added); each step then draws `batch` rows of one instance (round robin)
@@ -1820,7 +1821,9 @@ void mlp_fit_device(evoc_mlp* net, int32_t m, const uint16_t* const* xs,
         reinterpret_cast<uint32_t*>(sc.target.get()));
     EVOC_CHECK_LAUNCH();
     forward_backward(net, batch, sc, losses.get() + step);
-    adam_step(net, p->lr, p->beta1, p->beta2, p->eps);
+    const double frac = p->steps > 1 ? (double)step / (double)(p->steps - 1) : 0.0;
+    const float lr = (float)((double)p->lr + ((double)p->lr_end - (double)p->lr) * frac);
+    adam_step(net, lr, p->beta1, p->beta2, p->eps);
   }
   if (loss_history && p->steps > 0)
     EVOC_CUDA(cudaMemcpyAsync(loss_history, losses.get(), (size_t)p->steps * sizeof(float),

@@ -82,6 +82,7 @@ class MlpTrainParamsC(C.Structure):
         ("beta1", C.c_float),
         ("beta2", C.c_float),
         ("eps", C.c_float),
+        ("lr_end", C.c_float),
         ("seed", C.c_uint64),
     ]
 
@@ -97,12 +98,13 @@ class MlpTrainParams:
     beta1: float = 0.9
     beta2: float = 0.999
     eps: float = 1e-8
+    lr_end: float = 1e-4
     seed: int = 0
 
     def to_c(self) -> MlpTrainParamsC:
         return MlpTrainParamsC(int(self.steps), int(self.batch), int(self.align_every),
                                int(self.align_rows), self.lr, self.beta1, self.beta2,
-                               self.eps, int(self.seed))
+                               self.eps, self.lr_end, int(self.seed))
 
 
 class EpochStatsC(C.Structure):

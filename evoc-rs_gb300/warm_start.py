@@ -56,11 +56,12 @@ def fuzzy_graph(ctx, inst: dict):
                                 inst["k"], float(inst["k"]), True)
 
 
-def embed_device(ctx, graph, n: int, dim: int, n_epochs: int, seed: int, init=None):
+def embed_device(ctx, graph, n: int, dim: int, n_epochs: int, seed: int, init=None,
+                 initial_alpha: float = 0.1):
     """evoc_embedding on a device graph; init (n x dim f32 device tensor) or random."""
     torch = _torch()
     import evoc_gb300 as E
-    params = E.EvocEmbeddingParams(n_epochs=n_epochs)
+    params = E.EvocEmbeddingParams(n_epochs=n_epochs, initial_alpha=initial_alpha)
     plan = ctx.plan(graph, dim, params, seed=seed)
     out = torch.empty(n, dim, dtype=torch.float32, device="cuda")
     plan.run_device(None if init is None else init.data_ptr(), out.data_ptr())

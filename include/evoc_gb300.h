@@ -340,6 +340,7 @@ typedef struct {
   float beta1;         /*                                             (0.9)   */
   float beta2;         /*                                             (0.999) */
   float eps;           /*                                             (1e-8)  */
+  float lr_end;        /* step size reached linearly at the last step (1e-4)  */
   uint64_t seed;       /* row sampling                                (0)     */
 } evoc_mlp_train_params_t;
 
