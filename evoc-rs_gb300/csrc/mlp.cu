@@ -268,15 +268,18 @@ __global__ void __launch_bounds__(GTHREADS) k_gemm(GemmArgs g) {
 }
 
 // ---------------------------------------------------------------------------
-// Forward layer on the 5th-generation tensor cores (tcgen05):
-//   out = bf16(gelu(A W^T + bias)), pre = A W^T + bias (optional)
-// A [M][K] and W [N][K] are K-major BF16. One CTA computes a 128 x 256 tile
-// whose FP32 accumulator lives in tensor memory (256 columns x 128 lanes).
+// GEMM layers on the 5th-generation tensor cores (tcgen05):
+//   C = A B^T with A [M][K] and B [N][K] K-major BF16, then one of the TcEpi
+//   epilogues (forward: bias + GELU, or with the output layer fused;
+//   backward: times gelu'(pre), or FP32 split-K partials).
+// One CTA computes a 128 x 256 tile whose FP32 accumulator lives in tensor
+// memory (256 columns x 128 lanes).
 //
-// Mainloop: K advances 64 elements (one 128-byte swizzle atom) per stage
-// through a 4-stage shared-memory ring filled by cp.async in the 128-byte
-// swizzled K-major layout (row r, 16-byte chunk c at r * 128 + ((c ^ (r % 8))
-// * 16), 8-row groups 1024 bytes apart). One thread issues the four
+// Mainloop (k_gemm_tc, the cp.async-fed variant; k_gemm_tma below moves the
+// same tiles by TMA): K advances 64 elements (one 128-byte swizzle atom) per
+// stage through a 2- or 4-stage shared-memory ring in the 128-byte swizzled
+// K-major layout (row r, 16-byte chunk c at r * 128 + ((c ^ (r % 8)) * 16),
+// 8-row groups 1024 bytes apart). One thread issues the four
 // K = 16 MMAs of a stage (M = 128, N = 256, kind::f16 with BF16 inputs, FP32
 // accumulation) and commits them to the stage's mbarrier; the ring slot is
 // refilled once that barrier reports the MMAs done. Every wait is bounded

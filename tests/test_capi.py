@@ -82,3 +82,17 @@ def test_null_context_arguments_rejected():
     assert lib.evoc_fuzzy_set(None, None, None, 0, 0, 0.0, 1, ctypes.byref(h)) == E.EVOC_ERR_INVALID_ARGUMENT
     assert lib.evoc_ctx_create(0, None) != 0
     assert lib.evoc_last_error(None) is not None
+
+
+def test_mlp_train_params_default():
+    """evoc_mlp_train_params_default fills the documented defaults (no GPU)."""
+    import ctypes as C
+    import evoc_gb300 as E
+    p = E.MlpTrainParamsC()
+    E.load_library().evoc_mlp_train_params_default(C.byref(p))
+    d = E.MlpTrainParams()
+    assert (p.steps, p.batch, p.align_every, p.align_rows) == (d.steps, d.batch, d.align_every,
+                                                               d.align_rows)
+    for name in ("lr", "beta1", "beta2", "eps", "lr_end"):
+        assert getattr(p, name) == pytest.approx(getattr(d, name), rel=1e-6), name
+    assert p.seed == d.seed
