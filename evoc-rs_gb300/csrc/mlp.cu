@@ -357,6 +357,18 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64
     if (global_ns() - t0 > TC_WAIT_NS) return false;
   }
 }
+// Non-blocking: has the phase with the given parity completed?
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
 __device__ __forceinline__ void tc_fence_before() {
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 }
@@ -837,6 +849,298 @@ __global__ void __launch_bounds__(TC_THREADS, (STAGES <= 2 ? 2 : 1))
   }
 }
 
+// ---------------------------------------------------------------------------
+// Persistent, warp-specialised forward layer (TMA + tcgen05), for N <= 2 x 256
+// columns: one CTA per SM, a fixed column tile per CTA (CTA c takes column
+// tile c % nc and row tiles c / nc, c / nc + G / nc, ...), so its bias slice
+// and W3 slice are staged once.
+//   warp 0 (lane 0): TMA producer, running ahead through the smem ring across
+//                    tile boundaries (empty/full mbarriers);
+//   warp 1 (lane 0): MMA issuer into one of two 256-column TMEM accumulators
+//                    (tfull/tempty mbarriers), and, with HEAD, the output-layer
+//                    MMA chain of the previous tile once its activations are
+//                    staged (a2full -> hfull);
+//   warps 4..11:     epilogue, warp w on TMEM lanes 32 (w % 4) and column half
+//                    (w - 4) / 4; with HEAD the BF16 activations go to a
+//                    dedicated 64 KB swizzled tile instead of global memory.
+// The epilogue of tile i overlaps the mainloop of tile i + 1. Every wait is
+// bounded (2 s each); a timeout sets ST_WAIT_TIMEOUT and an abort flag that
+// every role checks before its next wait.
+// ---------------------------------------------------------------------------
+constexpr int PS_THREADS = 384;
+constexpr int PS_A2_BYTES = TC_BM * TC_BN * 2;  // the staged activation tile (HEAD)
+
+inline int ps_smem_bytes(int stages, bool head) {
+  return stages * TC_STAGE_BYTES + 1024 + (head ? PS_A2_BYTES + TC_W3_BYTES : 0) +
+         TC_BN * (int)sizeof(float);
+}
+
+template <int STAGES, bool HEAD>
+__global__ void __launch_bounds__(PS_THREADS, 1)
+    k_gemm_persist(const __grid_constant__ CUtensorMap map_a,
+                   const __grid_constant__ CUtensorMap map_b, GemmArgs g, HeadArgs h,
+                   int32_t* __restrict__ status) {
+  extern __shared__ unsigned char tc_raw[];
+  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES];
+  __shared__ __align__(8) uint64_t tfull[2], tempty[2], a2full, hfull;
+  __shared__ uint32_t tmem_slot;
+  __shared__ volatile int aborted;
+  const uint32_t raw = smem_u32(tc_raw);
+  unsigned char* ring = tc_raw + (((raw + 1023u) & ~1023u) - raw);
+  unsigned char* a2s = ring + STAGES * TC_STAGE_BYTES;            // HEAD: [4 atoms][128][128 B]
+  unsigned char* w3b = a2s + (HEAD ? PS_A2_BYTES : 0);            // HEAD: W3 slice
+  float* bias_s = reinterpret_cast<float*>(w3b + (HEAD ? TC_W3_BYTES : 0));
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nc = (g.N + TC_BN - 1) / TC_BN;          // column tiles (1 or 2)
+  const int n0 = (int)(blockIdx.x % nc) * TC_BN;
+  const int mt = (g.M + TC_BM - 1) / TC_BM;          // row tiles
+  const int first = (int)(blockIdx.x / nc), step = (int)(gridDim.x / nc);
+  const int kt = (g.K + TC_BK - 1) / TC_BK;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_slot)),
+                 "r"(2 * TC_TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&tfull[b], 1);
+      mbar_init(&tempty[b], 8);  // one arrival per epilogue warp
+    }
+    mbar_init(&a2full, 8);
+    mbar_init(&hfull, 1);
+    aborted = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  tc_stage_constants<HEAD>(g, h, w3b, bias_s, n0, tid);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  auto fail = [&]() {
+    aborted = 1;
+    atomicOr(status, (int32_t)ST_WAIT_TIMEOUT);
+  };
+
+  if (warp == 0) {
+    if (lane == 0) {  // ---- TMA producer
+      int64_t gk = 0;
+      for (int mtile = first; mtile < mt && !aborted; mtile += step) {
+        for (int kb = 0; kb < kt; ++kb, ++gk) {
+          const int slot = (int)(gk % STAGES);
+          if (gk >= STAGES &&
+              !mbar_wait(&empty[slot], (uint32_t)(((gk / STAGES) - 1) & 1), global_ns())) {
+            fail();
+            break;
+          }
+          if (aborted) break;
+          const uint32_t dst = smem_u32(ring + slot * TC_STAGE_BYTES);
+          mbar_expect_tx(&full[slot], (uint32_t)TC_STAGE_BYTES);
+          tma_load_2d(dst, &map_a, kb * TC_BK, mtile * TC_BM, &full[slot]);
+          tma_load_2d(dst + TC_A_BYTES, &map_b, kb * TC_BK, n0, &full[slot]);
+        }
+      }
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    if (lane == 0) {  // ---- MMA issuer
+      constexpr uint32_t idesc = tc_idesc(TC_BM, TC_BN);
+      constexpr uint32_t idesc16 = tc_idesc(TC_BM, 16);
+      auto issue_head = [&](int it) {  // output layer of local tile it (a2full seen)
+        tc_fence_after();
+        const uint32_t a0 = smem_u32(a2s), b0 = smem_u32(w3b);
+        const uint32_t acc = tmem + (uint32_t)((it & 1) * TC_BN);
+#pragma unroll
+        for (int k = 0; k < TC_BN / 16; ++k) {
+          const int atom = k >> 2, off = (k & 3) * 32;
+          tc_mma(acc, sw128_desc(a0 + atom * 16384 + off), sw128_desc(b0 + atom * 2048 + off),
+                 idesc16, k > 0 ? 1u : 0u);
+        }
+        tc_commit(&hfull);
+      };
+      // The head of tile i is issued as soon as its activations are staged:
+      // polled between the K steps of tile i + 1, or waited for at its end.
+      int pending = -1;
+      auto poll_head = [&]() {
+        if (HEAD && pending >= 0 && mbar_test(&a2full, (uint32_t)(pending & 1))) {
+          issue_head(pending);
+          pending = -1;
+        }
+      };
+      auto flush_head = [&]() {
+        if (HEAD && pending >= 0) {
+          if (!mbar_wait(&a2full, (uint32_t)(pending & 1), global_ns())) return false;
+          issue_head(pending);
+          pending = -1;
+        }
+        return true;
+      };
+      int64_t gk = 0;
+      int it = 0;
+      for (int mtile = first; mtile < mt && !aborted; mtile += step, ++it) {
+        const int b = it & 1;
+        if (it >= 2) {
+          bool okt = false;  // wait for buffer b, polling the pending head meanwhile
+          const uint64_t tw = global_ns();
+          while (true) {
+            poll_head();
+            if (mbar_test(&tempty[b], (uint32_t)(((it >> 1) - 1) & 1))) {
+              okt = true;
+              break;
+            }
+            if (global_ns() - tw > TC_WAIT_NS) break;
+          }
+          if (!okt) {
+            fail();
+            break;
+          }
+        }
+        tc_fence_after();
+        const uint32_t acc = tmem + (uint32_t)(b * TC_BN);
+        bool okk = true;
+        for (int kb = 0; kb < kt; ++kb, ++gk) {
+          const int slot = (int)(gk % STAGES);
+          if (!mbar_wait(&full[slot], (uint32_t)((gk / STAGES) & 1), global_ns())) {
+            okk = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t a0 = smem_u32(ring + slot * TC_STAGE_BYTES);
+          const uint32_t b0 = a0 + TC_A_BYTES;
+#pragma unroll
+          for (int k = 0; k < TC_BK / 16; ++k)
+            tc_mma(acc, sw128_desc(a0 + k * 32), sw128_desc(b0 + k * 32), idesc,
+                   (kb > 0 || k > 0) ? 1u : 0u);
+          tc_commit(&empty[slot]);
+          poll_head();
+        }
+        if (!okk) {
+          fail();
+          break;
+        }
+        tc_commit(&tfull[b]);
+        if (HEAD) {
+          if (!flush_head()) {  // the previous tile's head, if still pending
+            fail();
+            break;
+          }
+          pending = it;
+        }
+      }
+      if (HEAD && !aborted && !flush_head()) fail();
+    }
+    __syncwarp();
+  } else if (warp >= 4) {
+    // ---- epilogue (part 2)
+    const unsigned FULL = 0xffffffffu;
+    const int ew = warp - 4, lg = warp & 3, half = ew >> 2;
+    const int r = lg * 32 + lane;
+    // a bounded wait whose outcome the whole warp shares
+    auto wwait = [&](uint64_t* bar, uint32_t parity) {
+      const bool okw = mbar_wait(bar, parity, global_ns());
+      return __all_sync(FULL, okw ? 1 : 0) != 0;
+    };
+    int it = 0;
+    for (int mtile = first; mtile < mt; mtile += step, ++it) {
+      if (__any_sync(FULL, aborted)) break;
+      const int b = it & 1;
+      if (!wwait(&tfull[b], (uint32_t)((it >> 1) & 1))) {
+        fail();
+        break;
+      }
+      tc_fence_after();
+      const int row = mtile * TC_BM + r;
+      const uint32_t tl = tmem + (uint32_t)(b * TC_BN) + ((uint32_t)(lg * 32) << 16);
+#pragma unroll 1
+      for (int c = 0; c < TC_BN / 2; c += 32) {
+        const int col0 = half * (TC_BN / 2) + c;
+        uint32_t v[32];
+        tc_ld16_nowait(tl + (uint32_t)col0, v);
+        tc_ld16_nowait(tl + (uint32_t)col0 + 16u, v + 16);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+          const int col = col0 + 16 * hh, n = n0 + col;
+          float pv[16];
+          __align__(16) bf16 hb[16];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            pv[j] = __uint_as_float(v[16 * hh + j]) + bias_s[col + j];
+            hb[j] = __float2bfloat16_rn(gelu(pv[j]));
+          }
+          if (HEAD) {  // columns beyond N hold gelu(0) = 0
+            const int atom = col >> 6, ch = (col & 63) >> 3;
+            unsigned char* base = a2s + atom * 16384 + r * 128;
+            *reinterpret_cast<uint4*>(base + ((ch ^ (r & 7)) << 4)) =
+                reinterpret_cast<const uint4*>(hb)[0];
+            *reinterpret_cast<uint4*>(base + (((ch + 1) ^ (r & 7)) << 4)) =
+                reinterpret_cast<const uint4*>(hb)[1];
+          } else if (row < g.M && n < g.N) {
+            const int64_t o = (int64_t)row * g.N + n;
+            if (n + 16 <= g.N) {
+              uint4* dst = reinterpret_cast<uint4*>(g.outb + o);
+              dst[0] = reinterpret_cast<const uint4*>(hb)[0];
+              dst[1] = reinterpret_cast<const uint4*>(hb)[1];
+              if (g.pre) {
+                float4* pd = reinterpret_cast<float4*>(g.pre + o);
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                  pd[q] = make_float4(pv[4 * q], pv[4 * q + 1], pv[4 * q + 2], pv[4 * q + 3]);
+              }
+            } else {
+#pragma unroll
+              for (int j = 0; j < 16; ++j) {
+                if (n + j < g.N) {
+                  g.outb[o + j] = hb[j];
+                  if (g.pre) g.pre[o + j] = pv[j];
+                }
+              }
+            }
+          }
+        }
+      }
+      if (HEAD) {
+        fence_async_smem();  // the activation tile -> visible to the tensor cores
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&a2full);
+        if (!wwait(&hfull, (uint32_t)(it & 1))) {
+          fail();
+          break;
+        }
+        tc_fence_after();
+        if (half == 0) {
+          uint32_t y[16];
+          tc_ld16(tmem + (uint32_t)(b * TC_BN) + ((uint32_t)(lg * 32) << 16), y);
+          if (row < g.M) {
+            float* dst = h.ypart + ((int64_t)(blockIdx.x % nc) * g.M + row) * h.out;
+#pragma unroll
+            for (int o = 0; o < 16; ++o)
+              if (o < h.out) dst[o] = __uint_as_float(y[o]);
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[b]);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(2 * TC_TMEM_COLS)
+                 : "memory");
+  }
+}
+
 // y[r][o] = sum over column tiles t (in order) of ypart[t][r][o], plus b3[o].
 __global__ void k_head_combine(const float* __restrict__ ypart, int tiles, int64_t rows, int out,
                                const float* __restrict__ b3, float* __restrict__ y) {
@@ -1089,15 +1393,17 @@ void launch_gemm(const GemmArgs& ga, int splits, cudaStream_t s) {
   EVOC_CHECK_LAUNCH();
 }
 
-// Forward-layer kernel: tcgen05 with TMA loads (default); EVOC_MLP_GEMM=cpasync
-// selects tcgen05 with cp.async loads, EVOC_MLP_GEMM=mma the mma.sync kernel
-// (the cross-checks of the three paths).
-enum class FwdPath { kTma, kCpAsync, kMma };
+// Forward-layer kernel: the persistent warp-specialised tcgen05 kernel
+// (default, N <= 512); EVOC_MLP_GEMM=tma selects the one-tile-per-CTA TMA
+// kernel, cpasync the cp.async-fed one, mma the mma.sync kernel (the
+// cross-checks of the four paths).
+enum class FwdPath { kPersist, kTma, kCpAsync, kMma };
 FwdPath forward_path() {
   const char* e = std::getenv("EVOC_MLP_GEMM");
   if (e && std::strcmp(e, "mma") == 0) return FwdPath::kMma;
   if (e && std::strcmp(e, "cpasync") == 0) return FwdPath::kCpAsync;
-  return FwdPath::kTma;
+  if (e && std::strcmp(e, "tma") == 0) return FwdPath::kTma;
+  return FwdPath::kPersist;
 }
 bool use_tcgen05() { return forward_path() != FwdPath::kMma; }
 
@@ -1179,9 +1485,33 @@ void choose_splits_tc(int M, int N, int K, int num_sms, int* splits, int* kchunk
   *splits = std::max(1, (K + *kchunk - 1) / *kchunk);
 }
 
+// The persistent kernel: one CTA per SM (a multiple of the column tiles).
+template <int S, bool HEAD>
+void launch_persist(const GemmArgs& ga, const HeadArgs& ha, evoc_ctx* ctx) {
+  const int nc = (ga.N + TC_BN - 1) / TC_BN;
+  const int mt = (ga.M + TC_BM - 1) / TC_BM;
+  const int grid = nc * std::max(1, std::min(mt, ctx->num_sms / nc));
+  const int smem = ps_smem_bytes(S, HEAD);
+  const CUtensorMap ma = tmap_kmajor(ga.a, ga.M, ga.K, ga.lda, TC_BM);
+  const CUtensorMap mb = tmap_kmajor(ga.b, ga.N, ga.K, ga.ldb, TC_BN);
+  EVOC_CUDA(cudaFuncSetAttribute(k_gemm_persist<S, HEAD>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  k_gemm_persist<S, HEAD><<<grid, PS_THREADS, smem, ctx->stream>>>(ma, mb, ga, ha,
+                                                                   ctx->status.get());
+  EVOC_CHECK_LAUNCH();
+}
+
+bool use_persist(const GemmArgs& ga) {
+  return forward_path() == FwdPath::kPersist && ga.N <= 2 * TC_BN;
+}
+
 void launch_forward_gemm(const GemmArgs& ga, evoc_ctx* ctx) {
   if (!use_tcgen05()) {
     launch_gemm<true, true, EPI_BIAS_GELU>(ga, 1, ctx->stream);
+    return;
+  }
+  if (use_persist(ga)) {
+    launch_persist<4, false>(ga, HeadArgs{}, ctx);
     return;
   }
   const HeadArgs none{};
@@ -1193,6 +1523,10 @@ void launch_forward_gemm(const GemmArgs& ga, evoc_ctx* ctx) {
 
 // Second hidden layer fused with the output layer (inference on tcgen05).
 void launch_forward_head(const GemmArgs& ga, const HeadArgs& ha, evoc_ctx* ctx) {
+  if (use_persist(ga)) {
+    launch_persist<3, true>(ga, ha, ctx);
+    return;
+  }
   if (tc_stages() == 4)
     launch_tc<4, TC_HEAD>(ga, ha, ctx);
   else

@@ -75,19 +75,20 @@ def test_gradients_match_oracle(ctx, i, h, o, n):
         _close(got[name], want[name], name)
 
 
-@pytest.mark.parametrize("path", ["tma", "cpasync"])
+@pytest.mark.parametrize("path", ["persist", "tma", "cpasync"])
 @pytest.mark.parametrize("stages", ["2", "4"])
 @pytest.mark.parametrize("i,h,o,n", DIMS + [(128, 512, 8, 1000)])
 def test_tcgen05_forward_matches_mma_sync(ctx, i, h, o, n, stages, path, monkeypatch):
-    """The tcgen05 forward layers (TMA loads by default, or cp.async; the second
-    layer fused with the output layer) and the mma.sync kernels give the same
-    prediction up to FP32 accumulation order, and both match the oracle, for
-    either ring depth."""
+    """The tcgen05 forward layers (the persistent warp-specialised kernel by
+    default, the one-tile-per-CTA TMA kernel, or the cp.async-fed one; the
+    second layer fused with the output layer) and the mma.sync kernels give
+    the same prediction up to FP32 accumulation order, and both match the
+    oracle, for either ring depth of the non-persistent kernels."""
     net = _net(ctx, i, h, o)
     x, _ = _data(i, o, n, seed=8)
     monkeypatch.setenv("EVOC_TC_STAGES", stages)
-    if path == "cpasync":
-        monkeypatch.setenv("EVOC_MLP_GEMM", "cpasync")
+    if path != "persist":
+        monkeypatch.setenv("EVOC_MLP_GEMM", path)
     y_tc = net.predict(x)
     monkeypatch.setenv("EVOC_MLP_GEMM", "mma")
     y_mma = net.predict(x)
