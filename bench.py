@@ -597,7 +597,7 @@ def run_warm_start(args) -> dict:
         "gpu_launches": int(3 * chunks * (1 + args.c5_reps) + (chosen["epochs"] + 2 if chosen else 0)),
         "gpu_launches_note": "network forward (3 per 262,144-row chunk) and epoch loop of the "
                              "chosen warm run; fuzzy-set and set-up kernels not counted",
-        "roofline": {"bound": "tensor", "kernel": "k_gemm_tma (network forward, 1M rows)",
+        "roofline": {"bound": "tensor", "kernel": "k_gemm_persist (network forward, 1M rows)",
                      "achieved": round(tflops, 1), "peak": peak, "unit": "TFLOP/s",
                      "frac": round(tflops / peak, 4), "traffic": None,
                      "peak_src": "measured (cuBLAS bf16 burst)" if "hbm_gbs" in pk else "fallback",
@@ -607,10 +607,10 @@ def run_warm_start(args) -> dict:
 
 
 def run_mlp_forward(args) -> dict:
-    """The network's forward pass (two tcgen05 GEMM launches with TMA loads,
-    the output layer fused into the second, and one combine launch per 262,144
-    rows) over random unit-norm points, device-resident (value) and through
-    the host-buffer C ABI (e2e)."""
+    """The network's forward pass (two persistent tcgen05 GEMM launches with
+    TMA loads, the output layer fused into the second, and one combine launch
+    per 262,144 rows) over random unit-norm points, device-resident (value)
+    and through the host-buffer C ABI (e2e)."""
     import torch
     import evoc_gb300 as E
     torch.cuda.init()
@@ -665,7 +665,7 @@ def run_mlp_forward(args) -> dict:
                 "ms_per_step": round(e2e_ms, 3), "h2d_bytes_per_step": int(n * d * 4),
                 "d2h_bytes_per_step": int(n * dim * 4)},
         "gpu_launches": int(args.steps * 3 * chunks),
-        "roofline": {"bound": "tensor", "kernel": "k_gemm_tma", "achieved": round(tflops, 1),
+        "roofline": {"bound": "tensor", "kernel": "k_gemm_persist", "achieved": round(tflops, 1),
                      "peak": peak, "unit": "TFLOP/s", "frac": round(tflops / peak, 4),
                      "traffic": None,
                      "peak_src": "measured (cuBLAS bf16 burst)" if pk else "fallback"},
