@@ -56,6 +56,33 @@ __global__ void k_knn_offset(uint32_t* __restrict__ idx, int64_t total, int32_t 
   idx[e] = (uint32_t)(v + base);
 }
 
+// Self removal of a raw kNN search result (n rows of kr candidates that may
+// include the query itself): row i keeps its first k entries whose index is
+// not i, in order, and pads the rest with EVOC_KNN_PAD -- the reference's
+// filter(|j| j != i).take(k) (nearest_neighbour_gpu.rs:289-300), on the device.
+__global__ void k_knn_drop_self(const uint32_t* __restrict__ idx_raw,
+                                const float* __restrict__ dist_raw, int64_t n, int32_t kr,
+                                int32_t k, uint32_t* __restrict__ idx, float* __restrict__ dist) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t* ri = idx_raw + i * kr;
+  const float* rd = dist_raw + i * kr;
+  uint32_t* oi = idx + i * k;
+  float* od = dist + i * k;
+  int c = 0;
+  for (int j = 0; j < kr && c < k; ++j) {
+    const uint32_t v = ri[j];
+    if ((int64_t)v == i) continue;
+    oi[c] = v;
+    od[c] = rd[j];
+    ++c;
+  }
+  for (; c < k; ++c) {
+    oi[c] = EVOC_KNN_PAD;
+    od[c] = 0.0f;
+  }
+}
+
 std::vector<evoc::ProblemDesc> block_problems(const evoc_graph_t* g, int32_t m,
                                               const int64_t* n_per, const uint64_t* seeds) {
   if (!g || m <= 0 || !n_per || !seeds)
@@ -218,6 +245,35 @@ int evoc_fuzzy_set_device(evoc_ctx_t* ctx, const uint32_t* d_knn_idx,
   evoc::fuzzy_set_device(ctx, d_knn_idx, d_knn_dist, n, k,
                          effective_n_neighbours, symmetrise != 0, d_sigmas,
                          d_rhos, g.get());
+  evoc::check_status(ctx, "fuzzy set");
+  *out_graph = g.release();
+  EVOC_API_END(ctx)
+}
+
+int evoc_fuzzy_set_device_raw(evoc_ctx_t* ctx, const uint32_t* d_knn_idx_raw,
+                              const float* d_knn_dist_raw, int64_t n, int32_t k_raw,
+                              int32_t k, float effective_n_neighbours, int symmetrise,
+                              evoc_graph_t** out_graph) {
+  EVOC_API_BEGIN
+  if (!ctx || !out_graph)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "ctx or out_graph is NULL");
+  *out_graph = nullptr;
+  if (n < 0 || k < 1 || k_raw < k)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "need n >= 0 and 1 <= k <= k_raw");
+  if (n > 0 && (!d_knn_idx_raw || !d_knn_dist_raw))
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL kNN array");
+  use_device(ctx);
+  cudaStream_t s = ctx->stream;
+  evoc::DevBuf<uint32_t> idx((size_t)n * k, s);
+  evoc::DevBuf<float> dist((size_t)n * k, s);
+  if (n > 0) {
+    k_knn_drop_self<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(d_knn_idx_raw, d_knn_dist_raw, n,
+                                                               k_raw, k, idx.get(), dist.get());
+    EVOC_CHECK_LAUNCH();
+  }
+  std::unique_ptr<evoc_graph> g(new evoc_graph());
+  evoc::fuzzy_set_device(ctx, idx.get(), dist.get(), n, k, effective_n_neighbours,
+                         symmetrise != 0, nullptr, nullptr, g.get());
   evoc::check_status(ctx, "fuzzy set");
   *out_graph = g.release();
   EVOC_API_END(ctx)

@@ -50,7 +50,7 @@ EXPORTED = [
     "evoc_mlp_train_params_default", "evoc_mlp_create", "evoc_mlp_free",
     "evoc_mlp_n_params", "evoc_mlp_get_params", "evoc_mlp_set_params", "evoc_mlp_predict",
     "evoc_mlp_predict_device", "evoc_mlp_gradients", "evoc_mlp_fit_device",
-    "evoc_to_bf16_device", "evoc_procrustes",
+    "evoc_to_bf16_device", "evoc_procrustes", "evoc_fuzzy_set_device_raw",
 ]
 
 
@@ -154,6 +154,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "evoc_smooth_knn_dist": ([vp, vp, vp, i64, i32, u64, f32, i32, vp, vp], C.c_int),
         "evoc_fuzzy_set": ([vp, vp, vp, i64, i32, f32, C.c_int, pp], C.c_int),
         "evoc_fuzzy_set_device": ([vp, vp, vp, i64, i32, f32, C.c_int, vp, vp, pp], C.c_int),
+        "evoc_fuzzy_set_device_raw": ([vp, vp, vp, i64, i32, i32, f32, C.c_int, pp], C.c_int),
         "evoc_graph_from_csr": ([vp, vp, vp, vp, i64, pp], C.c_int),
         "evoc_graph_info": ([vp, C.POINTER(i64), C.POINTER(i64)], C.c_int),
         "evoc_graph_export": ([vp, vp, vp, vp], C.c_int),
@@ -495,6 +496,16 @@ class Context:
             float(effective_n_neighbours), int(bool(symmetrise)),
             C.c_void_p(d_sigmas) if d_sigmas else None,
             C.c_void_p(d_rhos) if d_rhos else None, C.byref(h)))
+        return Graph(self, h)
+
+    def fuzzy_set_device_raw(self, d_idx_raw: int, d_dist_raw: int, n: int, k_raw: int, k: int,
+                             effective_n_neighbours: float, symmetrise: bool = True) -> Graph:
+        """Fuzzy set from a raw device kNN result (k_raw candidates per row that may
+        include the query): self removed and the first k kept, on the device."""
+        h = C.c_void_p()
+        self._check(self.lib.evoc_fuzzy_set_device_raw(
+            self.handle, C.c_void_p(d_idx_raw), C.c_void_p(d_dist_raw), int(n), int(k_raw),
+            int(k), float(effective_n_neighbours), int(bool(symmetrise)), C.byref(h)))
         return Graph(self, h)
 
     def graph_from_csr(self, indptr, indices, weights) -> Graph:

@@ -145,6 +145,19 @@ EVOC_API int evoc_fuzzy_set_device(evoc_ctx_t* ctx, const uint32_t* d_knn_idx,
                           float* d_sigmas, float* d_rhos,
                           evoc_graph_t** out_graph);
 
+/* evoc_fuzzy_set_device on a raw device kNN search result that may include
+ * each query itself: n rows of k_raw candidates (for example the k + 1
+ * neighbours of a GPU self-query). Row i keeps its first k entries whose
+ * index is not i, in order, padding with EVOC_KNN_PAD -- the self removal of
+ * nearest_neighbour_gpu.rs:289-300, done on the device so the graph never
+ * makes the Vec<Vec<usize>> round trip through the host (lib.rs:218-246).
+ * Candidate rows that are padded must be padded at their ends. */
+EVOC_API int evoc_fuzzy_set_device_raw(evoc_ctx_t* ctx, const uint32_t* d_knn_idx_raw,
+                                       const float* d_knn_dist_raw, int64_t n,
+                                       int32_t k_raw, int32_t k,
+                                       float effective_n_neighbours, int symmetrise,
+                                       evoc_graph_t** out_graph);
+
 /* The fuzzy sets of n_problems independent kNN graphs in one pass: problem q
  * has n_per[q] rows of knn_idx[q] / knn_dist[q] (host, n_per[q] x k, indices
  * local to the problem, EVOC_KNN_PAD padding). The result is one

@@ -132,3 +132,52 @@ def test_fuzzy_large_properties(ctx):
     order = np.argsort(tkey)
     assert np.array_equal(tkey[order], key)
     assert np.array_equal(w[order].view(np.uint32), w.view(np.uint32))
+
+
+def _drop_self(raw_i, raw_d, k):
+    """The reference's self removal (nearest_neighbour_gpu.rs:289-300): row i
+    keeps its first k candidates that are not i; short rows are padded."""
+    n = raw_i.shape[0]
+    out_i = np.full((n, k), 0xFFFFFFFF, np.uint32)
+    out_d = np.zeros((n, k), np.float32)
+    for r in range(n):
+        keep = [j for j in range(raw_i.shape[1]) if raw_i[r, j] != r][:k]
+        out_i[r, :len(keep)] = raw_i[r, keep]
+        out_d[r, :len(keep)] = raw_d[r, keep]
+    return out_i, out_d
+
+
+def test_fuzzy_set_from_raw_device_knn(ctx, small_knn):
+    """A raw (k + 1)-wide device kNN result, the query itself at a random
+    position in most rows, some rows without it, some padded at the end:
+    removing self on the device gives the same graph as the host-side
+    removal followed by evoc_fuzzy_set."""
+    import torch
+    idx, dist, _ = small_knn
+    n, k = idx.shape
+    rng = np.random.default_rng(3)
+    raw_i = np.empty((n, k + 1), np.uint32)
+    raw_d = np.empty((n, k + 1), np.float32)
+    for r in range(n):
+        row_i, row_d = list(idx[r].astype(np.uint32)), list(dist[r])
+        if rng.random() < 0.9:
+            p = int(rng.integers(0, k + 1))
+            row_i.insert(p, r)
+            row_d.insert(p, 0.0)
+        else:
+            row_i.append(int(rng.integers(0, n)))
+            row_d.append(row_d[-1])
+        raw_i[r], raw_d[r] = row_i, row_d
+        if rng.random() < 0.05:  # a ragged candidate row
+            raw_i[r, -3:] = 0xFFFFFFFF
+    want_i, want_d = _drop_self(raw_i, raw_d, k)
+    ref = ctx.fuzzy_set(want_i, want_d, float(k), True)
+    di = torch.from_numpy(raw_i.view(np.int32)).cuda()
+    dd = torch.from_numpy(raw_d).cuda()
+    torch.cuda.synchronize()
+    g = ctx.fuzzy_set_device_raw(di.data_ptr(), dd.data_ptr(), n, k + 1, k, float(k), True)
+    for a, b in zip(g.export(), ref.export()):
+        np.testing.assert_array_equal(a, b)
+    import evoc_gb300 as E
+    with pytest.raises(E.EvocError):
+        ctx.fuzzy_set_device_raw(di.data_ptr(), dd.data_ptr(), n, k, k + 1, float(k), True)
