@@ -25,7 +25,7 @@ LIB = PKG / "libevoc_gb300.so"
 ORACLE_SRC = ROOT / "oracle" / "evoc_oracle.cpp"
 ORACLE_LIB = ROOT / "oracle" / "liboracle.so"
 
-SOURCES = ["primitives.cu", "fuzzy_set.cu", "embed.cu", "capi.cu", "noalloc.cu", "measure.cu", "mlp.cu"]
+SOURCES = ["primitives.cu", "fuzzy_set.cu", "embed.cu", "capi.cu", "noalloc.cu", "measure.cu", "mlp.cu", "label_prop.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",

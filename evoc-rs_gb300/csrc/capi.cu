@@ -615,6 +615,23 @@ int evoc_embed_batched(evoc_ctx_t* ctx, int32_t n_problems,
   EVOC_API_END(ctx)
 }
 
+// ---- label propagation partition -------------------------------------------
+
+int evoc_label_prop_partition(evoc_ctx_t* ctx, const evoc_graph_t* g, int64_t approx_n_parts,
+                              int32_t n_iter, uint64_t seed, uint32_t* partition,
+                              int64_t* n_parts) {
+  EVOC_API_BEGIN
+  if (!ctx || !g || !n_parts || (g->n > 0 && !partition))
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL argument");
+  use_device(ctx);
+  evoc::DevBuf<uint32_t> d((size_t)g->n, ctx->stream);
+  *n_parts = evoc::label_prop_partition(ctx, g, approx_n_parts, n_iter, seed, d.get());
+  if (g->n > 0)
+    EVOC_CUDA(cudaMemcpyAsync(partition, d.get(), d.bytes(), cudaMemcpyDeviceToHost, ctx->stream));
+  EVOC_CUDA(cudaStreamSynchronize(ctx->stream));
+  EVOC_API_END(ctx)
+}
+
 // ---- learned warm start ----------------------------------------------------
 
 void evoc_mlp_train_params_default(evoc_mlp_train_params_t* p) {

@@ -199,6 +199,12 @@ struct ProblemDesc {
   int64_t count = -1;
 };
 
+// ---- label_prop.cu ---------------------------------------------------------
+// Partition of g by label propagation (label_prop.rs:202-230) into
+// d_partition[n]; returns the number of parts.
+int64_t label_prop_partition(evoc_ctx* ctx, const evoc_graph* g, int64_t approx_n_parts,
+                             int32_t n_iter, uint64_t seed, uint32_t* d_partition);
+
 // ---- mlp.cu ----------------------------------------------------------------
 }  // namespace evoc
 

@@ -51,6 +51,7 @@ EXPORTED = [
     "evoc_mlp_n_params", "evoc_mlp_get_params", "evoc_mlp_set_params", "evoc_mlp_predict",
     "evoc_mlp_predict_device", "evoc_mlp_gradients", "evoc_mlp_fit_device",
     "evoc_to_bf16_device", "evoc_procrustes", "evoc_fuzzy_set_device_raw",
+    "evoc_label_prop_partition",
 ]
 
 
@@ -155,6 +156,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "evoc_fuzzy_set": ([vp, vp, vp, i64, i32, f32, C.c_int, pp], C.c_int),
         "evoc_fuzzy_set_device": ([vp, vp, vp, i64, i32, f32, C.c_int, vp, vp, pp], C.c_int),
         "evoc_fuzzy_set_device_raw": ([vp, vp, vp, i64, i32, i32, f32, C.c_int, pp], C.c_int),
+        "evoc_label_prop_partition": ([vp, vp, i64, i32, u64, vp, C.POINTER(i64)], C.c_int),
         "evoc_graph_from_csr": ([vp, vp, vp, vp, i64, pp], C.c_int),
         "evoc_graph_info": ([vp, C.POINTER(i64), C.POINTER(i64)], C.c_int),
         "evoc_graph_export": ([vp, vp, vp, vp], C.c_int),
@@ -399,6 +401,11 @@ class Mlp:
             pass
 
 
+def default_n_parts(n: int) -> int:
+    """label_propagation_init's part count (label_prop.rs:547-549)."""
+    return min(max(int(8.0 * np.sqrt(n)), 256), 16384, n)
+
+
 def procrustes(m, lib_path: str | None = None) -> np.ndarray:
     """evoc_procrustes: the orthogonal R maximising trace(R^T M) (host only)."""
     lib = load_library(lib_path)
@@ -507,6 +514,20 @@ class Context:
             self.handle, C.c_void_p(d_idx_raw), C.c_void_p(d_dist_raw), int(n), int(k_raw),
             int(k), float(effective_n_neighbours), int(bool(symmetrise)), C.byref(h)))
         return Graph(self, h)
+
+    def label_prop_partition(self, graph: Graph, approx_n_parts: int | None = None,
+                             n_iter: int = 20, seed: int = 42) -> tuple[np.ndarray, int]:
+        """label_prop_loop (label_prop.rs:202-230) on a device graph; the default
+        part count is label_propagation_init's clamp(8 sqrt(n), 256, 16384), <= n."""
+        n = graph.n
+        if approx_n_parts is None:
+            approx_n_parts = default_n_parts(n)
+        part = np.zeros(n, dtype=np.uint32)
+        k = C.c_int64()
+        self._check(self.lib.evoc_label_prop_partition(self.handle, graph.handle,
+                                                       int(approx_n_parts), int(n_iter),
+                                                       int(seed), _ptr(part), C.byref(k)))
+        return part, k.value
 
     def graph_from_csr(self, indptr, indices, weights) -> Graph:
         ip = np.ascontiguousarray(indptr, dtype=np.int64)

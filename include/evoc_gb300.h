@@ -328,6 +328,19 @@ EVOC_API int evoc_embed_batched(evoc_ctx_t* ctx, int32_t n_problems,
                        const float* const* inits, const uint64_t* seeds,
                        float* const* outs);
 
+/* ---- label propagation partition -------------------------------------------
+ * label_prop_loop (src/graph/label_prop.rs:202-230), the partition step of
+ * label_propagation_init (:537-564): approx_n_parts seed nodes (default
+ * clamp(8 sqrt(n), 256, 16384), at most n), n_iter conservative propagation
+ * rounds (default 20; :45-92), the sequential mop-up of unlabelled nodes
+ * (:105-142) and the remap to 0..n_parts (:155-180). partition (host, n)
+ * receives each node's part; *n_parts the number of parts. Vote sums are the
+ * reference's f32 additions in row order; the seed and fallback draws come
+ * from Philox4x32-10 instead of rand::SmallRng. */
+EVOC_API int evoc_label_prop_partition(evoc_ctx_t* ctx, const evoc_graph_t* g,
+                                       int64_t approx_n_parts, int32_t n_iter, uint64_t seed,
+                                       uint32_t* partition, int64_t* n_parts);
+
 /* ---- learned warm start ----------------------------------------------------
  * No counterpart in the reference: a multilayer perceptron
  *   in_dim -> hidden -> GELU -> hidden -> GELU -> out_dim

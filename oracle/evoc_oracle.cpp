@@ -12,6 +12,10 @@
 //   build_fuzzy_simplicial_set src/graph/fuzzy_graph.rs:275-295
 //   evoc_embedding             src/graph/embedding.rs:48-298
 //   EvocEmbeddingParams        src/graph/mod.rs:22-67
+//   label_prop_iteration       src/graph/label_prop.rs:45-92
+//   label_outliers             src/graph/label_prop.rs:105-142
+//   remap_labels               src/graph/label_prop.rs:155-180
+//   label_prop_loop            src/graph/label_prop.rs:202-230
 // with the same parallel decomposition as the reference's rayon code
 // (parallel rows in smooth_knn_dist, serial knn_to_coo and hash inserts,
 // parallel per-row union, parallel nodes / nodes / edges in the three epoch
@@ -651,6 +655,128 @@ int oracle_evoc_embedding(const int64_t* indptr, const uint32_t* indices,
   }
   std::memcpy(out, embd.data(), n * D * sizeof(float));
   return 0;
+}
+
+
+// ---------------------------------------------------------------------------
+// Label propagation partition (label_prop.rs:45-230). Labels are int64 as in
+// the reference; -1 is "unlabelled". The seed draws (label_prop.rs:216-219)
+// and the outlier fallback draws (:138-140) come from Philox4x32-10 instead of
+// rand::SmallRng (the counters below; the CUDA library uses the same ones).
+// ---------------------------------------------------------------------------
+static uint32_t lp_seed_draw(uint64_t seed, uint32_t i, uint32_t n) {
+  const uint32_t ctr[4] = {i, 0u, 0x4C50u, 0x53454544u};
+  const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  uint32_t o[4];
+  philox4x32_10(ctr, key, o);
+  return (uint32_t)(((uint64_t)o[0] * (uint64_t)n) >> 32);
+}
+static uint32_t lp_outlier_draw(uint64_t seed, uint64_t i, uint32_t range) {
+  const uint32_t ctr[4] = {(uint32_t)i, (uint32_t)(i >> 32), 0x4C50u, 0x4F555431u};
+  const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  uint32_t o[4];
+  philox4x32_10(ctr, key, o);
+  return (uint32_t)(((uint64_t)o[0] * (uint64_t)range) >> 32);
+}
+
+// label_prop.rs:45-92: one conservative iteration, parallel over nodes.
+void oracle_lp_iteration(const int64_t* indptr, const uint32_t* indices, const float* w,
+                         int64_t n, const int64_t* in, int64_t* out) {
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t i = 0; i < n; ++i) {
+    if (in[i] >= 0) {
+      out[i] = in[i];
+      continue;
+    }
+    std::vector<std::pair<int64_t, float>> votes;  // first-appearance order
+    for (int64_t e = indptr[i]; e < indptr[i + 1]; ++e) {
+      const int64_t l = in[indices[e]];
+      bool hit = false;
+      for (auto& v : votes)
+        if (v.first == l) {
+          v.second += w[e];
+          hit = true;
+          break;
+        }
+      if (!hit) votes.emplace_back(l, w[e]);
+    }
+    int64_t best = -1;
+    float max_vote = 1.0f;  // threshold
+    for (const auto& v : votes) {
+      if (v.first < 0) continue;
+      if (v.second > max_vote) {
+        max_vote = v.second;
+        best = v.first;
+      } else if (v.second == max_vote) {
+        best = v.first;  // last encountered wins
+      }
+    }
+    out[i] = best;
+  }
+}
+
+// label_prop.rs:105-142: sequential mop-up, a LIFO walk of at most 64 pops per
+// unlabelled node, then a random existing label.
+void oracle_lp_outliers(const int64_t* indptr, const uint32_t* indices, int64_t n,
+                        int64_t* labels, uint64_t seed) {
+  int64_t max_label = -1;
+  for (int64_t i = 0; i < n; ++i) max_label = std::max(max_label, labels[i]);
+  if (max_label < 0) return;
+  std::vector<uint32_t> queue;
+  for (int64_t i = 0; i < n; ++i) {
+    if (labels[i] >= 0) continue;
+    queue.assign(1, (uint32_t)i);
+    bool found = false;
+    for (int step = 0; step < 64 && !found; ++step) {
+      if (queue.empty()) break;
+      const uint32_t node = queue.back();
+      queue.pop_back();
+      for (int64_t e = indptr[node]; e < indptr[node + 1]; ++e) {
+        const uint32_t j = indices[e];
+        if (labels[j] >= 0) {
+          labels[i] = labels[j];
+          found = true;
+          break;
+        }
+        queue.push_back(j);
+      }
+    }
+    if (!found) labels[i] = (int64_t)lp_outlier_draw(seed, (uint64_t)i, (uint32_t)(max_label + 1));
+  }
+}
+
+// label_prop.rs:155-180: labels >= 0 to 0..n_unique in sorted order; each -1
+// gets the next new id in node order. Returns the number of labels.
+int64_t oracle_lp_remap(int64_t* labels, int64_t n) {
+  std::vector<int64_t> sorted;
+  for (int64_t i = 0; i < n; ++i)
+    if (labels[i] >= 0) sorted.push_back(labels[i]);
+  std::sort(sorted.begin(), sorted.end());
+  sorted.erase(std::unique(sorted.begin(), sorted.end()), sorted.end());
+  int64_t next = (int64_t)sorted.size();
+  for (int64_t i = 0; i < n; ++i) {
+    if (labels[i] < 0)
+      labels[i] = next++;
+    else
+      labels[i] = std::lower_bound(sorted.begin(), sorted.end(), labels[i]) - sorted.begin();
+  }
+  return next;
+}
+
+// label_prop.rs:202-230: seed, iterate, mop up, remap.
+int64_t oracle_lp_partition(const int64_t* indptr, const uint32_t* indices, const float* w,
+                            int64_t n, int64_t approx_n_parts, int32_t n_iter, uint64_t seed,
+                            uint32_t* partition) {
+  std::vector<int64_t> a((size_t)n, -1), b((size_t)n, -1);
+  for (int64_t i = 0; i < approx_n_parts; ++i) a[lp_seed_draw(seed, (uint32_t)i, (uint32_t)n)] = i;
+  for (int32_t it = 0; it < n_iter; ++it) {
+    oracle_lp_iteration(indptr, indices, w, n, a.data(), b.data());
+    a.swap(b);
+  }
+  oracle_lp_outliers(indptr, indices, n, a.data(), seed + 2000);
+  const int64_t parts = oracle_lp_remap(a.data(), n);
+  for (int64_t i = 0; i < n; ++i) partition[i] = (uint32_t)a[i];
+  return parts;
 }
 
 }  // extern "C"

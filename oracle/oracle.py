@@ -62,6 +62,10 @@ def lib() -> C.CDLL:
             "oracle_graph_free": ([vp], None),
             "oracle_evoc_embedding": ([vp, vp, vp, i64, i32, C.POINTER(OracleParams), vp, u64,
                                        i32, i32, vp, vp, vp, vp], C.c_int),
+            "oracle_lp_iteration": ([vp, vp, vp, i64, vp, vp], None),
+            "oracle_lp_outliers": ([vp, vp, i64, vp, u64], None),
+            "oracle_lp_remap": ([vp, i64], i64),
+            "oracle_lp_partition": ([vp, vp, vp, i64, i64, i32, u64, vp], i64),
         }
         for k, (a, r) in sigs.items():
             f = getattr(L, k)
@@ -198,3 +202,42 @@ def evoc_embedding(indptr, indices, weights, dim: int, n_epochs: int = 50,
     if want_times:
         res.append(times[:n_epochs])
     return res[0] if len(res) == 1 else tuple(res)
+
+
+# ---- label propagation partition (label_prop.rs:45-230) ---------------------
+def _csr(indptr, indices, weights=None):
+    ip = np.ascontiguousarray(indptr, dtype=np.int64)
+    ix = np.ascontiguousarray(indices, dtype=np.uint32)
+    w = None if weights is None else np.ascontiguousarray(weights, dtype=np.float32)
+    return ip, ix, w
+
+
+def lp_iteration(indptr, indices, weights, labels) -> np.ndarray:
+    ip, ix, w = _csr(indptr, indices, weights)
+    lab = np.ascontiguousarray(labels, dtype=np.int64)
+    out = np.empty_like(lab)
+    lib().oracle_lp_iteration(_p(ip), _p(ix), _p(w), len(ip) - 1, _p(lab), _p(out))
+    return out
+
+
+def lp_outliers(indptr, indices, labels, seed: int) -> np.ndarray:
+    ip, ix, _ = _csr(indptr, indices)
+    lab = np.array(labels, dtype=np.int64)
+    lib().oracle_lp_outliers(_p(ip), _p(ix), len(ip) - 1, _p(lab), seed)
+    return lab
+
+
+def lp_remap(labels) -> tuple[np.ndarray, int]:
+    lab = np.array(labels, dtype=np.int64)
+    k = lib().oracle_lp_remap(_p(lab), len(lab))
+    return lab, int(k)
+
+
+def lp_partition(indptr, indices, weights, approx_n_parts: int, n_iter: int = 20,
+                 seed: int = 42) -> tuple[np.ndarray, int]:
+    ip, ix, w = _csr(indptr, indices, weights)
+    n = len(ip) - 1
+    part = np.zeros(n, dtype=np.uint32)
+    k = lib().oracle_lp_partition(_p(ip), _p(ix), _p(w), n, approx_n_parts, n_iter, seed,
+                                  _p(part))
+    return part, int(k)
