@@ -70,6 +70,8 @@ WORKLOADS = {
     # n = points of the fresh evaluation instance
     "warm_start_c5": dict(n=1_000_000, d=768, k=30, dim=8, seed=777, hidden=512,
                           train_n=2_000_000, train_instances=20, train_seed=100),
+    # the label-propagation partition of the 2M graph (label_prop.rs:202-230)
+    "label_prop_2m": dict(n=2_000_000, d=768, k=30, dim=8, seed=2),
     # the warm-start network's forward pass alone (n = rows)
     "mlp_forward": dict(n=1_000_000, d=768, k=0, dim=8, seed=777, hidden=512),
 }
@@ -673,6 +675,56 @@ def run_mlp_forward(args) -> dict:
     }
 
 
+def run_label_prop(args) -> dict:
+    """The partition step of the label-propagation initialisation on the 2M
+    graph (default part count clamp(8 sqrt(n), 256, 16384), 20 rounds), through
+    the C ABI from the device graph; the oracle's CPU partition of the same
+    graph beside it (OpenMP rounds, sequential mop-up), and the two compared."""
+    import torch
+    import evoc_gb300 as E
+    import oracle as O
+    torch.cuda.init()
+    cfg, idx32, dist = make_workload("hierarchical_2m", args.n)
+    n, k = cfg["n"], cfg["k"]
+    ctx = E.Context(0)
+    g = ctx.fuzzy_set_device(idx32.data_ptr(), dist.data_ptr(), n, k, float(k), True)
+    parts = E.default_n_parts(n)
+    for _ in range(args.warmup):
+        part, n_parts = ctx.label_prop_partition(g, parts, 20, cfg["seed"])
+    ts = []
+    with ClockSampler() as clk:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            part, n_parts = ctx.label_prop_partition(g, parts, 20, cfg["seed"])
+            ts.append(time.perf_counter() - t)
+    ms = float(np.median(ts)) * 1e3
+    ip, ix, w = g.export()
+    t = time.perf_counter()
+    want, want_parts = O.lp_partition(ip, ix, w, parts, 20, cfg["seed"])
+    cpu_s = time.perf_counter() - t
+    same = bool(np.array_equal(part, want) and n_parts == want_parts)
+    g.free()
+    ctx.close()
+    return {
+        "metric": "label-propagation partition time at 2M pts (20 rounds)", "value": ms,
+        "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms, 3), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 votes, int32 labels",
+        "data": "synthetic (seeded, no dataset)",
+        "config": {"workload": "label_prop_2m", "n": n, "k": k, "nnz": int(len(ix)),
+                   "approx_n_parts": parts, "n_parts": int(n_parts), "rounds": 20,
+                   "time": "wall clock, synchronised, median of steps; from the device graph to "
+                           "the partition in host memory"},
+        "matches_oracle": same,
+        "cpu_baseline": {"value": round(cpu_s * 1e3, 1), "unit": "ms",
+                         "cores": O.max_threads(), "kind": "port",
+                         "sample": "the whole partition of the same graph (the oracle: OpenMP "
+                                   "rounds, sequential mop-up)"},
+        "clocks": clk.summary(),
+    }
+
+
 def run_reference(args) -> dict:
     """The reference's CPU path (the C++ restatement; Rust is not available)
     on the same workload: each step is one epoch of the embedding loop
@@ -758,6 +810,9 @@ def main() -> None:
         return
     if args.workload == "mlp_forward":
         print(json.dumps(run_mlp_forward(args)))
+        return
+    if args.workload == "label_prop_2m":
+        print(json.dumps(run_label_prop(args)))
         return
     print(json.dumps(run_batched(args) if args.workload == "batch_c4" else run_ours(args)))
 
