@@ -7,9 +7,10 @@
 //             node sums its neighbours' weights per label in row order, and
 //             adopts the label with the largest total if that total is at
 //             least 1.0 (ties: the label that first appears last);
-//   mop up    unlabelled nodes, in node order, walk a LIFO stack of at most
-//             64 pops for a labelled node, else take a random existing label
-//             (label_prop.rs:105-142);
+//   mop up    unlabelled nodes walk a LIFO stack of at most 64 pops for a
+//             labelled node, else take a random existing label
+//             (label_prop.rs:105-142); the reference's sequential order is
+//             kept by resolving walks that meet earlier outliers afterwards;
 //   remap     labels to 0..n_parts in sorted order, any -1 to new ids in
 //             node order (label_prop.rs:155-180).
 //
@@ -107,36 +108,65 @@ __global__ void k_lp_list(const int32_t* __restrict__ unl, const int64_t* __rest
   if (i < n && unl[i]) list[pos[i]] = (uint32_t)i;
 }
 
-// The sequential mop-up: one thread, unlabelled nodes in node order. Each
-// walk pops at most 64 nodes and pushes at most max_degree per pop, so the
-// stack (1 + 64 max_degree entries) cannot overflow.
-__global__ void k_lp_outliers(const int64_t* __restrict__ indptr,
-                              const uint32_t* __restrict__ indices, int32_t* __restrict__ labels,
-                              const uint32_t* __restrict__ list, int64_t count,
-                              const int32_t* __restrict__ mx, uint64_t seed,
-                              uint32_t* __restrict__ stack) {
-  if (blockIdx.x != 0 || threadIdx.x != 0) return;
-  const int32_t max_label = *mx;
-  if (max_label < 0) return;
-  for (int64_t u = 0; u < count; ++u) {
-    const uint32_t i = list[u];
-    int64_t top = 0;
-    stack[top++] = i;
-    bool found = false;
-    for (int step = 0; step < 64 && !found && top > 0; ++step) {
-      const uint32_t node = stack[--top];
-      for (int64_t q = indptr[node]; q < indptr[node + 1]; ++q) {
-        const uint32_t j = indices[q];
-        if (labels[j] >= 0) {
-          labels[i] = labels[j];
-          found = true;
-          break;
-        }
-        stack[top++] = j;
+// The mop-up (label_prop.rs:105-142) in parallel. In the reference's
+// sequential order, outlier i's walk stops at the first node that is labelled
+// by then: a node labelled before the mop-up, or an earlier outlier j < i
+// (every processed outlier has a label). So each walk runs against the
+// labels before the mop-up and yields a label, a pointer to an earlier
+// outlier (-2 - its list index), or the fallback draw; k_lp_jump then
+// resolves the pointers. A walk pops at most 64 nodes, so only the top 64
+// stack entries can ever be popped: the stack is a 64-entry ring that drops
+// its bottom entry when full.
+__global__ void k_lp_walk(const int64_t* __restrict__ indptr, const uint32_t* __restrict__ indices,
+                          const int32_t* __restrict__ labels, const int32_t* __restrict__ unl,
+                          const int64_t* __restrict__ pos, const uint32_t* __restrict__ list,
+                          int64_t count, int32_t max_label, uint64_t seed,
+                          int32_t* __restrict__ res) {
+  const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= count) return;
+  const uint32_t i = list[u];
+  uint32_t ring[64];
+  int64_t top = 0, bottom = 0;  // entries [bottom, top), slot = index % 64
+  ring[0] = i;
+  top = 1;
+  for (int step = 0; step < 64 && top > bottom; ++step) {
+    --top;
+    const uint32_t node = ring[top & 63];
+    for (int64_t q = indptr[node]; q < indptr[node + 1]; ++q) {
+      const uint32_t j = indices[q];
+      const int32_t l = labels[j];
+      if (l >= 0) {
+        res[u] = l;
+        return;
       }
+      if (unl[j] && j < i) {  // an earlier outlier: labelled by then
+        res[u] = (int32_t)(-2 - pos[j]);
+        return;
+      }
+      ring[top & 63] = j;
+      ++top;
+      if (top - bottom > 64) ++bottom;
     }
-    if (!found) labels[i] = (int32_t)lp_outlier_draw(seed, i, (uint32_t)max_label + 1u);
   }
+  res[u] = (int32_t)lp_outlier_draw(seed, i, (uint32_t)max_label + 1u);
+}
+
+// Pointer jumping over the walk results; pointers only go to earlier
+// outliers, so the chains end.
+__global__ void k_lp_jump(int32_t* __restrict__ res, int64_t count, int32_t* __restrict__ changed) {
+  const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= count) return;
+  const int32_t r = res[u];
+  if (r >= 0) return;
+  const int32_t rk = res[-2 - (int64_t)r];
+  res[u] = rk;
+  *changed = 1;
+}
+
+__global__ void k_lp_assign(const uint32_t* __restrict__ list, const int32_t* __restrict__ res,
+                            int64_t count, int32_t* __restrict__ labels) {
+  const int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (u < count) labels[list[u]] = res[u];
 }
 
 __global__ void k_lp_present(const int32_t* __restrict__ labels, int64_t n,
@@ -155,12 +185,6 @@ __global__ void k_lp_remap(const int32_t* __restrict__ labels, int64_t n,
   if (i >= n) return;
   const int32_t l = labels[i];
   part[i] = (uint32_t)(l >= 0 ? newid[l] : n_unique + negrank[i]);
-}
-
-__global__ void k_lp_maxdeg(const int64_t* __restrict__ indptr, int64_t n,
-                            unsigned long long* __restrict__ mx) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) atomicMax(mx, (unsigned long long)(indptr[i + 1] - indptr[i]));
 }
 
 inline unsigned grid_for(int64_t n, int t = 256) { return (unsigned)((n + t - 1) / t); }
@@ -205,17 +229,27 @@ int64_t label_prop_partition(evoc_ctx* ctx, const evoc_graph* g, int64_t approx_
   int64_t count = 0;
   EVOC_CUDA(cudaMemcpyAsync(&count, pos.get() + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
   EVOC_CUDA(cudaStreamSynchronize(s));
-  if (count > 0) {
-    DevBuf<unsigned long long> md(1, s);
-    EVOC_CUDA(cudaMemsetAsync(md.get(), 0, sizeof(unsigned long long), s));
-    k_lp_maxdeg<<<grid_for(n), 256, 0, s>>>(g->indptr.get(), n, md.get());
-    unsigned long long maxdeg = 0;
-    EVOC_CUDA(cudaMemcpyAsync(&maxdeg, md.get(), sizeof(maxdeg), cudaMemcpyDeviceToHost, s));
-    EVOC_CUDA(cudaStreamSynchronize(s));
-    DevBuf<uint32_t> list(count, s), stack(1 + 64 * (size_t)maxdeg, s);
+  int32_t max_label = -1;
+  EVOC_CUDA(cudaMemcpyAsync(&max_label, mx.get(), sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  EVOC_CUDA(cudaStreamSynchronize(s));
+  if (count > 0 && max_label >= 0) {
+    DevBuf<uint32_t> list(count, s);
+    DevBuf<int32_t> res(count, s);
     k_lp_list<<<grid_for(n), 256, 0, s>>>(unl.get(), pos.get(), n, list.get());
-    k_lp_outliers<<<1, 32, 0, s>>>(g->indptr.get(), g->indices.get(), la.get(), list.get(), count,
-                                   mx.get(), seed + 2000, stack.get());
+    k_lp_walk<<<grid_for(count, 128), 128, 0, s>>>(g->indptr.get(), g->indices.get(), la.get(),
+                                                   unl.get(), pos.get(), list.get(), count,
+                                                   max_label, seed + 2000, res.get());
+    EVOC_CHECK_LAUNCH();
+    for (int pass = 0; pass < 64; ++pass) {  // chains halve per pass
+      EVOC_CUDA(cudaMemsetAsync(flag.get(), 0, sizeof(int32_t), s));
+      k_lp_jump<<<grid_for(count), 256, 0, s>>>(res.get(), count, flag.get());
+      EVOC_CHECK_LAUNCH();
+      int32_t h = 0;
+      EVOC_CUDA(cudaMemcpyAsync(&h, flag.get(), sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+      EVOC_CUDA(cudaStreamSynchronize(s));
+      if (!h) break;
+    }
+    k_lp_assign<<<grid_for(count), 256, 0, s>>>(list.get(), res.get(), count, la.get());
     EVOC_CHECK_LAUNCH();
   }
   // remap: labels are below approx_n_parts, or -1 if nothing was labelled
