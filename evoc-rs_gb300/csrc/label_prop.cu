@@ -19,7 +19,8 @@
 // come from Philox4x32-10 (counters below) instead of rand::SmallRng. Each
 // node keeps its vote table in its own CSR row range of a scratch array
 // (a row has at most as many distinct labels as entries), so no node can
-// overflow it.
+// overflow it; rows longer than 64 also get a hash index (at most half full)
+// in four entries per row of two more scratch arrays.
 #include "evoc_internal.h"
 #include "evoc_device.cuh"
 
@@ -52,10 +53,15 @@ __global__ void k_lp_seed(int32_t* __restrict__ labels, int64_t n, int64_t parts
 }
 
 // One conservative iteration, thread per node.
+// Rows up to this degree search their vote table linearly; longer rows (hubs)
+// index it through a hash table, so a vote costs O(1) instead of O(distinct).
+constexpr int64_t LP_LINEAR_DEG = 64;
+
 __global__ void k_lp_iter(const int64_t* __restrict__ indptr, const uint32_t* __restrict__ indices,
                           const float* __restrict__ w, int64_t n, const int32_t* __restrict__ in,
                           int32_t* __restrict__ out, int32_t* __restrict__ vlab,
-                          float* __restrict__ vsum, int32_t* __restrict__ changed) {
+                          float* __restrict__ vsum, int32_t* __restrict__ hkey,
+                          int32_t* __restrict__ hpos, int32_t* __restrict__ changed) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int32_t cur = in[i];
@@ -63,19 +69,46 @@ __global__ void k_lp_iter(const int64_t* __restrict__ indptr, const uint32_t* __
     out[i] = cur;
     return;
   }
-  const int64_t b = indptr[i], e = indptr[i + 1];
+  const int64_t b = indptr[i], e = indptr[i + 1], deg = e - b;
   int64_t cnt = 0;  // distinct labelled labels, in first-appearance order
-  for (int64_t q = b; q < e; ++q) {
-    const int32_t l = in[indices[q]];
-    if (l < 0) continue;  // unlabelled votes never win
-    int64_t k = 0;
-    while (k < cnt && vlab[b + k] != l) ++k;
-    if (k < cnt) {
-      vsum[b + k] = __fadd_rn(vsum[b + k], w[q]);
-    } else {
-      vlab[b + cnt] = l;
-      vsum[b + cnt] = w[q];
-      ++cnt;
+  if (deg <= LP_LINEAR_DEG) {
+    for (int64_t q = b; q < e; ++q) {
+      const int32_t l = in[indices[q]];
+      if (l < 0) continue;  // unlabelled votes never win
+      int64_t k = 0;
+      while (k < cnt && vlab[b + k] != l) ++k;
+      if (k < cnt) {
+        vsum[b + k] = __fadd_rn(vsum[b + k], w[q]);
+      } else {
+        vlab[b + cnt] = l;
+        vsum[b + cnt] = w[q];
+        ++cnt;
+      }
+    }
+  } else {
+    // long row: an open-addressing table (label -> position in vlab/vsum) in
+    // the row's range [4b, 4e) of hkey/hpos, at most half full
+    int64_t cap = 1;
+    while (cap < 2 * deg) cap <<= 1;
+    int32_t* key = hkey + 4 * b;
+    int32_t* hp = hpos + 4 * b;
+    for (int64_t h = 0; h < cap; ++h) key[h] = -1;
+    const int64_t mask = cap - 1;
+    for (int64_t q = b; q < e; ++q) {
+      const int32_t l = in[indices[q]];
+      if (l < 0) continue;
+      int64_t h = (int64_t)(((uint32_t)l * 2654435761u) & (uint32_t)mask);
+      while (key[h] != -1 && key[h] != l) h = (h + 1) & mask;
+      if (key[h] == l) {
+        const int64_t k = hp[h];
+        vsum[b + k] = __fadd_rn(vsum[b + k], w[q]);
+      } else {
+        key[h] = l;
+        hp[h] = (int32_t)cnt;
+        vlab[b + cnt] = l;
+        vsum[b + cnt] = w[q];
+        ++cnt;
+      }
     }
   }
   int32_t best = -1;
@@ -201,6 +234,7 @@ int64_t label_prop_partition(evoc_ctx* ctx, const evoc_graph* g, int64_t approx_
   if (n_iter < 0) throw Error(EVOC_ERR_INVALID_ARGUMENT, "n_iter < 0");
   DevBuf<int32_t> la(n, s), lb(n, s), vlab(std::max<int64_t>(nnz, 1), s), flag(1, s);
   DevBuf<float> vsum(std::max<int64_t>(nnz, 1), s);
+  DevBuf<int32_t> hkey(std::max<int64_t>(4 * nnz, 1), s), hpos(std::max<int64_t>(4 * nnz, 1), s);
   k_lp_fill<<<grid_for(n), 256, 0, s>>>(la.get(), n);
   if (approx_n_parts > 0)
     k_lp_seed<<<grid_for(approx_n_parts), 256, 0, s>>>(la.get(), n, approx_n_parts, seed);
@@ -211,7 +245,8 @@ int64_t label_prop_partition(evoc_ctx* ctx, const evoc_graph* g, int64_t approx_
     EVOC_CUDA(cudaMemsetAsync(flag.get(), 0, sizeof(int32_t), s));
     k_lp_iter<<<grid_for(n, 128), 128, 0, s>>>(g->indptr.get(), g->indices.get(),
                                                g->weights.get(), n, la.get(), lb.get(),
-                                               vlab.get(), vsum.get(), flag.get());
+                                               vlab.get(), vsum.get(), hkey.get(), hpos.get(),
+                                               flag.get());
     EVOC_CHECK_LAUNCH();
     std::swap(la, lb);
     int32_t h = 0;

@@ -43,3 +43,19 @@ def test_isolated_nodes_and_no_seeds(ctx):
     _check(ctx, g, 2, 5, 7)
     part, k = _check(ctx, g, 0, 5, 7)
     assert k == 6 and sorted(part) == list(range(6))
+
+
+def test_hub_rows_use_the_hashed_table(ctx):
+    """A hub joined to every other node (degree 399, above the linear-search
+    limit of 64) among ring-linked leaves: identical to the oracle."""
+    n = 400
+    rng = np.random.default_rng(11)
+    hub_w = rng.uniform(0.3, 1.0, n - 1).astype(np.float32)
+    adj = [[(j, float(hub_w[j - 1])) for j in range(1, n)]]
+    for i in range(1, n):
+        nb = {0: float(hub_w[i - 1]), 1 + (i % (n - 1)): 1.0, 1 + ((i - 2) % (n - 1)): 1.0}
+        nb.pop(i, None)
+        adj.append(sorted(nb.items()))
+    g = ctx.graph_from_adjacency(adj)
+    for parts, rounds, seed in ((40, 3, 5), (150, 20, 9), (400, 1, 2)):
+        _check(ctx, g, parts, rounds, seed)
