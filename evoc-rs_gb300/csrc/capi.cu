@@ -745,6 +745,15 @@ int evoc_to_bf16_device(evoc_ctx_t* ctx, const float* d_in, int64_t count, uint1
   EVOC_API_END(ctx)
 }
 
+int evoc_selftest_wait_timeout(evoc_ctx_t* ctx, int32_t limit_ms) {
+  EVOC_API_BEGIN
+  if (!ctx || limit_ms < 1 || limit_ms > 2000)
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "limit_ms outside [1, 2000]");
+  use_device(ctx);
+  evoc::wait_timeout_selftest(ctx, limit_ms);
+  EVOC_API_END(ctx)
+}
+
 int evoc_procrustes(const double* m, int32_t d, double* r) {
   evoc_ctx* ctx = nullptr;
   EVOC_API_BEGIN

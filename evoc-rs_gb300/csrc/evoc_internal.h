@@ -227,6 +227,9 @@ void mlp_fit_device(evoc_mlp* net, int32_t m, const uint16_t* const* xs,
                     const evoc_mlp_train_params_t* p, float* loss_history);
 void to_bf16_device(evoc_ctx* ctx, const float* x, int64_t count, uint16_t* y);
 void procrustes(const double* m, int d, double* r);
+// Runs a kernel whose bounded wait cannot be satisfied; throws the
+// ST_WAIT_TIMEOUT error after limit_ms.
+void wait_timeout_selftest(evoc_ctx* ctx, int32_t limit_ms);
 }  // namespace evoc
 
 struct evoc_plan;  // defined in embed.cu

@@ -341,8 +341,10 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
                : "memory");
 }
-// Wait for the completion of the phase with the given parity; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t t0) {
+// Wait for the completion of the phase with the given parity; false once
+// limit_ns have passed since t0.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64_t t0,
+                                          uint64_t limit_ns = TC_WAIT_NS) {
   const uint32_t a = smem_u32(bar);
   while (true) {
     uint32_t done;
@@ -354,7 +356,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64
         : "r"(a), "r"(parity)
         : "memory");
     if (done) return true;
-    if (global_ns() - t0 > TC_WAIT_NS) return false;
+    if (global_ns() - t0 > limit_ns) return false;
   }
 }
 // Non-blocking: has the phase with the given parity completed?
@@ -1141,6 +1143,18 @@ __global__ void __launch_bounds__(PS_THREADS, 1)
   }
 }
 
+// Self-test of the timeout path: every thread waits on an mbarrier that
+// nothing arrives on, gives up after limit_ns, and the block records
+// ST_WAIT_TIMEOUT, as a tcgen05 kernel whose wait expired would.
+__global__ void k_wait_probe(int32_t* __restrict__ status, uint64_t limit_ns) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) mbar_init(&bar, 1);
+  __syncthreads();
+  const bool ok = mbar_wait(&bar, 0u, global_ns(), limit_ns);
+  if (!__syncthreads_and(ok ? 1 : 0) && threadIdx.x == 0)
+    atomicOr(status, (int32_t)ST_WAIT_TIMEOUT);
+}
+
 // y[r][o] = sum over column tiles t (in order) of ypart[t][r][o], plus b3[o].
 __global__ void k_head_combine(const float* __restrict__ ypart, int tiles, int64_t rows, int out,
                                const float* __restrict__ b3, float* __restrict__ y) {
@@ -1893,6 +1907,12 @@ void procrustes(const double* m, int d, double* r) {
       for (int k = 0; k < d; ++k) s += u[(size_t)i * d + k] * V(j, k);
       r[(size_t)i * d + j] = s;
     }
+}
+
+void wait_timeout_selftest(evoc_ctx* ctx, int32_t limit_ms) {
+  k_wait_probe<<<1, 64, 0, ctx->stream>>>(ctx->status.get(), (uint64_t)limit_ms * 1000000ull);
+  EVOC_CHECK_LAUNCH();
+  check_status(ctx, "wait self-test");
 }
 
 evoc_mlp* mlp_create(evoc_ctx* ctx, int in, int hid, int out, uint64_t seed) {

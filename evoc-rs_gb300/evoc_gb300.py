@@ -51,7 +51,7 @@ EXPORTED = [
     "evoc_mlp_n_params", "evoc_mlp_get_params", "evoc_mlp_set_params", "evoc_mlp_predict",
     "evoc_mlp_predict_device", "evoc_mlp_gradients", "evoc_mlp_fit_device",
     "evoc_to_bf16_device", "evoc_procrustes", "evoc_fuzzy_set_device_raw",
-    "evoc_label_prop_partition",
+    "evoc_label_prop_partition", "evoc_selftest_wait_timeout",
 ]
 
 
@@ -157,6 +157,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "evoc_fuzzy_set_device": ([vp, vp, vp, i64, i32, f32, C.c_int, vp, vp, pp], C.c_int),
         "evoc_fuzzy_set_device_raw": ([vp, vp, vp, i64, i32, i32, f32, C.c_int, pp], C.c_int),
         "evoc_label_prop_partition": ([vp, vp, i64, i32, u64, vp, C.POINTER(i64)], C.c_int),
+        "evoc_selftest_wait_timeout": ([vp, i32], C.c_int),
         "evoc_graph_from_csr": ([vp, vp, vp, vp, i64, pp], C.c_int),
         "evoc_graph_info": ([vp, C.POINTER(i64), C.POINTER(i64)], C.c_int),
         "evoc_graph_export": ([vp, vp, vp, vp], C.c_int),

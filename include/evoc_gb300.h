@@ -410,6 +410,12 @@ EVOC_API int evoc_mlp_fit_device(evoc_mlp_t* mlp, int32_t n_instances,
 EVOC_API int evoc_to_bf16_device(evoc_ctx_t* ctx, const float* d_in, int64_t count,
                                  uint16_t* d_out);
 
+/* Self-test of the bounded-wait path of the tcgen05 kernels: launches a
+ * kernel that waits on an mbarrier nothing arrives on, for limit_ms
+ * (1..2000), and returns the resulting EVOC_ERR_INTERNAL ("timed out"). The
+ * context stays usable. No counterpart. */
+EVOC_API int evoc_selftest_wait_timeout(evoc_ctx_t* ctx, int32_t limit_ms);
+
 /* Host only: the orthogonal d x d matrix R maximising trace(R^T M) for a
  * row-major d x d M (R = U V^T for M = U S V^T), 1 <= d <= 16. With
  * M = X^T Y for centred X and Y, X R is the rotation of X closest to Y. */

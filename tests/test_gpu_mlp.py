@@ -246,3 +246,19 @@ def test_warm_start_beats_random_init_at_reduced_epochs(ctx):
     qr = WS.quality(ev["x"], rand, ev["labels"], n_queries=1024)
     print("warm", qw, "random", qr)
     assert qw["trustworthiness"] > qr["trustworthiness"]
+
+
+def test_bounded_wait_times_out_and_the_context_survives(ctx):
+    """A wait that nothing satisfies gives up after its limit, the call
+    returns the timeout status, and the same context keeps working."""
+    import time
+    import evoc_gb300 as E
+    t = time.perf_counter()
+    rc = ctx.lib.evoc_selftest_wait_timeout(ctx.handle, 50)
+    dt = time.perf_counter() - t
+    assert rc == E.EVOC_ERR_INTERNAL
+    assert "timed out" in ctx.lib.evoc_last_error(ctx.handle).decode()
+    assert 0.04 < dt < 5.0
+    net = _net(ctx, 64, 64, 8)
+    x, _ = _data(64, 8, 300, seed=13)
+    _close(net.predict(x), M.forward(M.unpack(net.get_params(), 64, 64, 8), x)["y"], "after timeout")
