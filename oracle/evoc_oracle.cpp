@@ -35,7 +35,9 @@
 //      "Parallel random numbers: as easy as 1, 2, 3", SC 2011) instead of
 //      rand 0.10's SmallRng: negatives of edge e at epoch t use counter
 //      (j, t, e_lo, e_hi & 0x7fffffff) and key (seed_lo, seed_hi);
-//      k = (u32 * n) >> 32.
+//      k = (u32 * n) >> 32. The label-propagation seed draws
+//      (label_prop.rs:216-219) and outlier fallback draws (:138-140) use the
+//      counters of lp_seed_draw / lp_outlier_draw below.
 //   4. The squared distance (ann-search-rs 0.5.2 euclidean_simd, called at
 //      embedding.rs:210,237) is the serial left fold sum_d (a_d - b_d)^2.
 //   The per-node gradient is the reference's running sum (embedding.rs:
