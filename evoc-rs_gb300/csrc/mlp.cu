@@ -1167,7 +1167,10 @@ __global__ void k_head_combine(const float* __restrict__ ypart, int tiles, int64
 }
 
 // ---------------------------------------------------------------------------
-// Output layer (hidden -> out_dim, out_dim <= 16), one warp per row.
+// Output layer (hidden -> out_dim, out_dim <= 16), one warp per row: the
+// training step's head (loss and its gradients) and the output layer of the
+// mma.sync cross-check path; tcgen05 inference fuses it into the second
+// layer instead.
 // Inference writes y. Training also forms the MSE gradient
 //   dY = 2 (y - target) / (rows * out_dim),
 // its back-projection dH2 = (dY W3) * gelu'(H2) in BF16, and per-block sums of
@@ -1457,8 +1460,8 @@ CUtensorMap tmap_kmajor(const bf16* base, int64_t rows, int64_t k, int64_t ld, i
   return m;
 }
 
-// Ring depth of k_gemm_tc: 2 stages (two CTAs per SM) unless EVOC_TC_STAGES=4
-// (one CTA per SM, deeper prefetch).
+// Ring depth of the one-tile-per-CTA kernels (k_gemm_tc, k_gemm_tma): 2 stages
+// (two CTAs per SM) unless EVOC_TC_STAGES=4 (one CTA per SM, deeper prefetch).
 int tc_stages() {
   const char* e = std::getenv("EVOC_TC_STAGES");
   return (e && std::atoi(e) == 4) ? 4 : 2;
