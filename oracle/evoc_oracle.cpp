@@ -16,6 +16,8 @@
 //   label_outliers             src/graph/label_prop.rs:105-142
 //   remap_labels               src/graph/label_prop.rs:155-180
 //   label_prop_loop            src/graph/label_prop.rs:202-230
+//   label_propagation_init     src/graph/label_prop.rs:243-564 with the CSR
+//                              algebra of src/utils/sparse.rs:130-568
 // with the same parallel decomposition as the reference's rayon code
 // (parallel rows in smooth_knn_dist, serial knn_to_coo and hash inserts,
 // parallel per-row union, parallel nodes / nodes / edges in the three epoch
@@ -779,6 +781,421 @@ int64_t oracle_lp_partition(const int64_t* indptr, const uint32_t* indices, cons
   const int64_t parts = oracle_lp_remap(a.data(), n);
   for (int64_t i = 0; i < n; ++i) partition[i] = (uint32_t)a[i];
   return parts;
+}
+
+
+// ---------------------------------------------------------------------------
+// label_propagation_init (label_prop.rs:243-564) on the CSR algebra of
+// src/utils/sparse.rs:130-568, with the reference's summation orders:
+//   matmul        row-wise; per output row the products a_ik * b_kj are added
+//                 in the order of A's row entries, then B's row entries (the
+//                 first one set, later ones added), columns gathered sorted
+//                 (sparse.rs:307-365, SpaAcc :9-60);
+//   transpose     counting sort, rows in order (:256-296);
+//   norms         serial sums in storage order (:404-470);
+//   matmul_dense  per row, entries in order, row[k] += v * rhs[j][k] (:545-568).
+// Deviations: random draws from Philox (deviation 3); the PCA base case takes
+// its singular vectors from a Jacobi eigen-decomposition of X X^T, so their
+// signs follow a fixed convention (largest-magnitude component positive)
+// rather than faer's.
+// ---------------------------------------------------------------------------
+struct OCsr {
+  int64_t nrows = 0, ncols = 0;
+  std::vector<int64_t> indptr, indices;
+  std::vector<float> data;
+};
+
+static OCsr ocsr_from_partition(const std::vector<int64_t>& part, int64_t n_parts) {  // :243-254
+  OCsr m;
+  m.nrows = (int64_t)part.size();
+  m.ncols = n_parts;
+  m.indptr.resize(m.nrows + 1);
+  for (int64_t i = 0; i <= m.nrows; ++i) m.indptr[i] = i;
+  m.indices = part;
+  m.data.assign(m.nrows, 1.0f);
+  return m;
+}
+
+static OCsr ocsr_transpose(const OCsr& a) {  // :256-296
+  OCsr t;
+  t.nrows = a.ncols;
+  t.ncols = a.nrows;
+  t.indptr.assign(t.nrows + 1, 0);
+  for (int64_t c : a.indices) t.indptr[c + 1] += 1;
+  for (int64_t i = 0; i < t.nrows; ++i) t.indptr[i + 1] += t.indptr[i];
+  t.indices.resize(a.indices.size());
+  t.data.resize(a.data.size());
+  std::vector<int64_t> cur(t.indptr.begin(), t.indptr.end() - 1);
+  for (int64_t r = 0; r < a.nrows; ++r)
+    for (int64_t e = a.indptr[r]; e < a.indptr[r + 1]; ++e) {
+      const int64_t p = cur[a.indices[e]]++;
+      t.data[p] = a.data[e];
+      t.indices[p] = r;
+    }
+  return t;
+}
+
+static OCsr ocsr_matmul(const OCsr& a, const OCsr& b) {  // :307-365
+  OCsr c;
+  c.nrows = a.nrows;
+  c.ncols = b.ncols;
+  std::vector<std::vector<std::pair<int64_t, float>>> rows((size_t)a.nrows);
+#pragma omp parallel
+  {
+    std::vector<float> val((size_t)b.ncols, 0.0f);
+    std::vector<char> flag((size_t)b.ncols, 0);
+    std::vector<int64_t> touched;
+#pragma omp for schedule(dynamic, 64)
+    for (int64_t i = 0; i < a.nrows; ++i) {
+      touched.clear();
+      for (int64_t ae = a.indptr[i]; ae < a.indptr[i + 1]; ++ae) {
+        const int64_t k = a.indices[ae];
+        const float av = a.data[ae];
+        for (int64_t be = b.indptr[k]; be < b.indptr[k + 1]; ++be) {
+          const int64_t j = b.indices[be];
+          const float prod = av * b.data[be];
+          if (!flag[j]) {
+            flag[j] = 1;
+            touched.push_back(j);
+            val[j] = prod;
+          } else {
+            val[j] = val[j] + prod;
+          }
+        }
+      }
+      std::sort(touched.begin(), touched.end());
+      auto& row = rows[i];
+      row.reserve(touched.size());
+      for (int64_t j : touched) {
+        row.emplace_back(j, val[j]);
+        flag[j] = 0;
+        val[j] = 0.0f;
+      }
+    }
+  }
+  c.indptr.assign(c.nrows + 1, 0);
+  for (int64_t i = 0; i < c.nrows; ++i) c.indptr[i + 1] = c.indptr[i] + (int64_t)rows[i].size();
+  c.indices.reserve(c.indptr[c.nrows]);
+  c.data.reserve(c.indptr[c.nrows]);
+  for (auto& row : rows)
+    for (auto& e : row) {
+      c.indices.push_back(e.first);
+      c.data.push_back(e.second);
+    }
+  return c;
+}
+
+static OCsr ocsr_elementwise_mul(const OCsr& a, const OCsr& b) {  // :378-417
+  OCsr c;
+  c.nrows = a.nrows;
+  c.ncols = a.ncols;
+  c.indptr.assign(c.nrows + 1, 0);
+  for (int64_t i = 0; i < a.nrows; ++i) {
+    int64_t p = a.indptr[i], q = b.indptr[i];
+    const int64_t ep = a.indptr[i + 1], eq = b.indptr[i + 1];
+    while (p < ep && q < eq) {
+      if (a.indices[p] == b.indices[q]) {
+        c.indices.push_back(a.indices[p]);
+        c.data.push_back(a.data[p] * b.data[q]);
+        ++p;
+        ++q;
+      } else if (a.indices[p] < b.indices[q]) {
+        ++p;
+      } else {
+        ++q;
+      }
+    }
+    c.indptr[i + 1] = (int64_t)c.data.size();
+  }
+  return c;
+}
+
+static OCsr ocsr_normalise_cols_l2(const OCsr& a) {  // :427-458
+  std::vector<float> sq((size_t)a.ncols, 0.0f);
+  for (size_t e = 0; e < a.data.size(); ++e) sq[a.indices[e]] += a.data[e] * a.data[e];
+  std::vector<float> inv((size_t)a.ncols);
+  for (int64_t c = 0; c < a.ncols; ++c) {
+    const float nrm = std::sqrt(sq[c]);
+    inv[c] = nrm > 0.0f ? 1.0f / nrm : 1.0f;
+  }
+  OCsr r = a;
+  for (size_t e = 0; e < r.data.size(); ++e) r.data[e] = a.data[e] * inv[a.indices[e]];
+  return r;
+}
+
+static OCsr ocsr_normalise_rows_l1(const OCsr& a) {  // :468-492
+  OCsr r = a;
+  for (int64_t i = 0; i < a.nrows; ++i) {
+    float nrm = 0.0f;
+    for (int64_t e = a.indptr[i]; e < a.indptr[i + 1]; ++e) nrm += std::fabs(a.data[e]);
+    if (nrm > 0.0f) {
+      const float inv = 1.0f / nrm;
+      for (int64_t e = a.indptr[i]; e < a.indptr[i + 1]; ++e) r.data[e] = r.data[e] * inv;
+    }
+  }
+  return r;
+}
+
+static void ocsr_clip(OCsr& a, float lo, float hi) {  // :501-510
+  for (float& d : a.data) {
+    if (d < lo)
+      d = lo;
+    else if (d > hi)
+      d = hi;
+  }
+}
+
+static std::vector<float> ocsr_matmul_dense(const OCsr& a, const std::vector<float>& rhs,
+                                            int64_t d) {  // :545-568
+  std::vector<float> out((size_t)(a.nrows * d), 0.0f);
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t i = 0; i < a.nrows; ++i)
+    for (int64_t e = a.indptr[i]; e < a.indptr[i + 1]; ++e) {
+      const int64_t j = a.indices[e];
+      const float v = a.data[e];
+      for (int64_t k = 0; k < d; ++k) out[i * d + k] += v * rhs[j * d + k];
+    }
+  return out;
+}
+
+// label_prop.rs:243-280: per column, midpoint to 0 and half-range to 1.
+static void lp_unit_range(std::vector<float>& m, int64_t n, int64_t d) {
+  for (int64_t j = 0; j < d; ++j) {
+    float lo = std::numeric_limits<float>::infinity(), hi = -std::numeric_limits<float>::infinity();
+    for (int64_t i = 0; i < n; ++i) {
+      const float v = m[i * d + j];
+      if (v < lo) lo = v;
+      if (v > hi) hi = v;
+    }
+    const float range = hi - lo;
+    if (range > 0.0f) {
+      const float mid = (hi + lo) / 2.0f, half = range / 2.0f;
+      for (int64_t i = 0; i < n; ++i) m[i * d + j] = (m[i * d + j] - mid) / half;
+    }
+  }
+}
+
+// Symmetric Jacobi eigen-decomposition (cyclic sweeps) of a k x k matrix a
+// (row-major, destroyed): eigenvalues in w, eigenvectors in the columns of v.
+static void jacobi_eigen(std::vector<double>& a, int64_t k, std::vector<double>& w,
+                         std::vector<double>& v) {
+  v.assign((size_t)(k * k), 0.0);
+  for (int64_t i = 0; i < k; ++i) v[i * k + i] = 1.0;
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0.0;
+    for (int64_t p = 0; p < k; ++p)
+      for (int64_t q = p + 1; q < k; ++q) off += a[p * k + q] * a[p * k + q];
+    if (off < 1e-30) break;
+    for (int64_t p = 0; p < k; ++p)
+      for (int64_t q = p + 1; q < k; ++q) {
+        const double apq = a[p * k + q];
+        if (std::fabs(apq) < 1e-300) continue;
+        const double theta = (a[q * k + q] - a[p * k + p]) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+        for (int64_t r = 0; r < k; ++r) {  // A <- A J (columns p, q)
+          const double ap = a[r * k + p], aq = a[r * k + q];
+          a[r * k + p] = c * ap - sn * aq;
+          a[r * k + q] = sn * ap + c * aq;
+        }
+        for (int64_t r = 0; r < k; ++r) {  // A <- J^T A (rows p, q)
+          const double ap = a[p * k + r], aq = a[q * k + r];
+          a[p * k + r] = c * ap - sn * aq;
+          a[q * k + r] = sn * ap + c * aq;
+        }
+        for (int64_t r = 0; r < k; ++r) {
+          const double vp = v[r * k + p], vq = v[r * k + q];
+          v[r * k + p] = c * vp - sn * vq;
+          v[r * k + q] = sn * vp + c * vq;
+        }
+      }
+  }
+  w.resize((size_t)k);
+  for (int64_t i = 0; i < k; ++i) w[i] = a[i * k + i];
+}
+
+// label_prop.rs:288-330: the centred data's first components, u_j s_j, from
+// the eigenvectors of X X^T (sigma_j^2 = eigenvalue), then the unit range.
+static std::vector<float> lp_pca_init(const std::vector<float>& data, int64_t n, int64_t d,
+                                      int64_t n_comp, int64_t* out_cols) {
+  const int64_t k = std::min(std::min(n_comp, n), d);
+  std::vector<double> mean((size_t)d, 0.0);
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t j = 0; j < d; ++j) mean[j] += (double)data[i * d + j];
+  const double inv_n = 1.0 / (double)n;
+  for (double& m : mean) m *= inv_n;
+  std::vector<double> x((size_t)(n * d));
+  for (int64_t i = 0; i < n; ++i)
+    for (int64_t j = 0; j < d; ++j) x[i * d + j] = (double)data[i * d + j] - mean[j];
+  std::vector<double> g((size_t)(n * n), 0.0);
+  for (int64_t a = 0; a < n; ++a)
+    for (int64_t b = 0; b < n; ++b) {
+      double acc = 0.0;
+      for (int64_t j = 0; j < d; ++j) acc += x[a * d + j] * x[b * d + j];
+      g[a * n + b] = acc;
+    }
+  std::vector<double> w, v;
+  jacobi_eigen(g, n, w, v);
+  std::vector<int64_t> order((size_t)n);
+  for (int64_t i = 0; i < n; ++i) order[i] = i;
+  std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return w[a] > w[b]; });
+  std::vector<float> out((size_t)(n * k));
+  for (int64_t c = 0; c < k; ++c) {
+    const int64_t e = order[c];
+    const double sig = std::sqrt(std::max(w[e], 0.0));
+    int64_t big = 0;  // sign convention: the largest-magnitude entry is positive
+    for (int64_t i = 1; i < n; ++i)
+      if (std::fabs(v[i * n + e]) > std::fabs(v[big * n + e])) big = i;
+    const double sgn = v[big * n + e] < 0 ? -1.0 : 1.0;
+    for (int64_t i = 0; i < n; ++i) out[i * k + c] = (float)(sgn * v[i * n + e] * sig);
+  }
+  lp_unit_range(out, n, k);
+  *out_cols = k;
+  return out;
+}
+
+// label_prop.rs:338-360: uniform in [-1, 1] per coordinate, rows L2-normalised
+// (Philox draws: counter (q_lo, q_hi, "LP", "RINI"), key seed).
+static std::vector<float> lp_random_init(int64_t n, int64_t dim, uint64_t seed) {
+  std::vector<float> out((size_t)(n * dim));
+  const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  for (int64_t q = 0; q < n * dim; ++q) {
+    const uint32_t ctr[4] = {(uint32_t)q, (uint32_t)((uint64_t)q >> 32), 0x4C50u, 0x52494E49u};
+    uint32_t o[4];
+    philox4x32_10(ctr, key, o);
+    const double u = (double)((((uint64_t)o[1] << 32) | o[0]) >> 11) * (1.0 / 9007199254740992.0);
+    out[q] = (float)(u * 2.0 - 1.0);
+  }
+  for (int64_t i = 0; i < n; ++i) {
+    double nrm = 0.0;
+    for (int64_t j = 0; j < dim; ++j) nrm += (double)out[i * dim + j] * (double)out[i * dim + j];
+    nrm = std::sqrt(nrm);
+    if (nrm > 0.0)
+      for (int64_t j = 0; j < dim; ++j) out[i * dim + j] = (float)((double)out[i * dim + j] / nrm);
+  }
+  return out;
+}
+
+static int64_t lp_partition_csr(const OCsr& g, int64_t parts, int32_t n_iter, uint64_t seed,
+                                std::vector<int64_t>& part);
+
+// label_prop.rs:403-535
+static std::vector<float> lp_init_inner(const OCsr& g, int64_t dim, const std::vector<float>* data,
+                                        int64_t d, int32_t n_emb_epochs, int64_t approx_parts,
+                                        int32_t n_lp_iter, int64_t base_thr, double scaling,
+                                        uint64_t seed) {
+  const int64_t n = g.nrows;
+  if (n < base_thr) {  // :440-445
+    if (data && (int64_t)(data->size() / std::max<int64_t>(d, 1)) == n && dim <= d) {
+      int64_t cols = 0;
+      std::vector<float> pc = lp_pca_init(*data, n, d, dim, &cols);
+      if (cols == dim) return pc;
+      std::vector<float> full((size_t)(n * dim), 0.0f);  // fewer points than components
+      for (int64_t i = 0; i < n; ++i)
+        for (int64_t c = 0; c < cols; ++c) full[i * dim + c] = pc[i * cols + c];
+      return full;
+    }
+    return lp_random_init(n, dim, seed);
+  }
+  std::vector<int64_t> part;  // :448
+  const int64_t n_parts = lp_partition_csr(g, approx_parts, n_lp_iter, seed, part);
+  const OCsr base = ocsr_from_partition(part, n_parts);  // :455-457
+  const OCsr norm = ocsr_normalise_cols_l2(base);
+  const OCsr reducer = ocsr_normalise_rows_l1(ocsr_transpose(norm));
+  const OCsr nrt = ocsr_transpose(norm);  // :460-462
+  OCsr reduced = ocsr_matmul(ocsr_matmul(nrt, g), base);
+  ocsr_clip(reduced, 0.0f, 1.0f);
+  std::vector<float> rdata;  // :464-469
+  if (data) rdata = ocsr_matmul_dense(reducer, *data, d);
+  const int32_t e = std::min(n_emb_epochs, 255);
+  const std::vector<float> rinit =  // :472-483
+      lp_init_inner(reduced, dim, data ? &rdata : nullptr, d, e, approx_parts / 4, n_lp_iter,
+                    base_thr, scaling, seed + 3000);
+  // :486-498 short embedding of the coarse graph
+  std::vector<uint32_t> ridx(reduced.indices.begin(), reduced.indices.end());
+  OracleEmbedParams ep{e, 0.5f, 1.0f, (float)(0.001 * (double)e), 0.5f, 0.9f, 1e-7f};
+  std::vector<float> layout((size_t)(reduced.nrows * dim));
+  oracle_evoc_embedding(reduced.indptr.data(), ridx.data(), reduced.data.data(), reduced.nrows,
+                        (int32_t)dim, &ep, rinit.data(), seed + 4000, 0, e, layout.data(),
+                        nullptr, nullptr, nullptr);
+  // :500-510 expansion
+  const OCsr sym = ocsr_elementwise_mul(g, ocsr_transpose(g));
+  const OCsr expander = ocsr_normalise_rows_l1(ocsr_matmul(sym, norm));
+  const OCsr nrm_l1 = ocsr_normalise_rows_l1(norm);
+  const std::vector<float> expanded = ocsr_matmul_dense(expander, layout, dim);
+  const std::vector<float> direct = ocsr_matmul_dense(nrm_l1, layout, dim);
+  std::vector<float> res((size_t)(n * dim));
+  for (int64_t q = 0; q < n * dim; ++q) res[q] = (expanded[q] + direct[q]) * 0.5f;  // :512-516
+  const float inv_n = (float)(1.0 / (double)n);  // :518-528
+  for (int64_t j = 0; j < dim; ++j) {
+    float sum = 0.0f;
+    for (int64_t i = 0; i < n; ++i) sum += res[i * dim + j];
+    const float mean = sum * inv_n;
+    for (int64_t i = 0; i < n; ++i) res[i * dim + j] = res[i * dim + j] - mean;
+  }
+  const float scale = (float)scaling;  // :530-534
+  for (float& v : res) v = scale * v;
+  return res;
+}
+
+
+static int64_t lp_partition_csr(const OCsr& g, int64_t parts, int32_t n_iter, uint64_t seed,
+                                std::vector<int64_t>& part) {
+  std::vector<uint32_t> idx(g.indices.begin(), g.indices.end());
+  std::vector<uint32_t> p((size_t)g.nrows);
+  const int64_t k = oracle_lp_partition(g.indptr.data(), idx.data(), g.data.data(), g.nrows,
+                                        parts, n_iter, seed, p.data());
+  part.assign(p.begin(), p.end());
+  return k;
+}
+
+// label_prop.rs:243-280 on a row-major n x d f32 array (in place).
+void oracle_lp_unit_range(float* m, int64_t n, int64_t d) {
+  std::vector<float> v(m, m + n * d);
+  lp_unit_range(v, n, d);
+  std::memcpy(m, v.data(), v.size() * sizeof(float));
+}
+
+// The coarse graph of one level (label_prop.rs:455-462): clip(R^T G P) for the
+// partition `part` (n entries, n_parts parts); returned as an OracleGraph.
+OracleGraph* oracle_lp_coarse_graph(const int64_t* indptr, const uint32_t* indices,
+                                    const float* w, int64_t n, const uint32_t* part,
+                                    int64_t n_parts) {
+  OCsr g;
+  g.nrows = g.ncols = n;
+  g.indptr.assign(indptr, indptr + n + 1);
+  g.indices.assign(indices, indices + indptr[n]);
+  g.data.assign(w, w + indptr[n]);
+  std::vector<int64_t> pv(part, part + n);
+  const OCsr base = ocsr_from_partition(pv, n_parts);
+  const OCsr norm = ocsr_normalise_cols_l2(base);
+  OCsr red = ocsr_matmul(ocsr_matmul(ocsr_transpose(norm), g), base);
+  ocsr_clip(red, 0.0f, 1.0f);
+  OracleGraph* out = new OracleGraph();
+  out->n = red.nrows;
+  out->indptr = red.indptr;
+  out->indices.assign(red.indices.begin(), red.indices.end());
+  out->weights = red.data;
+  return out;
+}
+
+// label_propagation_init (label_prop.rs:537-564): data (n x d f32) may be NULL.
+int oracle_lp_init(const int64_t* indptr, const uint32_t* indices, const float* w, int64_t n,
+                   int32_t dim, const float* data, int64_t d, uint64_t seed, float* out) {
+  if (n <= 0 || dim <= 0) return -1;
+  OCsr g;
+  g.nrows = g.ncols = n;
+  g.indptr.assign(indptr, indptr + n + 1);
+  g.indices.assign(indices, indices + indptr[n]);
+  g.data.assign(w, w + indptr[n]);
+  const int64_t parts =
+      std::min<int64_t>(std::max<int64_t>((int64_t)(8.0 * std::sqrt((double)n)), 256), 16384);
+  std::vector<float> dv;
+  if (data) dv.assign(data, data + n * d);
+  const std::vector<float> res = lp_init_inner(g, dim, data ? &dv : nullptr, d, 50,
+                                               std::min(parts, n), 20, 64, 0.1, seed);
+  std::memcpy(out, res.data(), res.size() * sizeof(float));
+  return 0;
 }
 
 }  // extern "C"

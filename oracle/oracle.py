@@ -66,6 +66,9 @@ def lib() -> C.CDLL:
             "oracle_lp_outliers": ([vp, vp, i64, vp, u64], None),
             "oracle_lp_remap": ([vp, i64], i64),
             "oracle_lp_partition": ([vp, vp, vp, i64, i64, i32, u64, vp], i64),
+            "oracle_lp_unit_range": ([vp, i64, i64], None),
+            "oracle_lp_coarse_graph": ([vp, vp, vp, i64, vp, i64], vp),
+            "oracle_lp_init": ([vp, vp, vp, i64, i32, vp, i64, u64, vp], C.c_int),
         }
         for k, (a, r) in sigs.items():
             f = getattr(L, k)
@@ -241,3 +244,31 @@ def lp_partition(indptr, indices, weights, approx_n_parts: int, n_iter: int = 20
     k = lib().oracle_lp_partition(_p(ip), _p(ix), _p(w), n, approx_n_parts, n_iter, seed,
                                   _p(part))
     return part, int(k)
+
+
+def lp_unit_range(m) -> np.ndarray:
+    """normalise_to_unit_range (label_prop.rs:243-280)."""
+    a = np.array(m, dtype=np.float32, order="C")
+    lib().oracle_lp_unit_range(_p(a), a.shape[0], a.shape[1])
+    return a
+
+
+def lp_coarse_graph(indptr, indices, weights, partition, n_parts: int):
+    """clip(R^T G P) of one level (label_prop.rs:455-462) as CSR arrays."""
+    ip, ix, w = _csr(indptr, indices, weights)
+    part = np.ascontiguousarray(partition, dtype=np.uint32)
+    g = lib().oracle_lp_coarse_graph(_p(ip), _p(ix), _p(w), len(ip) - 1, _p(part), n_parts)
+    return _export(g)  # frees g
+
+
+def lp_init(indptr, indices, weights, dim: int, data=None, seed: int = 42) -> np.ndarray:
+    """label_propagation_init (label_prop.rs:537-564)."""
+    ip, ix, w = _csr(indptr, indices, weights)
+    n = len(ip) - 1
+    dd = None if data is None else np.ascontiguousarray(data, dtype=np.float32)
+    out = np.zeros((n, dim), dtype=np.float32)
+    rc = lib().oracle_lp_init(_p(ip), _p(ix), _p(w), n, dim, _p(dd),
+                              0 if dd is None else dd.shape[1], seed, _p(out))
+    if rc != 0:
+        raise ValueError("oracle_lp_init: invalid arguments")
+    return out
