@@ -84,6 +84,33 @@ def test_null_context_arguments_rejected():
     assert lib.evoc_last_error(None) is not None
 
 
+def test_null_handles_rejected_by_the_newer_entry_points():
+    """The warm-start, kNN-handoff, partition and self-test entry points reject
+    NULL handles with EVOC_ERR_INVALID_ARGUMENT before any device work."""
+    ensure_library()
+    import evoc_gb300 as E
+    lib = E.load_library()
+    h = ctypes.c_void_p()
+    bad = E.EVOC_ERR_INVALID_ARGUMENT
+    k = ctypes.c_int64()
+    loss = (ctypes.c_float * 1)()
+    p = E.MlpTrainParams().to_c()
+    assert lib.evoc_mlp_create(None, 64, 64, 8, 0, ctypes.byref(h)) == bad
+    assert lib.evoc_mlp_get_params(None, None) == bad
+    assert lib.evoc_mlp_set_params(None, None) == bad
+    assert lib.evoc_mlp_predict(None, None, 0, None) == bad
+    assert lib.evoc_mlp_predict_device(None, None, 0, None) == bad
+    assert lib.evoc_mlp_gradients(None, None, None, 1, loss, None) == bad
+    assert lib.evoc_mlp_fit_device(None, 1, None, None, None, ctypes.byref(p), None) == bad
+    assert lib.evoc_mlp_n_params(None) == 0
+    lib.evoc_mlp_free(None)  # no-op
+    assert lib.evoc_to_bf16_device(None, None, 0, None) == bad
+    assert lib.evoc_fuzzy_set_device_raw(None, None, None, 0, 2, 1, 1.0, 1, ctypes.byref(h)) == bad
+    assert lib.evoc_label_prop_partition(None, None, 1, 1, 0, None, ctypes.byref(k)) == bad
+    assert lib.evoc_selftest_wait_timeout(None, 10) == bad
+    assert "NULL" in lib.evoc_last_error(None).decode() or lib.evoc_last_error(None)
+
+
 def test_mlp_train_params_default():
     """evoc_mlp_train_params_default fills the documented defaults (no GPU)."""
     import ctypes as C
