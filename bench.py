@@ -202,15 +202,23 @@ def l2_gather_bytes(dimp: int, stats: np.ndarray) -> np.ndarray:
 
 
 def cpu_epochs_sample(ip, ix, w, dim, seed, stats, t0: int, n_ep: int, max_seconds: float):
-    """Oracle edge-updates/s over epochs [t0, t0 + n_ep) of the same run."""
+    """Oracle edge-updates/s over epochs [t0, t0 + n_ep) of the same run, and
+    the oracle's embedding after those epochs (from the random init)."""
     import oracle as O
     cores = O.max_threads()
-    _, st, secs = O.evoc_embedding(ip, ix, w, dim, seed=seed, start_epoch=t0,
-                                   end_epoch=t0 + n_ep, want_stats=True, want_times=True)
+    emb, st, secs = O.evoc_embedding(ip, ix, w, dim, seed=seed, start_epoch=t0,
+                                     end_epoch=t0 + n_ep, want_stats=True, want_times=True)
     sel = slice(t0, t0 + n_ep)
     fired = float(st[sel, 0].sum())
     tsec = float(secs[sel].sum())
-    return fired / tsec, cores, tsec
+    return fired / tsec, cores, tsec, emb, st
+
+
+def _same_bits(a: np.ndarray, b: np.ndarray) -> bool:
+    a = np.ascontiguousarray(a)
+    b = np.ascontiguousarray(b)
+    return a.shape == b.shape and a.dtype == b.dtype and np.array_equal(
+        a.view(np.uint8), b.view(np.uint8))
 
 
 def combine_replicas(res: dict, world: int, device) -> dict:
@@ -357,12 +365,38 @@ def run_ours(args) -> dict:
     }
     if not args.no_cpu_baseline:
         ip, ix, w = graph.export()
-        val, cores, tsec = cpu_epochs_sample(ip, ix, w, dim, cfg["seed"], stats,
-                                             args.cpu_t0, args.cpu_epochs, 30.0)
+        t0, ne_cpu = args.cpu_t0, min(args.cpu_epochs, n_epochs - args.cpu_t0)
+        val, cores, tsec, cpu_emb, cpu_st = cpu_epochs_sample(ip, ix, w, dim, cfg["seed"], stats,
+                                                              t0, ne_cpu, 30.0)
         res["cpu_baseline"] = {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
-                               "sample": f"epochs {args.cpu_t0}..{args.cpu_t0 + args.cpu_epochs - 1}"
+                               "sample": f"epochs {t0}..{t0 + ne_cpu - 1}"
                                          f" of the same 50-epoch run on the same graph "
                                          f"({tsec:.1f} s of CPU time)"}
+        # parity at the benchmarked size: the oracle's embedding against the
+        # GPU's. Epoch 0 fires no edge (every epochs_per_sample is >= 1), so
+        # epochs 1..49 from the random init equal the whole 50-epoch run and
+        # the timed loop's own output is compared; other samples are compared
+        # with the same epochs run on the GPU.
+        if t0 <= 1 and t0 + ne_cpu == n_epochs:
+            gpu_emb = out.cpu().numpy()
+            compared = "the timed loop's output (50 epochs)"
+        else:
+            gpu_emb = plan.debug_run(None, t0, t0 + ne_cpu)
+            compared = f"epochs {t0}..{t0 + ne_cpu - 1} run on the GPU"
+        emb_ok = _same_bits(gpu_emb, cpu_emb)
+        stats_ok = bool(np.array_equal(stats[t0:t0 + ne_cpu, :2], cpu_st[t0:t0 + ne_cpu, :2]))
+        # the fuzzy simplicial set against the oracle's, from the same host kNN
+        import oracle as O
+        t = time.time()
+        rip, rix, rw = O.fuzzy_set(idx_np, dist_np, float(k), True)
+        csr_s = time.time() - t
+        csr_ok = _same_bits(ip, rip) and _same_bits(ix, rix) and _same_bits(w, rw)
+        res["parity"] = bool(emb_ok and csr_ok and stats_ok)
+        res["parity_detail"] = {
+            "embedding_bit_exact": emb_ok, "embedding_compared": compared,
+            "schedule_stats_equal": stats_ok,
+            "fuzzy_set_csr_bit_exact": csr_ok, "oracle_fuzzy_set_s": round(csr_s, 1),
+            "nnz": int(len(ix))}
     plan.free()
     graph.free()
     ctx.close()

@@ -60,8 +60,9 @@ constexpr int64_t LP_LINEAR_DEG = 64;
 __global__ void k_lp_iter(const int64_t* __restrict__ indptr, const uint32_t* __restrict__ indices,
                           const float* __restrict__ w, int64_t n, const int32_t* __restrict__ in,
                           int32_t* __restrict__ out, int32_t* __restrict__ vlab,
-                          float* __restrict__ vsum, int32_t* __restrict__ hkey,
-                          int32_t* __restrict__ hpos, int32_t* __restrict__ changed) {
+                          float* __restrict__ vsum, const int64_t* __restrict__ hoff,
+                          int32_t* __restrict__ hkey, int32_t* __restrict__ hpos,
+                          int32_t* __restrict__ changed) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int32_t cur = in[i];
@@ -87,11 +88,10 @@ __global__ void k_lp_iter(const int64_t* __restrict__ indptr, const uint32_t* __
     }
   } else {
     // long row: an open-addressing table (label -> position in vlab/vsum) in
-    // the row's range [4b, 4e) of hkey/hpos, at most half full
-    int64_t cap = 1;
-    while (cap < 2 * deg) cap <<= 1;
-    int32_t* key = hkey + 4 * b;
-    int32_t* hp = hpos + 4 * b;
+    // the row's own range [hoff[i], hoff[i + 1]) of hkey/hpos, at most half full
+    const int64_t cap = hoff[i + 1] - hoff[i];
+    int32_t* key = hkey + hoff[i];
+    int32_t* hp = hpos + hoff[i];
     for (int64_t h = 0; h < cap; ++h) key[h] = -1;
     const int64_t mask = cap - 1;
     for (int64_t q = b; q < e; ++q) {
@@ -124,6 +124,21 @@ __global__ void k_lp_iter(const int64_t* __restrict__ indptr, const uint32_t* __
   }
   out[i] = best;
   if (best >= 0) *changed = 1;
+}
+
+// Hash-table slots of each row: the power of two >= 2 deg for rows longer
+// than LP_LINEAR_DEG, none for the others (they search their votes linearly).
+__global__ void k_lp_hcap(const int64_t* __restrict__ indptr, int64_t n,
+                          int64_t* __restrict__ cap_out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t deg = indptr[i + 1] - indptr[i];
+  int64_t cap = 0;
+  if (deg > LP_LINEAR_DEG) {
+    cap = 1;
+    while (cap < 2 * deg) cap <<= 1;
+  }
+  cap_out[i] = cap;
 }
 
 __global__ void k_lp_max(const int32_t* __restrict__ labels, int64_t n, int32_t* __restrict__ mx,
@@ -234,7 +249,16 @@ int64_t label_prop_partition(evoc_ctx* ctx, const evoc_graph* g, int64_t approx_
   if (n_iter < 0) throw Error(EVOC_ERR_INVALID_ARGUMENT, "n_iter < 0");
   DevBuf<int32_t> la(n, s), lb(n, s), vlab(std::max<int64_t>(nnz, 1), s), flag(1, s);
   DevBuf<float> vsum(std::max<int64_t>(nnz, 1), s);
-  DevBuf<int32_t> hkey(std::max<int64_t>(4 * nnz, 1), s), hpos(std::max<int64_t>(4 * nnz, 1), s);
+  // hash tables only for the long rows, packed by a prefix sum of their sizes
+  DevBuf<int64_t> hcap(n, s), hoff(n + 1, s);
+  k_lp_hcap<<<grid_for(n), 256, 0, s>>>(g->indptr.get(), n, hcap.get());
+  EVOC_CHECK_LAUNCH();
+  exclusive_scan_i64(hcap.get(), hoff.get(), n, s);
+  int64_t htot = 0;
+  EVOC_CUDA(cudaMemcpyAsync(&htot, hoff.get() + n, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  EVOC_CUDA(cudaStreamSynchronize(s));
+  hcap.release();
+  DevBuf<int32_t> hkey(std::max<int64_t>(htot, 1), s), hpos(std::max<int64_t>(htot, 1), s);
   k_lp_fill<<<grid_for(n), 256, 0, s>>>(la.get(), n);
   if (approx_n_parts > 0)
     k_lp_seed<<<grid_for(approx_n_parts), 256, 0, s>>>(la.get(), n, approx_n_parts, seed);
@@ -245,7 +269,8 @@ int64_t label_prop_partition(evoc_ctx* ctx, const evoc_graph* g, int64_t approx_
     EVOC_CUDA(cudaMemsetAsync(flag.get(), 0, sizeof(int32_t), s));
     k_lp_iter<<<grid_for(n, 128), 128, 0, s>>>(g->indptr.get(), g->indices.get(),
                                                g->weights.get(), n, la.get(), lb.get(),
-                                               vlab.get(), vsum.get(), hkey.get(), hpos.get(),
+                                               vlab.get(), vsum.get(), hoff.get(), hkey.get(),
+                                               hpos.get(),
                                                flag.get());
     EVOC_CHECK_LAUNCH();
     std::swap(la, lb);

@@ -8,7 +8,8 @@
 // defined only up to isometry), with a mean-squared-error loss and Adam.
 //
 // Numerics: weights and activations feed the tensor cores as BF16 and are
-// accumulated in FP32 (mma.sync m16n8k16); pre-activations, the loss, all
+// accumulated in FP32 (tcgen05.mma kind::f16 into tensor memory by default;
+// an mma.sync m16n8k16 path stays as a cross-check); pre-activations, the loss, all
 // gradients and the Adam state are FP32; an FP32 master copy of every
 // parameter is what Adam updates, and its BF16 copy is refreshed each step.
 // Every reduction has a fixed order, so results are reproducible run to run.

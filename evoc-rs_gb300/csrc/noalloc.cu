@@ -11,13 +11,18 @@
 // symmetrise = 0 (smooth_knn_dist + knn_to_coo + coo_to_adjacency_list,
 // src/graph/fuzzy_graph.rs:33-159, :242-256), bit for bit, into caller-owned
 // output buffers. Its per-row scratch lives in one file-scope device array of
-// fixed size (EVOC_NOALLOC_SCRATCH_BYTES), which every GPU that loads the
-// library holds until the process exits.
+// fixed size (EVOC_NOALLOC_SCRATCH_BYTES). CUDA loads device code lazily by
+// default, so the array (with this file's kernels) is placed on a GPU by the
+// first call there, and stays until the process exits; callers that reserve
+// their memory budget make a small first call at start-up, or run with
+// CUDA_MODULE_LOADING=EAGER.
 //
 // Set-up: on its first call on a device (with that device current) the entry
 // point looks up the array's device address with cudaGetSymbolAddress and
-// caches it; the host-side symbol itself is only a stand-in and is never
-// passed to a kernel. Make that first call before any stream capture.
+// keeps it for the life of the process; the host-side symbol itself is only a
+// stand-in and is never passed to a kernel. Make that first call before any
+// stream capture, and do not reset the device while the library is in use
+// (the kept address would go stale).
 //
 // Sharing: every call on a device uses the same array and leaves the last
 // call's contents in it. The status word is cleared at the start of each

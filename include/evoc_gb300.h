@@ -177,8 +177,11 @@ EVOC_API int evoc_graph_from_csr(evoc_ctx_t* ctx, const int64_t* indptr,
                         const uint32_t* indices, const float* weights,
                         int64_t n, evoc_graph_t** out_graph);
 
-/* Scratch of evoc_knn_to_csr_noalloc: one device array of this many bytes,
- * held by every GPU that loads the library until the process exits. */
+/* Scratch of evoc_knn_to_csr_noalloc: one device array of this many bytes.
+ * CUDA loads the library's device code lazily (the default since CUDA 12.2),
+ * so a GPU holds the array from the first evoc_knn_to_csr_noalloc call on it
+ * (or from process start with CUDA_MODULE_LOADING=EAGER) until the process
+ * exits. */
 #define EVOC_NOALLOC_SCRATCH_BYTES (16u << 20)
 
 /* Weighted directed kNN graph without allocating anything (no counterpart in
@@ -204,8 +207,14 @@ EVOC_API int evoc_graph_from_csr(evoc_ctx_t* ctx, const int64_t* indptr,
  *   with EVOC_ERR_INVALID_ARGUMENT.
  * - All calls on a device share that array. Calls whose GPU work overlaps
  *   race on it.
- * - The first call on a device looks up the array's device address. Make
- *   that first call before any stream capture.
+ * - The first call on a device loads this code onto the device, which places
+ *   the array and the kernels in device memory (about 16 MiB), and looks up
+ *   the array's device address. So make a first call (a one-row call will
+ *   do) at start-up, before the caller reserves its memory budget and before
+ *   any stream capture; or set CUDA_MODULE_LOADING=EAGER before CUDA starts.
+ * - The address is kept per device for the life of the process. Do not reset
+ *   a device (cudaDeviceReset) while the library is in use on it: later calls
+ *   would pass a stale address.
  * - Errors are reported through evoc_last_error(NULL). */
 EVOC_API int evoc_knn_to_csr_noalloc(const uint32_t* d_knn_idx,
                                      const float* d_knn_dist, int64_t n,

@@ -64,6 +64,35 @@ def test_noalloc_matches_allocating_entry_point(ctx):
         assert np.array_equal(weights[:nnz].cpu().numpy().view(np.uint32), rw.view(np.uint32))
 
 
+def test_noalloc_call_allocates_no_device_memory(ctx):
+    """After a first call (which loads the code and places the scratch array),
+    a call with fresh inputs leaves the device's free memory unchanged."""
+    import torch
+    import evoc_gb300 as E
+    lib = E.load_library()
+    n, k = 2500, 12
+    bufs = []
+    for seed in (31, 32):
+        idx, dist = _inputs(seed, n, k)
+        bufs.append((torch.from_numpy(idx.view(np.int32)).cuda(), torch.from_numpy(dist).cuda()))
+    indptr = torch.empty(n + 1, dtype=torch.int64, device="cuda")
+    indices = torch.empty(n * k, dtype=torch.int32, device="cuda")
+    weights = torch.empty(n * k, dtype=torch.float32, device="cuda")
+    nnz = C.c_int64(-1)
+
+    def call(d_idx, d_dist):
+        return lib.evoc_knn_to_csr_noalloc(d_idx.data_ptr(), d_dist.data_ptr(), n, k, float(k),
+                                           indptr.data_ptr(), indices.data_ptr(),
+                                           weights.data_ptr(), n * k, C.byref(nnz), None)
+
+    assert call(*bufs[0]) == E.EVOC_OK
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    assert call(*bufs[1]) == E.EVOC_OK
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info()[0] == free_before
+
+
 def test_noalloc_rejects_oversize_and_small_capacity(ctx):
     import torch
     import evoc_gb300 as E
