@@ -771,22 +771,28 @@ __global__ void k_edge_sched(const float* __restrict__ e_ps, int64_t U, int32_t 
   const unsigned FULL = 0xffffffffu;
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = e < U;
-  Sched sc;
-  sc.init(valid ? e_ps[e] : 3.0e38f, neg_factor, valid);
+  const float ps = valid ? e_ps[e] : 3.0e38f;
+  const float pn = fmul(ps, neg_factor);
+  float ns = ps, nn = pn, mx = 0.0f;
   uint32_t fm[2] = {0u, 0u}, n0[2] = {0u, 0u}, n1[2] = {0u, 0u};  // epochs 0-31, 32-63
-  float mx = 0.0f;
+  // the same recurrence as Sched::stepf, with the count kept in float and its
+  // two low bits taken by comparisons (count 3 stands for 3 or more)
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     const int32_t t_end = min(ne, 32 * (h + 1));
-    for (int32_t t = 32 * h; t < t_end; ++t) {
-      float c = 0.0f;
-      const bool f = valid && sc.stepf((float)t, &c);
-      const uint32_t c3 = c >= 3.0f ? 3u : (uint32_t)c;
-      const int b = t - 32 * h;
-      fm[h] |= (f ? 1u : 0u) << b;
-      n0[h] |= (c3 & 1u) << b;
-      n1[h] |= (c3 >> 1) << b;
-      mx = fmaxf(mx, c);
+    float tf = (float)(32 * h);
+    uint32_t bit = 1u;
+    for (int32_t t = 32 * h; t < t_end; ++t, tf = fadd(tf, 1.0f), bit <<= 1) {
+      if (!(ns > tf)) fm[h] |= bit;  // fires (also for a NaN schedule, which never updates)
+      if (ns <= tf) {
+        ns = fadd(ns, ps);
+        const float x = floorf(fdiv(fsub(tf, nn), pn));
+        const float c = (x > 0.0f && x < 18446744073709551616.0f) ? x : 0.0f;
+        nn = fadd(nn, fmul(c, pn));
+        if (c == 1.0f || c >= 3.0f) n0[h] |= bit;
+        if (c >= 2.0f) n1[h] |= bit;
+        mx = fmaxf(mx, c);
+      }
     }
   }
   if (valid) {
@@ -904,40 +910,64 @@ __device__ __forceinline__ uint32_t tile_word(const uint32_t* __restrict__ plane
 }
 
 // Count pass from the planes: warp per tile; slots per epoch = fired entries
-// + their negatives (N0 + 2 N1). Per-epoch totals of fired entries and
-// negatives go to fired[t] / negs[t].
-__global__ void k_plane_count(const int64_t* __restrict__ inc_ptr, int64_t n, int64_t ntiles,
-                              int64_t W, int32_t ne, const uint32_t* __restrict__ fplane,
-                              const uint32_t* __restrict__ nplane0,
-                              const uint32_t* __restrict__ nplane1,
-                              int32_t* __restrict__ counts,
-                              unsigned long long* __restrict__ fired,
-                              unsigned long long* __restrict__ negs) {
+// + their negatives (N0 + 2 N1), written to counts[t * ntiles + tile]. The
+// loads of 8 epochs are issued together (the pass is latency-bound), and the
+// per-epoch totals of fired entries and negatives (fired[t], negs[t]) are
+// summed in shared memory by the block's 8 warps before one global atomic each.
+constexpr int COUNT_EU = 8;
+__global__ void __launch_bounds__(256) k_plane_count(
+    const int64_t* __restrict__ inc_ptr, int64_t n, int64_t ntiles, int64_t W, int32_t ne,
+    const uint32_t* __restrict__ fplane, const uint32_t* __restrict__ nplane0,
+    const uint32_t* __restrict__ nplane1, int32_t* __restrict__ counts,
+    unsigned long long* __restrict__ fired, unsigned long long* __restrict__ negs) {
+  __shared__ unsigned long long sfired[64], snegs[64];
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) sfired[i] = snegs[i] = 0ull;
+  __syncthreads();
   const int64_t tile = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (tile >= ntiles) return;
-  const int64_t v0 = tile * TILE;
-  const int nt = (int)min((int64_t)TILE, n - v0);
-  const int64_t P0 = inc_ptr[v0], P1 = inc_ptr[v0 + nt];
-  const int64_t wb = P0 >> 5, we = P1 > P0 ? ((P1 - 1) >> 5) + 1 : wb;
-  const uint32_t lo_mask = ~0u << (P0 & 31);
-  const uint32_t hi_mask = ~0u >> (31 - (int)((P1 - 1) & 31));
-  for (int32_t t = 0; t < ne; ++t) {
-    const int64_t po = (int64_t)t * W;
-    int cf = 0, cn = 0;
-    for (int64_t w = wb + lane; w < we; w += 32) {
-      cf += __popc(tile_word(fplane + po, w, wb, we, lo_mask, hi_mask));
-      cn += __popc(tile_word(nplane0 + po, w, wb, we, lo_mask, hi_mask)) +
-            2 * __popc(tile_word(nplane1 + po, w, wb, we, lo_mask, hi_mask));
+  if (tile < ntiles) {
+    const int64_t v0 = tile * TILE;
+    const int nt = (int)min((int64_t)TILE, n - v0);
+    const int64_t P0 = inc_ptr[v0], P1 = inc_ptr[v0 + nt];
+    const int64_t wb = P0 >> 5, we = P1 > P0 ? ((P1 - 1) >> 5) + 1 : wb;
+    const uint32_t lo_mask = ~0u << (P0 & 31);
+    const uint32_t hi_mask = ~0u >> (31 - (int)((P1 - 1) & 31));
+    for (int32_t t0 = 0; t0 < ne; t0 += COUNT_EU) {
+      int cf[COUNT_EU], cn[COUNT_EU];
+#pragma unroll
+      for (int u = 0; u < COUNT_EU; ++u) cf[u] = cn[u] = 0;
+      for (int64_t w = wb + lane; w < we; w += 32) {
+        uint32_t x[COUNT_EU], y0[COUNT_EU], y1[COUNT_EU];
+#pragma unroll
+        for (int u = 0; u < COUNT_EU; ++u) {
+          const int64_t po = (int64_t)min(t0 + u, ne - 1) * W;
+          x[u] = tile_word(fplane + po, w, wb, we, lo_mask, hi_mask);
+          y0[u] = tile_word(nplane0 + po, w, wb, we, lo_mask, hi_mask);
+          y1[u] = tile_word(nplane1 + po, w, wb, we, lo_mask, hi_mask);
+        }
+#pragma unroll
+        for (int u = 0; u < COUNT_EU; ++u) {
+          cf[u] += __popc(x[u]);
+          cn[u] += __popc(y0[u]) + 2 * __popc(y1[u]);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < COUNT_EU; ++u) {
+        const int32_t t = t0 + u;
+        const int f = __reduce_add_sync(FULL, cf[u]), g = __reduce_add_sync(FULL, cn[u]);
+        if (lane == 0 && t < ne) {
+          counts[(int64_t)t * ntiles + tile] = f + g;
+          if (f) atomicAdd_block(&sfired[t], (unsigned long long)f);
+          if (g) atomicAdd_block(&snegs[t], (unsigned long long)g);
+        }
+      }
     }
-    cf = __reduce_add_sync(FULL, cf);
-    cn = __reduce_add_sync(FULL, cn);
-    if (lane == 0) {
-      counts[(int64_t)t * ntiles + tile] = cf + cn;
-      if (cf) atomicAdd(&fired[t], (unsigned long long)cf);
-      if (cn) atomicAdd(&negs[t], (unsigned long long)cn);
-    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < ne; t += blockDim.x) {
+    if (sfired[t]) atomicAdd(&fired[t], sfired[t]);
+    if (snegs[t]) atomicAdd(&negs[t], snegs[t]);
   }
 }
 
@@ -956,157 +986,142 @@ __device__ __forceinline__ int nth_set_bit(uint32_t m, int r) {
   return pos;
 }
 
-// Fill pass from the planes (n_epochs <= 64, at most 3 negatives per edge and
-// epoch): warp per (tile, epoch), numbered tile-major: a hub tile's epochs
-// run in parallel, and the warps of one tile read its partner ids from L2
-// together. For each 32-word window of the tile's entries, a prefix sum of the
-// words' fired counts numbers the fired entries in incidence order; each
-// batch of 32 consecutive fired entries goes one per lane (the word by a
-// shuffle binary search, the bit by nth_set_bit), so every lane has work and
-// the batch's slots (each attraction, then its negatives, placed by a prefix
-// of the per-entry slot counts) land close together. Every (epoch, tile)
-// segment holds the terms in the order of the reference's serial sum.
-// Negative draws (Philox counter (j, epoch, edge)) are queued in shared memory
-// and drawn 32 at a time.
-constexpr int DRAW_Q = 160;  // >= 31 left over + 32 lanes x 3 negatives
-struct DrawJob {
+// Fill pass from the planes, block per (tile, FILL_EPB epochs). The block
+// stages the tile's partner ids and each entry's tile-local node in shared
+// memory (FILL_SEG entries at a time, coalesced); warp w then writes the
+// slots of epoch FILL_EPB * g + w. Per 32-word window of fire bits, lane l
+// takes word l: its slot count (fired entries + their negatives) and its
+// negative-draw count are prefix-summed over the lanes, and the lane walks its
+// word's fired entries in order, storing each attraction slot at its place and
+// queueing its negatives (slot position, edge, draw index) in shared memory.
+// The queue is then drawn (Philox) 32 at a time by the whole warp. A window
+// with more draws than the queue holds draws them inline instead (the same
+// draws at the same places). Every (epoch, tile) segment holds the terms in
+// the order of the reference's serial sum: entries in incidence order, each
+// attraction followed by its negatives.
+constexpr int FILL_EPB = 8;
+constexpr int FILL_SEG = 4096;
+constexpr int FILL_Q = 128;  // queued draws per warp and window
+struct FillJob {
   int64_t q;        // slot index
   uint32_t eidx;    // edge id
   uint32_t jn;      // draw index j | tile-local node << 8
 };
 struct PlaneFillSmem {
-  DrawJob job[DRAW_Q];
-  int64_t pb[TILE + 1];  // incidence offsets of the tile's nodes (entry -> node)
-  int64_t eb[TILE];      // edge-id bases of the tile's nodes
+  uint32_t part[FILL_SEG];           // partner of each staged entry
+  uint8_t node[FILL_SEG];            // tile-local node of each staged entry
+  int64_t pb[TILE + 1];              // incidence offsets of the tile's nodes
+  int64_t eb[TILE];                  // edge-id bases of the tile's nodes
+  FillJob job[FILL_EPB][FILL_Q];     // per-warp draw queues
 };
 
-// Draws the first `cnt` queued jobs, one per lane, and writes their slots.
-__device__ __forceinline__ void drain_jobs(const DrawJob* __restrict__ job, int cnt, int lane,
-                                           int32_t t, int64_t v0, uint32_t n_total,
-                                           uint64_t seed,
-                                           const uint32_t* __restrict__ prob_of_node,
-                                           const ProbInfo* __restrict__ prob,
-                                           uint2* __restrict__ slots) {
-  if (lane < cnt) {
-    const DrawJob jb = job[lane];
-    const uint32_t node = jb.jn >> 8;
-    uint32_t nb = 0, np = n_total;
-    uint64_t sd = seed;
-    if (prob_of_node) {
-      const ProbInfo pi = prob[prob_of_node[v0 + node]];
-      nb = pi.node_base;
-      np = pi.n;
-      sd = pi.seed;
-    }
-    slots[jb.q] = make_uint2(nb + negative_draw(sd, jb.jn & 0xffu, (uint32_t)t, jb.eidx, np),
-                             node | 32u);
+__device__ __forceinline__ uint2 negative_slot(uint64_t seed, uint32_t j, int32_t t, uint32_t eidx,
+                                               uint32_t node, int64_t v0, uint32_t n_total,
+                                               const uint32_t* __restrict__ prob_of_node,
+                                               const ProbInfo* __restrict__ prob) {
+  uint32_t nb = 0, np = n_total;
+  uint64_t sd = seed;
+  if (prob_of_node) {
+    const ProbInfo pi = prob[prob_of_node[v0 + node]];
+    nb = pi.node_base;
+    np = pi.n;
+    sd = pi.seed;
   }
+  return make_uint2(nb + negative_draw(sd, j, (uint32_t)t, eidx, np), node | 32u);
 }
 
-__global__ void __launch_bounds__(128) k_plane_fill(
+__global__ void __launch_bounds__(32 * FILL_EPB) k_plane_fill(
     const int64_t* __restrict__ inc_ptr, const uint32_t* __restrict__ inc_other,
     const int64_t* __restrict__ eidx_base, int64_t n, int64_t ntiles, int64_t W, int32_t ne,
     const uint32_t* __restrict__ fplane, const uint32_t* __restrict__ nplane0,
     const uint32_t* __restrict__ nplane1, const int64_t* __restrict__ tile_off,
     const uint32_t* __restrict__ prob_of_node, const ProbInfo* __restrict__ prob,
     uint64_t seed, uint2* __restrict__ slots) {
-  __shared__ PlaneFillSmem sm_all[4];
-  PlaneFillSmem& sm = sm_all[threadIdx.x >> 5];
+  __shared__ PlaneFillSmem sm;
   const unsigned FULL = 0xffffffffu;
-  const int lane = threadIdx.x & 31;
-  const int64_t item = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (item >= (int64_t)ne * ntiles) return;
-  const int64_t tile = item / ne;
-  const int32_t t = (int32_t)(item - tile * ne);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int ngroups = (ne + FILL_EPB - 1) / FILL_EPB;
+  const int64_t tile = blockIdx.x / ngroups;
+  const int32_t t = (int32_t)(blockIdx.x % ngroups) * FILL_EPB + wid;
   const int64_t v0 = tile * TILE;
   const int nt = (int)min((int64_t)TILE, n - v0);
-  sm.pb[lane] = inc_ptr[v0 + min(lane, nt)];  // lanes >= nt hold the end
-  if (lane == 0) sm.pb[TILE] = inc_ptr[v0 + nt];
-  sm.eb[lane] = (lane < nt) ? eidx_base[v0 + lane] : 0;
-  __syncwarp();
-  const int64_t P0 = sm.pb[0];
-  const int64_t P1 = sm.pb[nt];
-  if (P1 <= P0) return;
-  const int64_t wb = P0 >> 5, we = ((P1 - 1) >> 5) + 1;
-  const uint32_t lo_mask = ~0u << (P0 & 31);
-  const uint32_t hi_mask = ~0u >> (31 - (int)((P1 - 1) & 31));
+  if (threadIdx.x <= TILE) sm.pb[threadIdx.x] = inc_ptr[v0 + min((int)threadIdx.x, nt)];
+  if (threadIdx.x < TILE) sm.eb[threadIdx.x] = (int)threadIdx.x < nt ? eidx_base[v0 + threadIdx.x] : 0;
+  __syncthreads();
+  const int64_t P0 = sm.pb[0], P1 = sm.pb[nt];
+  if (P1 <= P0) return;  // the whole block: no entries
+  const bool active = t < ne;
+  int64_t cur = active ? tile_off[(int64_t)t * ntiles + tile] : 0;
   const int64_t po = (int64_t)t * W;
-  int64_t cur = tile_off[(int64_t)t * ntiles + tile];
-  int qn = 0;  // queued draws
-  int node = 0;  // node of this lane's current entry (a lane's entries only move forward)
-  for (int64_t ws = wb; ws < we; ws += 32) {
-    const int64_t w = ws + lane;
-    const uint32_t xw = tile_word(fplane + po, w, wb, we, lo_mask, hi_mask);
-    // negative bits are set only on fired entries: masking by xw keeps the tile's
-    const uint32_t g0w = xw ? nplane0[po + w] & xw : 0u, g1w = xw ? nplane1[po + w] & xw : 0u;
-    int fincl = __popc(xw);  // fired entries up to and including this lane's word
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(FULL, fincl, o);
-      if (lane >= o) fincl += y;
-    }
-    const int ftot = __shfl_sync(FULL, fincl, 31);
-    // batches of 32 consecutive fired entries (incidence order), one per lane
-    for (int k0 = 0; k0 < ftot; k0 += 32) {
-      const int k = k0 + lane;
-      int j = 0;  // the word (lane) holding fired entry k: first j with fincl[j] > k
+  FillJob* job = sm.job[wid];
+  const uint32_t lt = (1u << lane) - 1u;
+  for (int64_t sb = P0; sb < P1; sb += FILL_SEG) {
+    const int64_t se = min(sb + (int64_t)FILL_SEG, P1);
+    __syncthreads();  // the previous segment's readers are done
+    for (int64_t p = sb + threadIdx.x; p < se; p += blockDim.x) {
+      sm.part[p - sb] = inc_other[p];
+      int l = 0;  // last node l < nt with pb[l] <= p (empty rows are skipped)
 #pragma unroll
       for (int step = 16; step >= 1; step >>= 1)
-        if (__shfl_sync(FULL, fincl, j + step - 1) <= k) j += step;
-      const uint32_t xj = __shfl_sync(FULL, xw, j);
-      const uint32_t g0j = __shfl_sync(FULL, g0w, j), g1j = __shfl_sync(FULL, g1w, j);
-      const int fex = __shfl_sync(FULL, fincl, j) - __popc(xj);
-      const bool valid = k < ftot;
-      int nn = 0;
-      int64_t p = 0;
-      if (valid) {
-        const int b = nth_set_bit(xj, k - fex);
-        p = ((ws + j) << 5) + b;
-        nn = (int)(((g0j >> b) & 1u) | (((g1j >> b) & 1u) << 1));
-      }
-      const int cnt = valid ? 1 + nn : 0;  // this entry's slots: attraction + negatives
-      int cincl = cnt;
+        if (l + step < nt && sm.pb[l + step] <= p) l += step;
+      sm.node[p - sb] = (uint8_t)l;
+    }
+    __syncthreads();
+    if (!active) continue;
+    const int64_t wb = sb >> 5, we = ((se - 1) >> 5) + 1;
+    const uint32_t lo_mask = ~0u << (sb & 31);
+    const uint32_t hi_mask = ~0u >> (31 - (int)((se - 1) & 31));
+    for (int64_t ws = wb; ws < we; ws += 32) {
+      const int64_t w = ws + lane;
+      uint32_t f = tile_word(fplane + po, w, wb, we, lo_mask, hi_mask);
+      // negative bits are set only on fired entries: masking by f keeps the segment's
+      const uint32_t g0 = f ? nplane0[po + w] & f : 0u, g1 = f ? nplane1[po + w] & f : 0u;
+      const int nneg = __popc(g0) + 2 * __popc(g1);
+      int sincl = __popc(f) + nneg, jincl = nneg;  // inclusive prefix sums over lanes
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(FULL, cincl, o);
-        if (lane >= o) cincl += y;
+        const int y = __shfl_up_sync(FULL, sincl, o), z = __shfl_up_sync(FULL, jincl, o);
+        if (lane >= o) {
+          sincl += y;
+          jincl += z;
+        }
       }
-      const int64_t q = cur + cincl - cnt;
-      cur += __shfl_sync(FULL, cincl, 31);
-      uint32_t eidx = 0;
-      int64_t q0 = 0;
-      if (valid) {
-        while (node + 1 < nt && sm.pb[node + 1] <= p) ++node;
-        slots[q] = make_uint2(inc_other[p], (uint32_t)node);
-        q0 = q + 1;
-        eidx = (uint32_t)(p + sm.eb[node]);
+      const int stot = __shfl_sync(FULL, sincl, 31), jtot = __shfl_sync(FULL, jincl, 31);
+      if (stot == 0) continue;
+      const bool queued = jtot <= FILL_Q;
+      int64_t q = cur + sincl - (__popc(f) + nneg);
+      int jq = jincl - nneg;
+      __syncwarp();  // the previous window's drain has read its jobs
+      while (f) {
+        const int b = __ffs(f) - 1;
+        f &= f - 1;
+        const int64_t p = (w << 5) + b;
+        const int li = (int)(p - sb);
+        const uint32_t node = sm.node[li];
+        slots[q++] = make_uint2(sm.part[li], node);
+        const uint32_t nn = ((g0 >> b) & 1u) | (((g1 >> b) & 1u) << 1);
+        if (nn) {
+          const uint32_t eidx = (uint32_t)(p + sm.eb[node]);
+          for (uint32_t j = 0; j < nn; ++j, ++q) {
+            if (queued)
+              job[jq++] = FillJob{q, eidx, j | (node << 8)};
+            else
+              slots[q] = negative_slot(seed, j, t, eidx, node, v0, (uint32_t)n, prob_of_node, prob);
+          }
+        }
       }
-      // queue this batch's draws, level by level (draw j of every lane with
-      // more than j negatives); their order in the queue does not matter
-      const uint32_t lt = (1u << lane) - 1u;
-      const uint32_t b1 = __ballot_sync(FULL, nn >= 1), b2 = __ballot_sync(FULL, nn >= 2),
-                     b3 = __ballot_sync(FULL, nn >= 3);
-      const int c1 = __popc(b1), c2 = __popc(b2);
-      const int add = c1 + c2 + __popc(b3);
-      if (add == 0) continue;
-      __syncwarp();  // earlier drains have read their jobs
-      if (nn >= 1) sm.job[qn + __popc(b1 & lt)] = DrawJob{q0, eidx, (uint32_t)node << 8};
-      if (nn >= 2)
-        sm.job[qn + c1 + __popc(b2 & lt)] = DrawJob{q0 + 1, eidx, 1u | ((uint32_t)node << 8)};
-      if (nn >= 3)
-        sm.job[qn + c1 + c2 + __popc(b3 & lt)] =
-            DrawJob{q0 + 2, eidx, 2u | ((uint32_t)node << 8)};
-      qn += add;
-      __syncwarp();
-      while (qn >= 32) {
-        drain_jobs(sm.job + (qn - 32), 32, lane, t, v0, (uint32_t)n, seed, prob_of_node, prob,
-                   slots);
-        qn -= 32;
+      cur += stot;
+      if (queued && jtot > 0) {
+        __syncwarp();  // the jobs are in shared memory
+        for (int i = lane; i < jtot; i += 32) {
+          const FillJob jb = job[i];
+          const uint32_t node = jb.jn >> 8;
+          slots[jb.q] = negative_slot(seed, jb.jn & 0xffu, t, jb.eidx, node, v0, (uint32_t)n,
+                                      prob_of_node, prob);
+        }
       }
     }
   }
-  __syncwarp();
-  drain_jobs(sm.job, qn, lane, t, v0, (uint32_t)n, seed, prob_of_node, prob, slots);
 }
 
 // Count pass (general path): warp per tile; each lane runs the
@@ -1726,7 +1741,8 @@ static bool build_slots(evoc_plan* pl, const float* inc_ps, const uint8_t* inc_u
   const ProbInfo* pinfo = pl->n_problems > 1 ? pl->prob.get() : nullptr;
   const uint64_t seed0 = pl->seeds.empty() ? 0 : pl->seeds[0];
   if (use_planes) {
-    k_plane_fill<<<(unsigned)(((int64_t)ne * pl->ntiles + 3) / 4), 128, 0, s>>>(
+    const int64_t ngroups = (ne + FILL_EPB - 1) / FILL_EPB;
+    k_plane_fill<<<(unsigned)(ngroups * pl->ntiles), 32 * FILL_EPB, 0, s>>>(
         pl->inc_ptr.get(), pl->inc_other.get(), pl->eidx_base.get(), n, pl->ntiles, planes_w,
         ne, fpl.get(), npl0.get(), npl1.get(), off.get(), pon, pinfo, seed0, pl->slots.get());
   } else {
