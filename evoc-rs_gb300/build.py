@@ -22,7 +22,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libevoc_gb300.so"
-ORACLE_SRC = ROOT / "oracle" / "evoc_oracle.cpp"
+ORACLE_SRCS = [ROOT / "oracle" / "evoc_oracle.cpp", ROOT / "oracle" / "evoc_labels_oracle.cpp"]
 ORACLE_LIB = ROOT / "oracle" / "liboracle.so"
 
 SOURCES = ["primitives.cu", "fuzzy_set.cu", "embed.cu", "capi.cu", "noalloc.cu", "measure.cu", "mlp.cu", "label_prop.cu"]
@@ -81,10 +81,10 @@ def build_library(verbose: bool = False, extra: list[str] | None = None) -> Path
 
 def build_oracle(verbose: bool = False) -> Path:
     """The oracle is test infrastructure: built for the tests and the CPU baseline."""
-    if _stale(ORACLE_LIB, [ORACLE_SRC]):
+    if _stale(ORACLE_LIB, ORACLE_SRCS):
         cxx = os.environ.get("CXX", "g++")
         _run([cxx, "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp",
-              "-ffp-contract=off", "-o", str(ORACLE_LIB), str(ORACLE_SRC)])
+              "-ffp-contract=off", "-o", str(ORACLE_LIB), *map(str, ORACLE_SRCS)])
     if verbose:
         print(f"built {ORACLE_LIB}")
     return ORACLE_LIB

@@ -13,7 +13,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "liboracle.so"
-SRC = HERE / "evoc_oracle.cpp"
+SRCS = [HERE / "evoc_oracle.cpp", HERE / "evoc_labels_oracle.cpp"]
 
 
 class OracleParams(C.Structure):
@@ -28,9 +28,9 @@ class OracleStats(C.Structure):
 
 
 def build() -> Path:
-    if not LIB.exists() or LIB.stat().st_mtime < SRC.stat().st_mtime:
+    if not LIB.exists() or any(LIB.stat().st_mtime < s.stat().st_mtime for s in SRCS):
         subprocess.run(["g++", "-O3", "-std=c++17", "-fPIC", "-shared", "-fopenmp",
-                        "-ffp-contract=off", "-o", str(LIB), str(SRC)], check=True)
+                        "-ffp-contract=off", "-o", str(LIB), *map(str, SRCS)], check=True)
     return LIB
 
 
@@ -69,6 +69,16 @@ def lib() -> C.CDLL:
             "oracle_lp_unit_range": ([vp, i64, i64], None),
             "oracle_lp_coarse_graph": ([vp, vp, vp, i64, vp, i64], vp),
             "oracle_lp_init": ([vp, vp, vp, i64, i32, vp, i64, u64, vp], C.c_int),
+            "oracle_build_mst": ([vp, i64, i64, i64, vp, vp, vp], i64),
+            "oracle_linkage": ([vp, vp, vp, i64, i64, vp, vp], None),
+            "oracle_leaf_labels": ([vp, i64, i64, i64, i64, vp, vp], i64),
+            "oracle_cluster_layers": ([vp, i64, i64, i64, i64, C.c_double, i64], vp),
+            "oracle_layers_count": ([vp], i64),
+            "oracle_layers_get": ([vp, i64, vp, vp, vp], None),
+            "oracle_layers_free": ([vp], None),
+            "oracle_find_peaks": ([vp, i64, vp], i64),
+            "oracle_barcodes": ([vp, i64, i64, i64, i64, vp, vp, vp, vp], i64),
+            "oracle_search_n_clusters": ([vp, i64, i64, i64, i64, vp, vp], i64),
         }
         for k, (a, r) in sigs.items():
             f = getattr(L, k)
@@ -272,3 +282,148 @@ def lp_init(indptr, indices, weights, dim: int, data=None, seed: int = 42) -> np
     if rc != 0:
         raise ValueError("oracle_lp_init: invalid arguments")
     return out
+
+
+# ---------------------------------------------------------------------------
+# Clustering of the embedding (evoc_labels_oracle.cpp): the reference's own
+# CPU stage after the embedding, restated to compare labels.
+# ---------------------------------------------------------------------------
+def _emb(embedding) -> np.ndarray:
+    e = np.ascontiguousarray(embedding, dtype=np.float32)
+    if e.ndim != 2:
+        raise ValueError("embedding must be n x dim")
+    return e
+
+
+def build_mst(embedding, min_samples: int = 5):
+    """Boruvka MST over mutual reachability (src/clustering/mst.rs:82-166):
+    (u, v, weight) arrays of the n - 1 edges in insertion order."""
+    e = _emb(embedding)
+    n, d = e.shape
+    m = max(n - 1, 0)
+    u = np.zeros(m, np.int64)
+    v = np.zeros(m, np.int64)
+    w = np.zeros(m, np.float32)
+    k = lib().oracle_build_mst(_p(e), n, d, int(min_samples), _p(u), _p(v), _p(w))
+    return u[:k], v[:k], w[:k]
+
+
+def linkage(u, v, w, n: int):
+    """mst_to_linkage_tree (src/clustering/linkage.rs:39-85): rows (left,
+    right, size) and distances."""
+    u = np.ascontiguousarray(u, np.int64)
+    v = np.ascontiguousarray(v, np.int64)
+    w = np.ascontiguousarray(w, np.float32)
+    m = len(u)
+    lr = np.zeros((m, 3), np.int64)
+    dist = np.zeros(m, np.float32)
+    lib().oracle_linkage(_p(u), _p(v), _p(w), m, int(n), _p(lr), _p(dist))
+    return lr, dist
+
+
+def leaf_labels(embedding, min_samples: int = 5, min_cluster_size: int = 5):
+    """Leaf clusters of the condensed tree at one min_cluster_size (the base
+    layer of build_cluster_layers): (labels, strengths, n_leaves)."""
+    e = _emb(embedding)
+    n, d = e.shape
+    lab = np.zeros(n, np.int64)
+    st = np.zeros(n, np.float32)
+    k = lib().oracle_leaf_labels(_p(e), n, d, int(min_samples), int(min_cluster_size), _p(lab),
+                                 _p(st))
+    return lab, st, int(k)
+
+
+def build_cluster_layers(embedding, min_samples: int = 5, base_min_cluster_size: int = 5,
+                         min_similarity_threshold: float = 0.2, max_layers: int = 10):
+    """build_cluster_layers (src/clustering/persistence.rs:387-463): lists of
+    per-layer labels, strengths and persistence scores, finest layer first."""
+    e = _emb(embedding)
+    n, d = e.shape
+    L = lib()
+    h = L.oracle_cluster_layers(_p(e), n, d, int(min_samples), int(base_min_cluster_size),
+                                float(min_similarity_threshold), int(max_layers))
+    labels, strengths, pers = [], [], []
+    try:
+        for i in range(L.oracle_layers_count(h)):
+            lab = np.zeros(n, np.int64)
+            st = np.zeros(n, np.float32)
+            p = C.c_double(0.0)
+            L.oracle_layers_get(h, i, _p(lab), _p(st), C.byref(p))
+            labels.append(lab)
+            strengths.append(st)
+            pers.append(p.value)
+    finally:
+        L.oracle_layers_free(h)
+    return labels, strengths, pers
+
+
+def best_labels(layers) -> np.ndarray:
+    """EvocResult::best_labels (src/lib.rs:124-137): the layer with the highest
+    persistence score (Iterator::max_by: the last of equal maxima), or the
+    only layer."""
+    labels, _, pers = layers
+    if len(labels) <= 1:
+        return labels[0]
+    best, bi = None, 0
+    for i, p in enumerate(pers):  # max_by keeps the last of equal maxima
+        if best is None or not (p < best):
+            best, bi = p, i
+    return labels[bi]
+
+
+def find_peaks(x) -> np.ndarray:
+    a = np.ascontiguousarray(x, np.float32)
+    out = np.zeros(max(len(a), 1), np.int64)
+    k = lib().oracle_find_peaks(_p(a), len(a), _p(out))
+    return out[:k]
+
+
+def barcodes(embedding, min_samples: int, min_cluster_size: int):
+    """min_cluster_size_barcode + compute_total_persistence: (barcodes as
+    rows of birth, death, parent, lambda_death; sizes; persistence)."""
+    e = _emb(embedding)
+    n, d = e.shape
+    bc = np.zeros((max(n, 1), 4), np.float64)
+    sizes = np.zeros(max(n, 1), np.float32)
+    pers = np.zeros(max(n, 1), np.float32)
+    ns = C.c_int64(0)
+    k = lib().oracle_barcodes(_p(e), n, d, int(min_samples), int(min_cluster_size), _p(bc),
+                              _p(sizes), _p(pers), C.byref(ns))
+    return bc[:k], sizes[:ns.value], pers[:ns.value]
+
+
+def search_for_n_clusters(embedding, min_samples: int, target_k: int):
+    """search_for_n_clusters (src/lib.rs:377-452): (labels, strengths, k)."""
+    e = _emb(embedding)
+    n, d = e.shape
+    lab = np.zeros(n, np.int64)
+    st = np.zeros(n, np.float32)
+    k = lib().oracle_search_n_clusters(_p(e), n, d, int(min_samples), int(target_k), _p(lab),
+                                       _p(st))
+    return lab, st, int(k)
+
+
+def adjusted_rand_index(a, b) -> float:
+    """Adjusted Rand index (Hubert and Arabie, 1985) of two labelings; every
+    label value (noise -1 included) is its own class, as in the usual
+    contingency-table formula."""
+    a = np.asarray(a)
+    b = np.asarray(b)
+    if a.shape != b.shape:
+        raise ValueError("labelings differ in length")
+    n = a.size
+    if n < 2:
+        return 1.0
+    _, ai = np.unique(a, return_inverse=True)
+    _, bi = np.unique(b, return_inverse=True)
+    cont = np.zeros((ai.max() + 1, bi.max() + 1), np.int64)
+    np.add.at(cont, (ai, bi), 1)
+    comb = lambda x: x * (x - 1) / 2.0
+    s_ij = comb(cont.astype(np.float64)).sum()
+    s_a = comb(cont.sum(1).astype(np.float64)).sum()
+    s_b = comb(cont.sum(0).astype(np.float64)).sum()
+    expected = s_a * s_b / comb(float(n))
+    mx = 0.5 * (s_a + s_b)
+    if mx == expected:
+        return 1.0
+    return float((s_ij - expected) / (mx - expected))

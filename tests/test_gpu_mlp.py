@@ -246,6 +246,15 @@ def test_warm_start_beats_random_init_at_reduced_epochs(ctx):
     qr = WS.quality(ev["x"], rand, ev["labels"], n_queries=1024)
     print("warm", qw, "random", qr)
     assert qw["trustworthiness"] > qr["trustworthiness"]
+    # final labels (the reference's clustering stage, restated in the oracle)
+    # against those of the plain method (random init, 50 epochs)
+    import oracle as O
+    plain = WS.embed_device(ctx, g, ev["n"], 8, 50, 777)
+    lab = lambda e: O.best_labels(O.build_cluster_layers(e.cpu().numpy(), 5, 5, 0.2, 10))
+    lp = lab(plain)
+    ari_w, ari_r = O.adjusted_rand_index(lab(warm), lp), O.adjusted_rand_index(lab(rand), lp)
+    print("labels ARI vs the plain method: warm start", ari_w, "random init", ari_r)
+    assert ari_w > ari_r
 
 
 def test_bounded_wait_times_out_and_the_context_survives(ctx):

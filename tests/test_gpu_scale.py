@@ -8,7 +8,8 @@ exact cosine kNN graph built on the GPU (input preparation, untimed). Then:
   oracle's bit for bit: sigma, rho, CSR structure, neighbour order, weights;
 * the full 50-epoch embedding (src/graph/embedding.rs:48-298, default
   parameters, random init) must equal the oracle's bit for bit, and so must a
-  one-epoch gradient from a perturbed state.
+  one-epoch gradient from a perturbed state; the final cluster labels of the
+  two embeddings must reach an adjusted Rand index of at least 0.98.
 
 A second case puts hub nodes of degree 16,500 and 20,000 (the degree profile
 of the 2M-point graph, whose largest degree is 16,487) next to ordinary rows;
@@ -66,11 +67,17 @@ def test_fuzzy_set_200k_vs_oracle(ctx, knn_200k, graph_200k):
 
 
 def test_embedding_200k_vs_oracle(ctx, oracle, graph_200k):
-    """The full default run: 50 epochs, dim 8, random init, seed 1."""
+    """The full default run: 50 epochs, dim 8, random init, seed 1; then the
+    final labels (src/clustering/*.rs via the oracle's restatement) of both
+    embeddings: adjusted Rand index >= 0.98 (they are identical)."""
     g, (ip, ix, w), _, _ = graph_200k
     gpu = ctx.embed(g, 8, seed=1)
     ref = oracle.evoc_embedding(ip, ix, w, 8, seed=1)
     _assert_bits(gpu, ref, "embedding")
+    lg = oracle.best_labels(oracle.build_cluster_layers(gpu, 5, 5, 0.2, 10))
+    lr = oracle.best_labels(oracle.build_cluster_layers(ref, 5, 5, 0.2, 10))
+    assert oracle.adjusted_rand_index(lg, lr) >= 0.98
+    assert np.array_equal(lg, lr)
 
 
 def test_gradient_200k_vs_oracle(ctx, oracle, graph_200k):
