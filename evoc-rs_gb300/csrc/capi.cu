@@ -168,6 +168,8 @@ int evoc_ctx_create(int device, evoc_ctx_t** out) {
   EVOC_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
   c->status.alloc(1, c->stream);
   EVOC_CUDA(cudaMemsetAsync(c->status.get(), 0, sizeof(int32_t), c->stream));
+  c->sk_steps.alloc(1, c->stream);
+  EVOC_CUDA(cudaMemsetAsync(c->sk_steps.get(), 0, sizeof(unsigned long long), c->stream));
   EVOC_CUDA(cudaStreamSynchronize(c->stream));
   *out = c.release();
   EVOC_API_END(ctx)
@@ -178,6 +180,7 @@ void evoc_ctx_destroy(evoc_ctx_t* ctx) {
   cudaSetDevice(ctx->device);
   cudaStream_t s = ctx->stream;
   ctx->status.release();
+  ctx->sk_steps.release();
   ctx->slot_cache.release();
   if (s) {
     cudaStreamSynchronize(s);
@@ -192,6 +195,18 @@ const char* evoc_last_error(const evoc_ctx_t* ctx) {
 
 void* evoc_ctx_stream(const evoc_ctx_t* ctx) {
   return ctx ? (void*)ctx->stream : nullptr;
+}
+
+int evoc_ctx_smooth_knn_steps(evoc_ctx_t* ctx, int64_t* steps) {
+  EVOC_API_BEGIN
+  if (!ctx || !steps) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL argument");
+  use_device(ctx);
+  unsigned long long v = 0;
+  EVOC_CUDA(cudaMemcpyAsync(&v, ctx->sk_steps.get(), sizeof(v), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+  EVOC_CUDA(cudaStreamSynchronize(ctx->stream));
+  *steps = (int64_t)v;
+  EVOC_API_END(ctx)
 }
 
 int evoc_smooth_knn_dist(evoc_ctx_t* ctx, const float* dists,

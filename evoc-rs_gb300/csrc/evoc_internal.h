@@ -145,6 +145,9 @@ struct evoc_ctx {
   // that fits in it (stream order makes the reuse safe): repeated one-shot
   // embeddings skip a multi-gigabyte allocation each.
   evoc::DevBuf<uint2> slot_cache;
+  // Row-sum evaluations (bisection steps over all rows) of the most recent
+  // smooth_knn pass on this context: the work figure of its ALU bound.
+  evoc::DevBuf<unsigned long long> sk_steps;
 };
 
 struct evoc_graph {

@@ -10,11 +10,13 @@
 // Pipeline (all on the context stream):
 //   k_knn_rowlen     warp per row: row length (first EVOC_KNN_PAD) and index
 //                    validation.
-//   k_smooth_knn     thread per row: rho, the sigma bisection with the row's
-//                    distances staged in shared memory, then the membership
-//                    weights. The sum over the row is serial in row order, as
-//                    in the reference (fuzzy_graph.rs:72-76), so sigma is
-//                    bit-identical to a serial CPU evaluation.
+//   k_smooth_knn     lane per row (a pool of rows per warp, a finished lane
+//                    takes the next): rho and the sigma bisection with the
+//                    rows' distances staged in shared memory. The sum over the
+//                    row is serial in row order, as in the reference
+//                    (fuzzy_graph.rs:72-76), so sigma is bit-identical to a
+//                    serial CPU evaluation.
+//   k_knn_weights    elementwise membership weights (fuzzy_graph.rs:138-145).
 //   k_forward_rows   thread per row: drop self loops, sort by column keeping
 //                    the last of equal columns (HashMap::insert overwrites,
 //                    fuzzy_graph.rs:189), count in-degrees.
@@ -62,100 +64,161 @@ __global__ void k_knn_rowlen(const uint32_t* __restrict__ idx, int64_t n,
 }
 
 // ---------------------------------------------------------------------------
-// smooth_knn_dist + membership weights (thread per row).
-// Shared memory holds R rows with an odd stride kp so that threads reading
-// the same column index of different rows hit different banks.
+// smooth_knn_dist (fuzzy_graph.rs:33-98): rho and the sigma bisection, one
+// row per lane at a time. The sum over the row stays serial in row order, so
+// sigma is bit-identical to a serial CPU evaluation. Rows need different
+// numbers of bisection steps (a handful up to n_iter), so instead of one row
+// per lane for the whole launch, each warp owns a pool of rows staged in
+// shared memory (odd row stride: lanes on different rows hit different banks)
+// and a lane that finishes its row takes the pool's next one at the end of
+// the step; the warp runs about the mean step count of its rows rather than
+// their maximum. The membership weights are a separate elementwise pass.
 // ---------------------------------------------------------------------------
-__global__ void k_smooth_knn(const float* __restrict__ dist,
-                             const int32_t* __restrict__ row_len, int64_t n,
-                             int32_t k, int32_t kp, double target, float lc,
-                             int32_t n_iter, float* __restrict__ sigma_out,
-                             float* __restrict__ rho_out,
-                             float* __restrict__ w_out,
-                             int32_t* __restrict__ status) {
-  extern __shared__ float sm[];
-  const int R = blockDim.x;
-  const int64_t row0 = (int64_t)blockIdx.x * R;
-  const int64_t rows_here = min((int64_t)R, n - row0);
-  const int64_t elems = rows_here * k;
-  const float* src = dist + row0 * (int64_t)k;
-  for (int64_t e = threadIdx.x; e < elems; e += R) {
-    const int64_t r = e / k;
-    sm[r * kp + (e - r * k)] = src[e];
-  }
-  __syncthreads();
-  const int64_t i = row0 + threadIdx.x;
-  if (threadIdx.x < rows_here) {
-    float* d = sm + threadIdx.x * kp;
-    const int32_t len = row_len ? row_len[i] : k;
-    bool ok = true;
-    for (int32_t j = 0; j < len; ++j)
-      if (d[j] != d[j]) ok = false;
-    if (!ok) set_status(status, ST_BAD_VALUE);
-    float rho = 0.0f;
-    if (lc > 0.0f) {  // fuzzy_graph.rs:49-62
-      if (len <= 0) {
-        set_status(status, ST_EMPTY_ROW);
-        ok = false;
-      } else {
-        const float lm1 = max0(fsub(lc, 1.0f));
-        const float fl = floorf(lm1);
-        int64_t id = (int64_t)fl;
-        if (id > len - 1) id = len - 1;
-        const float frac = fsub(lm1, fl);
-        if (frac > 0.0f && id + 1 < len)
-          rho = fadd(fmul(d[id], fsub(1.0f, frac)), fmul(d[id + 1], frac));
-        else
-          rho = d[id];
-      }
+constexpr int SK_WARPS = 4;
+
+struct RowState {
+  int32_t row;   // pool slot, or >= pool size when the lane is done
+  int32_t len;
+  int32_t it;
+  float rho, lo, hi, mid;
+};
+
+__device__ __forceinline__ void sk_start_row(RowState& st, const float* __restrict__ d,
+                                             int32_t len, float lc, int32_t* __restrict__ status,
+                                             bool& ok) {
+  st.len = len;
+  st.it = 0;
+  st.lo = 0.0f;
+  st.hi = 3.40282347e+38f;
+  st.mid = 1.0f;
+  ok = true;
+  for (int32_t j = 0; j < len; ++j)
+    if (d[j] != d[j]) ok = false;
+  if (!ok) set_status(status, ST_BAD_VALUE);
+  float rho = 0.0f;
+  if (lc > 0.0f) {  // fuzzy_graph.rs:49-62
+    if (len <= 0) {
+      set_status(status, ST_EMPTY_ROW);
+      ok = false;
+    } else {
+      const float lm1 = max0(fsub(lc, 1.0f));
+      const float fl = floorf(lm1);
+      int64_t id = (int64_t)fl;
+      if (id > len - 1) id = len - 1;
+      const float frac = fsub(lm1, fl);
+      if (frac > 0.0f && id + 1 < len)
+        rho = fadd(fmul(d[id], fsub(1.0f, frac)), fmul(d[id + 1], frac));
+      else
+        rho = d[id];
     }
-    float lo = 0.0f, hi = 3.40282347e+38f, mid = 1.0f;
-    if (ok) {
-      for (int32_t it = 0; it < n_iter; ++it) {  // fuzzy_graph.rs:71-93
+  }
+  st.rho = rho;
+}
+
+__global__ void __launch_bounds__(32 * SK_WARPS) k_smooth_knn(
+    const float* __restrict__ dist, const int32_t* __restrict__ row_len, int64_t n, int32_t k,
+    int32_t kp, int32_t pool, double target, float lc, int32_t n_iter,
+    float* __restrict__ sigma_out, float* __restrict__ rho_out, int32_t* __restrict__ status,
+    unsigned long long* __restrict__ steps) {
+  extern __shared__ float sm[];
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float* sd = sm + (size_t)wid * pool * kp;
+  const int64_t row0 = ((int64_t)blockIdx.x * SK_WARPS + wid) * pool;
+  if (row0 >= n) return;  // whole warp
+  const int rows = (int)min((int64_t)pool, n - row0);
+  {
+    const float* src = dist + row0 * (int64_t)k;
+    const int64_t elems = (int64_t)rows * k;
+    for (int64_t e = lane; e < elems; e += 32) {
+      const int64_t r = e / k;
+      sd[r * kp + (e - r * k)] = src[e];
+    }
+  }
+  __syncwarp();
+  const uint32_t lt = (1u << lane) - 1u;
+  RowState st;
+  bool ok = false;
+  st.row = lane;
+  int next = 32;  // the pool's next unstarted row (warp-uniform)
+  uint32_t nsteps = 0;  // row sums evaluated by this lane
+  if (st.row < rows) {
+    sk_start_row(st, sd + st.row * kp, row_len ? row_len[row0 + st.row] : k, lc, status, ok);
+  }
+  for (;;) {
+    const bool active = st.row < rows;
+    if (__ballot_sync(FULL, active) == 0) break;
+    bool done = false;
+    if (active) {
+      if (!ok) {
+        st.mid = 0.0f;
+        st.rho = 0.0f;
+        done = true;
+      } else if (st.it >= n_iter) {
+        done = true;
+      } else {  // one bisection step, fuzzy_graph.rs:71-93
+        const float* d = sd + st.row * kp;
+        ++nsteps;
         float val = 0.0f;
-        for (int32_t j = 0; j < len; ++j) {
-          const float adjusted = max0(fsub(d[j], rho));
-          val = fadd(val, evoc_expf(-fdiv(adjusted, mid)));
+        for (int32_t j = 0; j < st.len; ++j) {
+          const float adjusted = max0(fsub(d[j], st.rho));
+          val = fadd(val, evoc_expf(-fdiv(adjusted, st.mid)));
         }
         const double vd = (double)val;
-        if (fabs(vd - target) < 1e-5) break;
-        if (vd > target) {
-          hi = mid;
-          mid = fdiv(fadd(lo, hi), 2.0f);
+        if (fabs(vd - target) < 1e-5) {
+          done = true;
         } else {
-          lo = mid;
-          if (hi == 3.40282347e+38f)
-            mid = fmul(mid, 2.0f);
-          else
-            mid = fdiv(fadd(lo, hi), 2.0f);
+          if (vd > target) {
+            st.hi = st.mid;
+            st.mid = fdiv(fadd(st.lo, st.hi), 2.0f);
+          } else {
+            st.lo = st.mid;
+            if (st.hi == 3.40282347e+38f)
+              st.mid = fmul(st.mid, 2.0f);
+            else
+              st.mid = fdiv(fadd(st.lo, st.hi), 2.0f);
+          }
+          ++st.it;
         }
       }
-    } else {
-      mid = 0.0f;
-      rho = 0.0f;
-    }
-    sigma_out[i] = mid;
-    rho_out[i] = rho;
-    if (w_out) {  // knn_to_coo weights, fuzzy_graph.rs:138-145
-      for (int32_t j = 0; j < len; ++j) {
-        const float adjusted = max0(fsub(d[j], rho));
-        float w;
-        if (mid > 0.0f)
-          w = evoc_expf(-fdiv(adjusted, mid));
-        else
-          w = (adjusted > 0.0f) ? 0.0f : 1.0f;
-        d[j] = w;
+      if (done) {
+        sigma_out[row0 + st.row] = st.mid;
+        rho_out[row0 + st.row] = st.rho;
       }
     }
-  }
-  if (w_out) {
-    __syncthreads();
-    float* dst = w_out + row0 * (int64_t)k;
-    for (int64_t e = threadIdx.x; e < elems; e += R) {
-      const int64_t r = e / k;
-      dst[e] = sm[r * kp + (e - r * k)];
+    // lanes whose row is done take the pool's next rows, in lane order
+    const uint32_t need = __ballot_sync(FULL, done);
+    if (done) {
+      st.row = next + __popc(need & lt);
+      if (st.row < rows)
+        sk_start_row(st, sd + st.row * kp, row_len ? row_len[row0 + st.row] : k, lc, status, ok);
     }
+    next += __popc(need);
   }
+  const unsigned tot = __reduce_add_sync(FULL, nsteps);
+  if (lane == 0 && tot) atomicAdd(steps, (unsigned long long)tot);
+}
+
+// knn_to_coo's membership weights (fuzzy_graph.rs:138-145), elementwise:
+// w = exp(-max(0, d - rho) / sigma), or 0 / 1 when sigma <= 0.
+__global__ void k_knn_weights(const float* __restrict__ dist, const int32_t* __restrict__ row_len,
+                              int64_t n, int32_t k, const float* __restrict__ sigma,
+                              const float* __restrict__ rho, float* __restrict__ w) {
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= n * (int64_t)k) return;
+  const int64_t i = e / k;
+  const int32_t j = (int32_t)(e - i * k);
+  const int32_t len = row_len ? row_len[i] : k;
+  float out = 0.0f;
+  if (j < len) {
+    const float mid = sigma[i];
+    const float adjusted = max0(fsub(dist[e], rho[i]));
+    if (mid > 0.0f)
+      out = evoc_expf(-fdiv(adjusted, mid));
+    else
+      out = (adjusted > 0.0f) ? 0.0f : 1.0f;
+  }
+  w[e] = out;
 }
 
 // ---------------------------------------------------------------------------
@@ -401,17 +464,27 @@ void smooth_knn_device(evoc_ctx* ctx, const float* d_dist,
                        float* d_weights_out, const uint32_t* /*unused*/) {
   if (n == 0) return;
   const int32_t kp = k | 1;
-  const int R = rows_per_block(kp);
-  const size_t smem = (size_t)R * kp * sizeof(float);
+  // rows per warp: 64 where they fit in 48 KB per block, else one per lane
+  int pool = 64;
+  while (pool > 32 && (size_t)SK_WARPS * pool * kp * sizeof(float) > 48 * 1024) pool /= 2;
+  const size_t smem = (size_t)SK_WARPS * pool * kp * sizeof(float);
   if (smem > 200 * 1024)
-    throw Error(EVOC_ERR_UNSUPPORTED, "k too large (k <= 1599 supported)");
+    throw Error(EVOC_ERR_UNSUPPORTED, "k too large (k <= 399 supported)");
   set_smem_limit((const void*)k_smooth_knn, smem);
   const double target = std::log2((double)k_target);
-  const int64_t blocks = (n + R - 1) / R;
-  k_smooth_knn<<<(unsigned)blocks, R, smem, ctx->stream>>>(
-      d_dist, d_row_len, n, k, kp, target, local_connectivity, n_iter, d_sigma,
-      d_rho, d_weights_out, ctx->status.get());
+  const int64_t per_block = (int64_t)SK_WARPS * pool;
+  const int64_t blocks = (n + per_block - 1) / per_block;
+  EVOC_CUDA(cudaMemsetAsync(ctx->sk_steps.get(), 0, sizeof(unsigned long long), ctx->stream));
+  k_smooth_knn<<<(unsigned)blocks, 32 * SK_WARPS, smem, ctx->stream>>>(
+      d_dist, d_row_len, n, k, kp, pool, target, local_connectivity, n_iter, d_sigma, d_rho,
+      ctx->status.get(), ctx->sk_steps.get());
   EVOC_CHECK_LAUNCH();
+  if (d_weights_out) {
+    const int64_t elems = n * (int64_t)k;
+    k_knn_weights<<<(unsigned)((elems + 255) / 256), 256, 0, ctx->stream>>>(
+        d_dist, d_row_len, n, k, d_sigma, d_rho, d_weights_out);
+    EVOC_CHECK_LAUNCH();
+  }
 }
 
 void fuzzy_set_device(evoc_ctx* ctx, const uint32_t* d_idx,

@@ -51,7 +51,7 @@ EXPORTED = [
     "evoc_mlp_n_params", "evoc_mlp_get_params", "evoc_mlp_set_params", "evoc_mlp_predict",
     "evoc_mlp_predict_device", "evoc_mlp_gradients", "evoc_mlp_fit_device",
     "evoc_to_bf16_device", "evoc_procrustes", "evoc_fuzzy_set_device_raw",
-    "evoc_label_prop_partition", "evoc_selftest_wait_timeout",
+    "evoc_label_prop_partition", "evoc_selftest_wait_timeout", "evoc_ctx_smooth_knn_steps",
 ]
 
 
@@ -152,6 +152,7 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "evoc_ctx_destroy": ([vp], None),
         "evoc_last_error": ([vp], C.c_char_p),
         "evoc_ctx_stream": ([vp], C.c_void_p),
+        "evoc_ctx_smooth_knn_steps": ([vp, C.POINTER(C.c_int64)], C.c_int),
         "evoc_smooth_knn_dist": ([vp, vp, vp, i64, i32, u64, f32, i32, vp, vp], C.c_int),
         "evoc_fuzzy_set": ([vp, vp, vp, i64, i32, f32, C.c_int, pp], C.c_int),
         "evoc_fuzzy_set_device": ([vp, vp, vp, i64, i32, f32, C.c_int, vp, vp, pp], C.c_int),
@@ -446,6 +447,13 @@ class Context:
         g = C.c_double()
         self._check(self.lib.evoc_gather_peak(self.handle, int(nbytes), C.byref(g)))
         return g.value
+
+    def smooth_knn_steps(self) -> int:
+        """Row-sum evaluations (bisection steps over all rows) of the most
+        recent smooth_knn_dist pass on this context."""
+        v = C.c_int64()
+        self._check(self.lib.evoc_ctx_smooth_knn_steps(self.handle, C.byref(v)))
+        return v.value
 
     @property
     def stream(self) -> int:

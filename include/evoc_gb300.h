@@ -114,6 +114,12 @@ EVOC_API const char* evoc_last_error(const evoc_ctx_t* ctx);
  * work or events around the library's (no counterpart). */
 EVOC_API void* evoc_ctx_stream(const evoc_ctx_t* ctx);
 
+/* Bisection steps of the most recent smooth_knn_dist pass on ctx (by
+ * evoc_smooth_knn_dist or a fuzzy set): the number of row-sum evaluations
+ * over all rows, each of which evaluates one exp per row entry. A work
+ * count for measurement (no counterpart). */
+EVOC_API int evoc_ctx_smooth_knn_steps(evoc_ctx_t* ctx, int64_t* steps);
+
 /* ---- fuzzy simplicial set ------------------------------------------------ */
 
 /* smooth_knn_dist (src/graph/fuzzy_graph.rs:33-98) on host arrays.
