@@ -290,6 +290,7 @@ def run_ours(args) -> dict:
     graph = ctx.fuzzy_set_device(idx32.data_ptr(), dist.data_ptr(), n, k, float(k), True)
     fuzzy_s = time.time() - t
     plan = ctx.plan(graph, dim, params, seed=cfg["seed"])
+    tuned = plan.autotune()  # also applies to later plans of this shape (e2e, set-up timing)
     stats = plan.stats()
     n_epochs = params.n_epochs
     fired_per_step = float(stats[:, 0].sum())
@@ -378,6 +379,7 @@ def run_ours(args) -> dict:
                 "kernel": "k_epoch_slot" if info["n_slots"] else "k_epoch",
                 "launch_ms": round(t_launch * 1e3, 4), "warps_per_block": info["warps_per_block"],
                 "epoch_path": "slots" if info["n_slots"] else "bit-planes",
+                "autotuned": tuned,
                 "hbm": hbm, "l2": l2,
                 "roofline_ms": round(t_roof * 1e3, 4),
                 "frac_of_roofline": round(t_roof / t_launch, 4)}
@@ -490,6 +492,7 @@ def run_batched(args) -> dict:
     graphs = [ctx.fuzzy_set_device(i.data_ptr(), d.data_ptr(), i.shape[0], k, float(k), True)
               for i, d in probs]
     plan = ctx.plan_batched(graphs, dim, params, seeds=seeds)
+    tuned = plan.autotune()
     stats = plan.stats()
     fired_per_step = float(stats[:, 0].sum())
     n_tot = plan.n
@@ -525,6 +528,25 @@ def run_batched(args) -> dict:
             gb.free()
         torch.cuda.synchronize()
         e2e_s = (time.perf_counter() - t) / e2e_steps
+        # the same 256 problems one by one through the plain GPU path (the C
+        # ABI's fuzzy set and embedding per problem, host buffers)
+        outs_h = [np.empty((sz, dim), np.float32) for sz in sizes_h]
+        ctx.embed(ctx.fuzzy_set(*host[0], float(k), True), dim, params, seed=seeds[0],
+                  out=outs_h[0])  # warm-up
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for q, (ih, dh) in enumerate(host):
+            gq = ctx.fuzzy_set(ih, dh, float(k), True)
+            ctx.embed(gq, dim, params, seed=seeds[q], out=outs_h[q])
+            gq.free()
+        torch.cuda.synchronize()
+        one_by_one_s = time.perf_counter() - t
+        # the batched run's blocks equal the separate runs
+        gb = ctx.fuzzy_set_batched(host, float(k), True)
+        blk = ctx.embed_blocks(gb, sizes_h, dim, params, seeds=seeds)
+        gb.free()
+        same_as_separate = all(np.array_equal(a.view(np.uint32), b.view(np.uint32))
+                               for a, b in zip(blk, outs_h))
     ms_step = ms_total / args.steps
     epoch_ms = plan.profile_epochs(None, out.data_ptr())
     info = plan.info()
@@ -551,6 +573,13 @@ def run_batched(args) -> dict:
         "e2e": {"value": fired_per_step / e2e_s, "unit": UNIT, "ms_per_step": round(e2e_s * 1e3, 3),
                 "h2d_bytes_per_step": int(sum(sizes) * k * 8),
                 "d2h_bytes_per_step": int(sum(sizes) * dim * 4)},
+        "one_by_one": {"ms": round(one_by_one_s * 1e3, 2),
+                       "speedup_of_batched_e2e": round(one_by_one_s / e2e_s, 3),
+                       "blocks_equal_separate_runs": bool(same_as_separate),
+                       "note": "the same 256 problems through evoc_fuzzy_set + evoc_embed one "
+                               "problem at a time (host buffers), against the batched e2e step "
+                               "(evoc_fuzzy_set_batched + evoc_embed_blocks)"},
+        "autotuned": tuned,
         "gpu_launches": int(args.steps * (params.n_epochs + 2)),
         "roofline": {"bound": "hbm", "achieved": round(bytes_launch / t_launch / 1e9, 1),
                      "peak": pk["hbm_gbs"], "unit": "GB/s",

@@ -561,6 +561,25 @@ int evoc_plan_info(const evoc_plan_t* plan, int64_t* n_edges,
   return EVOC_OK;
 }
 
+int evoc_plan_set_config(evoc_plan_t* plan, int32_t variant, int32_t warps_per_block,
+                         int32_t blocks_per_sm) {
+  evoc_ctx* ctx = plan ? evoc::plan_ctx(plan) : nullptr;
+  EVOC_API_BEGIN
+  if (!plan) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL plan");
+  use_device(ctx);
+  evoc::plan_configure(plan, variant, warps_per_block, blocks_per_sm);
+  EVOC_API_END(ctx)
+}
+
+int evoc_plan_autotune(evoc_plan_t* plan, int32_t* config, float* ms_per_launch) {
+  evoc_ctx* ctx = plan ? evoc::plan_ctx(plan) : nullptr;
+  EVOC_API_BEGIN
+  if (!plan) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL plan");
+  use_device(ctx);
+  evoc::plan_autotune(plan, config, ms_per_launch);
+  EVOC_API_END(ctx)
+}
+
 int evoc_plan_stats(const evoc_plan_t* plan, evoc_epoch_stats_t* stats) {
   evoc_ctx* ctx = plan ? evoc::plan_ctx(plan) : nullptr;
   EVOC_API_BEGIN

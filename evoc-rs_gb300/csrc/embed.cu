@@ -39,7 +39,11 @@
 #include <cstdlib>
 #include <cstring>
 #include <chrono>
+#include <fstream>
+#include <map>
 #include <memory>
+#include <mutex>
+#include <sstream>
 #include <string>
 #include <utility>
 
@@ -92,6 +96,8 @@ struct evoc_plan {
   evoc::DevBuf<uint2> slots;
   evoc::DevBuf<unsigned long long> work_ctr;  // per epoch
   unsigned slot_grid = 0;                     // persistent grid of the slots kernel
+  int32_t kvariant = 0;                       // slots-kernel variant (SLOT_VARIANTS)
+  int32_t blocks_per_sm = 0;                  // persistent blocks per SM (0: as many as fit)
   bool stats_done = false;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -1288,15 +1294,13 @@ __global__ void k_slot_stats(const int64_t* __restrict__ tile_off,
 // SLOT_PARTS lanes, each adding its DIMP / SLOT_PARTS dims of the node's run,
 // in slot order, onto the node's running gradient in shared memory.
 // Then Adam (embedding.rs:256-272), lane per node.
-constexpr int SLOT_WIN = 128;
-constexpr int SLOT_U = 2;
 template <int DIMP>
 constexpr int slot_parts() { return DIMP >= 8 ? 2 : 1; }
 
-template <int DIMP>
+template <int DIMP, int WIN>
 struct alignas(16) SlotSmem {
   float rows[TILE][DIMP];      // e_cur rows of the tile's nodes
-  float c[SLOT_WIN][DIMP];     // contributions of the window's slots
+  float c[WIN][DIMP];          // contributions of the window's slots
   float S[TILE][DIMP];         // running gradients
   int32_t start[TILE];         // first window slot of each node's run (or none)
   int32_t end[TILE];           // one past its last
@@ -1336,8 +1340,8 @@ __device__ __forceinline__ void slot_contrib(float (&c)[DIMP], bool neg,
 }
 
 // Phase 1 for U slots per lane: window slots ib + 32 u + lane, u < U.
-template <int DIMP, int U>
-__device__ __forceinline__ void slot_group(const EpochArgs& a, SlotSmem<DIMP>& sm,
+template <int DIMP, int WIN, int U>
+__device__ __forceinline__ void slot_group(const EpochArgs& a, SlotSmem<DIMP, WIN>& sm,
                                            const uint2* __restrict__ wslots, int ib, int wn,
                                            int lane, int& carry, uint32_t& act_mask,
                                            float two_noise, float gamma4) {
@@ -1378,8 +1382,8 @@ __device__ __forceinline__ void slot_group(const EpochArgs& a, SlotSmem<DIMP>& s
   }
 }
 
-template <int DIMP>
-__device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP>& sm, int64_t tile,
+template <int DIMP, int WIN, int SU>
+__device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP, WIN>& sm, int64_t tile,
                                           int lane) {
   const unsigned FULL = 0xffffffffu;
   const int64_t v0 = tile * TILE;
@@ -1396,21 +1400,21 @@ __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP>& sm
   const float two_noise = fmul(2.0f, a.noise);
   const float gamma4 = fmul(a.gamma, 4.0f);
   uint32_t act_mask = 0;
-  for (int64_t w0 = s0; w0 < s1; w0 += SLOT_WIN) {
-    const int wn = (int)min((int64_t)SLOT_WIN, s1 - w0);
+  for (int64_t w0 = s0; w0 < s1; w0 += WIN) {
+    const int wn = (int)min((int64_t)WIN, s1 - w0);
     const uint2* wslots = a.slots + w0;
-    sm.start[lane] = SLOT_WIN;  // none
+    sm.start[lane] = WIN;  // none
     __syncwarp();
     int carry = -1;  // node of the previous slot of the window
     int ib = 0;
-    for (; ib + 32 * SLOT_U <= wn; ib += 32 * SLOT_U)
-      slot_group<DIMP, SLOT_U>(a, sm, wslots, ib, wn, lane, carry, act_mask, two_noise, gamma4);
+    for (; ib + 32 * SU <= wn; ib += 32 * SU)
+      slot_group<DIMP, WIN, SU>(a, sm, wslots, ib, wn, lane, carry, act_mask, two_noise, gamma4);
     for (; ib < wn; ib += 32)
-      slot_group<DIMP, 1>(a, sm, wslots, ib, wn, lane, carry, act_mask, two_noise, gamma4);
+      slot_group<DIMP, WIN, 1>(a, sm, wslots, ib, wn, lane, carry, act_mask, two_noise, gamma4);
     __syncwarp();
     // run of node l: [start[l], first start of a later node or wn)
     const int st = sm.start[lane];
-    int sfx = (st == SLOT_WIN) ? wn : st;
+    int sfx = (st == WIN) ? wn : st;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const int y = __shfl_down_sync(FULL, sfx, o);
@@ -1419,7 +1423,7 @@ __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP>& sm
     int en = __shfl_down_sync(FULL, sfx, 1);
     if (lane == 31) en = wn;
     sm.end[lane] = en;
-    const uint32_t present = __ballot_sync(FULL, st != SLOT_WIN);
+    const uint32_t present = __ballot_sync(FULL, st != WIN);
     __syncwarp();
     constexpr int PARTS = slot_parts<DIMP>(), PD = DIMP / PARTS;  // dims per lane
     const int ntask = __popc(present) * PARTS;
@@ -1499,18 +1503,18 @@ using EpochKernel = void (*)(EpochArgs);
 
 // Register cap: 7 blocks of 128 threads per SM (72 registers) for DIMP <= 8
 // measured fastest; the occupancy it buys outweighs per-warp parallelism.
-template <int DIMP>
+template <int DIMP, int WIN, int SU>
 __global__ void __launch_bounds__(128, DIMP <= 8 ? 7 : 4) k_epoch_slot(EpochArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31;
-  SlotSmem<DIMP>& sm = reinterpret_cast<SlotSmem<DIMP>*>(smem_raw)[threadIdx.x >> 5];
+  SlotSmem<DIMP, WIN>& sm = reinterpret_cast<SlotSmem<DIMP, WIN>*>(smem_raw)[threadIdx.x >> 5];
   const int64_t ntiles = ((int64_t)a.n_total + TILE - 1) / TILE;
   for (;;) {
     unsigned long long w = 0;
     if (lane == 0) w = atomicAdd(a.work_ctr, 1ull);
     w = __shfl_sync(0xffffffffu, w, 0);
     if ((int64_t)w >= ntiles) break;
-    slot_tile<DIMP>(a, sm, (int64_t)a.tile_order[w], lane);
+    slot_tile<DIMP, WIN, SU>(a, sm, (int64_t)a.tile_order[w], lane);
   }
 }
 
@@ -1527,17 +1531,38 @@ size_t tile_smem(int dimp) {
   return sizeof(TileSmem<16>);
 }
 
-EpochKernel pick_slot_kernel(int dimp) {
-  if (dimp == 4) return k_epoch_slot<4>;
-  if (dimp == 8) return k_epoch_slot<8>;
-  if (dimp == 16) return k_epoch_slot<16>;
-  return nullptr;
-}
+// Variants of the slots kernel: (slot window, slots per lane per group). All
+// give identical results; the autotuner picks one per plan shape.
+struct SlotVariant {
+  int win, u;
+};
+constexpr SlotVariant SLOT_VARIANTS[] = {{128, 2}, {64, 2}, {256, 2}, {128, 1}};
+constexpr int N_SLOT_VARIANTS = 4;
 
-size_t slot_smem(int dimp) {
-  if (dimp == 4) return sizeof(SlotSmem<4>);
-  if (dimp == 8) return sizeof(SlotSmem<8>);
-  return sizeof(SlotSmem<16>);
+template <int WIN, int SU>
+EpochKernel pick_slot_wu(int dimp) {
+  if (dimp == 4) return k_epoch_slot<4, WIN, SU>;
+  if (dimp == 8) return k_epoch_slot<8, WIN, SU>;
+  return k_epoch_slot<16, WIN, SU>;
+}
+EpochKernel pick_slot_kernel(int dimp, int kv) {
+  switch (kv) {
+    case 1: return pick_slot_wu<64, 2>(dimp);
+    case 2: return pick_slot_wu<256, 2>(dimp);
+    case 3: return pick_slot_wu<128, 1>(dimp);
+    default: return pick_slot_wu<128, 2>(dimp);
+  }
+}
+template <int WIN>
+size_t slot_smem_w(int dimp) {
+  if (dimp == 4) return sizeof(SlotSmem<4, WIN>);
+  if (dimp == 8) return sizeof(SlotSmem<8, WIN>);
+  return sizeof(SlotSmem<16, WIN>);
+}
+size_t slot_smem(int dimp, int kv) {
+  const int win = SLOT_VARIANTS[kv].win;
+  return win == 64 ? slot_smem_w<64>(dimp) : win == 256 ? slot_smem_w<256>(dimp)
+                                                        : slot_smem_w<128>(dimp);
 }
 
 // Warps (node tiles) per thread block of k_epoch; EVOC_WARPS_PER_BLOCK
@@ -1588,7 +1613,8 @@ void launch_epoch(evoc_plan* pl, int32_t t, const float* e_cur, float* e_next,
     a.tile_order = pl->tile_order.get();
     a.slots = pl->slots.get();
     a.work_ctr = pl->work_ctr.get() + t;  // zeroed before the epoch loop
-    pick_slot_kernel(pl->dimp)<<<pl->slot_grid, 32 * wpb, wpb * slot_smem(pl->dimp), s>>>(a);
+    pick_slot_kernel(pl->dimp, pl->kvariant)<<<pl->slot_grid, 32 * wpb,
+                                                wpb * slot_smem(pl->dimp, pl->kvariant), s>>>(a);
   } else {
     pick_kernel(pl->dimp)<<<grid, 32 * wpb, wpb * tile_smem(pl->dimp), s>>>(a);
   }
@@ -1777,6 +1803,193 @@ void plan_info(const evoc_plan* p, int64_t* n_edges, int64_t* n_inc,
   if (wpb) *wpb = p->lanes;
   if (n_slots) *n_slots = p->use_slots ? p->n_slots : 0;
 }
+static void load_init(evoc_plan* pl, const float* d_init, cudaStream_t s);
+void plan_apply_tuned(evoc_plan* pl);
+
+// Epoch-kernel configuration of a plan: slots-kernel variant, warps per
+// block and a cap on persistent blocks per SM (0: as many as fit). The
+// persistent grid is recomputed and the captured epoch loop dropped (it is
+// captured again with the new launch shape on the next run). Results do not
+// depend on the configuration.
+void plan_configure(evoc_plan* pl, int kv, int wpb, int bps) {
+  if (kv < 0 || kv >= N_SLOT_VARIANTS)
+    throw Error(EVOC_ERR_INVALID_ARGUMENT, "epoch kernel variant out of range");
+  if (wpb != 1 && wpb != 2 && wpb != 4)
+    throw Error(EVOC_ERR_INVALID_ARGUMENT, "warps per block must be 1, 2 or 4");
+  if (bps < 0) throw Error(EVOC_ERR_INVALID_ARGUMENT, "blocks per SM must be >= 0");
+  pl->kvariant = kv;
+  pl->lanes = wpb;
+  pl->blocks_per_sm = bps;
+  if (pl->graph_exec) {
+    cudaGraphExecDestroy(pl->graph_exec);
+    pl->graph_exec = nullptr;
+  }
+  if (pl->graph) {
+    cudaGraphDestroy(pl->graph);
+    pl->graph = nullptr;
+  }
+  if (!pl->use_slots) return;
+  const void* fn = (const void*)pick_slot_kernel(pl->dimp, kv);
+  const size_t smem = (size_t)wpb * slot_smem(pl->dimp, kv);
+  if (smem > 48 * 1024)
+    EVOC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int nb = 0, dev = 0, sms = 0;
+  EVOC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, 32 * wpb, smem));
+  if (bps) nb = std::min(nb, bps);
+  EVOC_CUDA(cudaGetDevice(&dev));
+  EVOC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int64_t want = (int64_t)std::max(nb, 1) * sms;
+  const int64_t need = (pl->ntiles + wpb - 1) / wpb;
+  pl->slot_grid = (unsigned)std::max<int64_t>(1, std::min(want, need));
+}
+
+namespace {
+// Autotuner cache: plan shape -> configuration and its time per launch. In
+// memory for the process; with EVOC_TUNE_CACHE=<file> also read from and
+// appended to that file (one "key variant wpb bps ms" line per shape).
+struct TuneEntry {
+  int kv, wpb, bps;
+  float ms;
+};
+std::mutex g_tune_mu;
+std::map<std::string, TuneEntry> g_tune;
+bool g_tune_loaded = false;
+
+void tune_load_locked() {
+  if (g_tune_loaded) return;
+  g_tune_loaded = true;
+  const char* f = std::getenv("EVOC_TUNE_CACHE");
+  if (!f || !*f) return;
+  std::ifstream in(f);
+  std::string line;
+  while (std::getline(in, line)) {
+    std::istringstream ls(line);
+    std::string key;
+    TuneEntry e{};
+    if (ls >> key >> e.kv >> e.wpb >> e.bps >> e.ms && e.kv >= 0 && e.kv < N_SLOT_VARIANTS &&
+        (e.wpb == 1 || e.wpb == 2 || e.wpb == 4) && e.bps >= 0)
+      g_tune[key] = e;
+  }
+}
+
+// The shape a configuration is tuned for: padded row width, nodes and slots
+// per epoch (each on a half-octave grid), problem count (one or many), epoch
+// count and the device's SM count.
+std::string tune_key(const evoc_plan* pl, int sms) {
+  const int32_t ne = std::max(pl->params.n_epochs, 1);
+  const double spe = (double)pl->n_slots / ne;
+  auto bucket = [](double x) { return x < 1.0 ? 0 : (int)std::lround(2.0 * std::log2(x)); };
+  std::ostringstream k;
+  k << "d" << pl->dimp << "_n" << bucket((double)pl->n) << "_s" << bucket(spe) << "_p"
+    << (pl->n_problems > 1 ? "m" : "1") << "_e" << ne << "_sm" << sms;
+  return k.str();
+}
+}  // namespace
+
+// Configures a plan from the tuning cache when its shape was tuned before
+// (in this process or in the EVOC_TUNE_CACHE file); otherwise leaves it as it is.
+void plan_apply_tuned(evoc_plan* pl) {
+  if (!pl->use_slots || !pl->has_edges || pl->params.n_epochs <= 1) return;
+  int dev = 0, sms = 0;
+  EVOC_CUDA(cudaGetDevice(&dev));
+  EVOC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const std::string key = tune_key(pl, sms);
+  TuneEntry e{};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    tune_load_locked();
+    auto it = g_tune.find(key);
+    if (it == g_tune.end()) return;
+    e = it->second;
+  }
+  plan_configure(pl, e.kv, e.wpb, e.bps);
+}
+
+// Times every configuration on a sample of this plan's epochs (the real
+// slots kernel from a random state, CUDA events on the plan's stream) and
+// keeps the fastest; a shape tuned before in this process (or found in the
+// EVOC_TUNE_CACHE file) is configured without timing. Plans on the bit-plane
+// path have nothing to tune.
+void plan_autotune(evoc_plan* pl, int32_t* config, float* ms_out) {
+  cudaStream_t s = pl->ctx->stream;
+  const int32_t ne = pl->params.n_epochs;
+  float best_ms = 0.0f;
+  if (pl->use_slots && pl->has_edges && ne > 1) {
+    int dev = 0, sms = 0;
+    EVOC_CUDA(cudaGetDevice(&dev));
+    EVOC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const std::string key = tune_key(pl, sms);
+    TuneEntry hit{};
+    bool found = false;
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      tune_load_locked();
+      auto it = g_tune.find(key);
+      if (it != g_tune.end()) {
+        hit = it->second;
+        found = true;
+      }
+    }
+    if (found) {
+      plan_configure(pl, hit.kv, hit.wpb, hit.bps);
+      best_ms = hit.ms;
+    } else {
+      std::vector<int32_t> ts;  // sample epochs spread over the run (epoch 0 fires nothing)
+      for (int q = 1; q <= 5; ++q) {
+        const int32_t t = std::max(1, std::min(ne - 1, (int32_t)((int64_t)q * ne / 6)));
+        if (ts.empty() || ts.back() != t) ts.push_back(t);
+      }
+      load_init(pl, nullptr, s);
+      EVOC_CUDA(cudaMemsetAsync(pl->m.get(), 0, pl->m.bytes(), s));
+      EVOC_CUDA(cudaMemsetAsync(pl->v.get(), 0, pl->v.bytes(), s));
+      cudaEvent_t e0 = nullptr, e1 = nullptr;
+      EVOC_CUDA(cudaEventCreate(&e0));
+      EVOC_CUDA(cudaEventCreate(&e1));
+      TuneEntry best{0, pl->lanes, 0, 3.0e38f};
+      try {
+        const int wpbs[3] = {1, 2, 4};
+        for (int kv = 0; kv < N_SLOT_VARIANTS; ++kv)
+          for (int wpb : wpbs) {
+            plan_configure(pl, kv, wpb, 0);
+            float total = 0.0f;
+            for (int rep = 0; rep < 2; ++rep) {  // the first pass warms up
+              EVOC_CUDA(cudaMemsetAsync(pl->work_ctr.get(), 0, pl->work_ctr.bytes(), s));
+              EVOC_CUDA(cudaEventRecord(e0, s));
+              for (int32_t t : ts) launch_epoch(pl, t, pl->e0, pl->e1, nullptr, s);
+              EVOC_CUDA(cudaEventRecord(e1, s));
+              EVOC_CUDA(cudaEventSynchronize(e1));
+              EVOC_CUDA(cudaEventElapsedTime(&total, e0, e1));
+            }
+            const float per = total / (float)ts.size();
+            if (per < best.ms) best = TuneEntry{kv, wpb, 0, per};
+          }
+      } catch (...) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        throw;
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      plan_configure(pl, best.kv, best.wpb, best.bps);
+      best_ms = best.ms;
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      g_tune[key] = best;
+      if (const char* f = std::getenv("EVOC_TUNE_CACHE"))
+        if (*f) {
+          std::ofstream o(f, std::ios::app);
+          o << key << " " << best.kv << " " << best.wpb << " " << best.bps << " " << best.ms
+            << "\n";
+        }
+    }
+  }
+  if (config) {
+    config[0] = pl->kvariant;
+    config[1] = pl->lanes;
+    config[2] = pl->blocks_per_sm;
+  }
+  if (ms_out) *ms_out = best_ms;
+}
+
 int64_t plan_n(const evoc_plan* p) { return p->n; }
 int32_t plan_n_epochs(const evoc_plan* p) { return p->params.n_epochs; }
 bool plan_has_edges(const evoc_plan* p) { return p->has_edges; }
@@ -2073,17 +2286,10 @@ evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
   pl->m.alloc(n * pl->dimp, s);
   pl->v.alloc(n * pl->dimp, s);
   pl->lanes = default_wpb();
-  if (pl->use_slots) {  // persistent grid: as many warps as fit on the device
-    int nb = 0, dev = 0, sms = 0;
-    const size_t smem = (size_t)pl->lanes * slot_smem(pl->dimp);
-    EVOC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &nb, (const void*)pick_slot_kernel(pl->dimp), 32 * pl->lanes, smem));
-    EVOC_CUDA(cudaGetDevice(&dev));
-    EVOC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    const int64_t want = (int64_t)std::max(nb, 1) * sms;
-    const int64_t need = (pl->ntiles + pl->lanes - 1) / pl->lanes;
-    pl->slot_grid = (unsigned)std::max<int64_t>(1, std::min(want, need));
+  if (pl->use_slots) {
     pl->work_ctr.alloc(std::max<int32_t>(ne, 1), s);
+    plan_configure(pl.get(), 0, pl->lanes, 0);
+    plan_apply_tuned(pl.get());  // a configuration tuned for this shape, if any
   }
   trace.mark("moments");
   EVOC_CUDA(cudaStreamSynchronize(s));

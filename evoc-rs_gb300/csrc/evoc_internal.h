@@ -247,6 +247,8 @@ void plan_debug_run(evoc_plan* plan, const float* h_init, int32_t start_epoch,
                     int32_t end_epoch, float* h_out, float* h_grad);
 void plan_stats(const evoc_plan* plan, evoc_epoch_stats_t* stats);
 void plan_free(evoc_plan* plan);
+void plan_configure(evoc_plan* plan, int variant, int warps_per_block, int blocks_per_sm);
+void plan_autotune(evoc_plan* plan, int32_t* config, float* ms_per_launch);
 evoc_ctx* plan_ctx(const evoc_plan* plan);
 // Random 32-byte row gathers over an L2-resident buffer of `bytes`: GB/s
 // (measurement hook for the roofline's L2 bound).

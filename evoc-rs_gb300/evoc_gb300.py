@@ -52,6 +52,7 @@ EXPORTED = [
     "evoc_mlp_predict_device", "evoc_mlp_gradients", "evoc_mlp_fit_device",
     "evoc_to_bf16_device", "evoc_procrustes", "evoc_fuzzy_set_device_raw",
     "evoc_label_prop_partition", "evoc_selftest_wait_timeout", "evoc_ctx_smooth_knn_steps",
+    "evoc_plan_set_config", "evoc_plan_autotune",
 ]
 
 
@@ -153,6 +154,8 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "evoc_last_error": ([vp], C.c_char_p),
         "evoc_ctx_stream": ([vp], C.c_void_p),
         "evoc_ctx_smooth_knn_steps": ([vp, C.POINTER(C.c_int64)], C.c_int),
+        "evoc_plan_set_config": ([vp, C.c_int32, C.c_int32, C.c_int32], C.c_int),
+        "evoc_plan_autotune": ([vp, vp, C.POINTER(C.c_float)], C.c_int),
         "evoc_smooth_knn_dist": ([vp, vp, vp, i64, i32, u64, f32, i32, vp, vp], C.c_int),
         "evoc_fuzzy_set": ([vp, vp, vp, i64, i32, f32, C.c_int, pp], C.c_int),
         "evoc_fuzzy_set_device": ([vp, vp, vp, i64, i32, f32, C.c_int, vp, vp, pp], C.c_int),
@@ -292,6 +295,21 @@ class Plan:
                                                       C.byref(p), C.byref(l), C.byref(r)))
         return {"n_edges": e.value, "n_incidence": i.value, "neg_planes": p.value,
                 "warps_per_block": l.value, "n_slots": r.value}
+
+    def set_config(self, variant: int, warps_per_block: int, blocks_per_sm: int = 0) -> None:
+        """Epoch-kernel configuration (identical results for every choice)."""
+        self._ctx._check(self._ctx.lib.evoc_plan_set_config(self.handle, int(variant),
+                                                             int(warps_per_block),
+                                                             int(blocks_per_sm)))
+
+    def autotune(self) -> dict:
+        """Pick the fastest epoch-kernel configuration for this plan's shape
+        (cached per shape); returns it with its time per epoch launch."""
+        cfg = np.zeros(3, dtype=np.int32)
+        ms = C.c_float()
+        self._ctx._check(self._ctx.lib.evoc_plan_autotune(self.handle, _ptr(cfg), C.byref(ms)))
+        return {"variant": int(cfg[0]), "warps_per_block": int(cfg[1]),
+                "blocks_per_sm": int(cfg[2]), "ms_per_launch": round(float(ms.value), 4)}
 
     def stats(self) -> np.ndarray:
         arr = (EpochStatsC * max(self.n_epochs, 1))()

@@ -307,6 +307,26 @@ EVOC_API int evoc_plan_profile_epochs(evoc_plan_t* plan, const float* d_init,
  * roofline's L2 bound (no counterpart). */
 EVOC_API int evoc_gather_peak(evoc_ctx_t* ctx, int64_t bytes, double* gbs);
 
+/* Epoch-kernel configuration of a plan (no counterpart): variant 0..3 of the
+ * gradient-slots kernel as (slot window, slots per lane per group) = (128, 2),
+ * (64, 2), (256, 2), (128, 1); warps (32-node tiles) per thread block 1, 2
+ * or 4; persistent blocks per SM capped at blocks_per_sm (0: as many as
+ * fit). Every configuration gives identical results; only speed differs. */
+EVOC_API int evoc_plan_set_config(evoc_plan_t* plan, int32_t variant,
+                                  int32_t warps_per_block, int32_t blocks_per_sm);
+
+/* Autotuner (no counterpart): times every configuration above on a sample of
+ * the plan's epochs (CUDA events on the context's stream) and keeps the
+ * fastest. The choice is cached per plan shape (padded dim, node and slot
+ * counts on a half-octave grid, one or many problems, epochs, SM count) for
+ * the process, and in the file named by the EVOC_TUNE_CACHE environment
+ * variable when it is set; a cached shape is configured without timing.
+ * config (3 values, may be NULL) receives (variant, warps_per_block,
+ * blocks_per_sm); *ms_per_launch (may be NULL) the chosen configuration's
+ * time per epoch launch (0 when nothing was tuned: no slots, no edges, or
+ * fewer than 2 epochs). */
+EVOC_API int evoc_plan_autotune(evoc_plan_t* plan, int32_t* config, float* ms_per_launch);
+
 /* Layout facts of a plan (any pointer may be NULL): undirected edges,
  * per-node incidence entries (2 per edge), negative-count bit planes per
  * epoch, warps (32-node tiles) per thread block of the epoch kernel, and the
