@@ -72,6 +72,8 @@ WORKLOADS = {
                           train_n=2_000_000, train_instances=20, train_seed=100),
     # the label-propagation partition of the 2M graph (label_prop.rs:202-230)
     "label_prop_2m": dict(n=2_000_000, d=768, k=30, dim=8, seed=2),
+    # the whole label-propagation initialisation of the 2M graph with its points
+    "lp_init_2m": dict(n=2_000_000, d=768, k=30, dim=8, seed=2),
     # the warm-start network's forward pass alone (n = rows)
     "mlp_forward": dict(n=1_000_000, d=768, k=0, dim=8, seed=777, hidden=512),
 }
@@ -137,8 +139,9 @@ class ClockSampler:
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(sm)}
 
 
-def make_workload(name: str, n_override: int | None):
-    """Points and cosine kNN graph on the GPU (untimed input preparation)."""
+def make_workload(name: str, n_override: int | None, keep_points: bool = False):
+    """Points and cosine kNN graph on the GPU (untimed input preparation);
+    with keep_points the points (n x d f32, device) are returned as well."""
     import torch
     import workloads as W
     cfg = dict(WORKLOADS[name])
@@ -156,7 +159,8 @@ def make_workload(name: str, n_override: int | None):
         x, _ = W.blobs_sphere_torch(n, d, 20, 0.15, seed)
         groups = None
     idx, dist = W.knn_torch(x, k, groups)
-    del x
+    if not keep_points:
+        del x
     assert int(idx.min()) >= 0
     idx32 = idx.to(torch.int32).contiguous()  # uint32 bit pattern (n < 2^31)
     dist = dist.contiguous()
@@ -164,6 +168,8 @@ def make_workload(name: str, n_override: int | None):
     torch.cuda.synchronize()
     torch.cuda.empty_cache()  # release the kNN scratch before the library allocates
     cfg["prep_s"] = round(time.time() - t0, 1)
+    if keep_points:
+        return cfg, idx32, dist, x.contiguous()
     return cfg, idx32, dist
 
 
@@ -871,6 +877,62 @@ def run_label_prop(args) -> dict:
     }
 
 
+def run_lp_init(args) -> dict:
+    """label_propagation_init (label_prop.rs:537-564) on the 2M graph with the
+    768-d points (PCA base case), as evoc() runs it before the embedding: GPU
+    time from the device graph and points to the device initial embedding
+    (median of steps), the oracle's CPU restatement of the same call beside it
+    (one run), and the two results compared bit for bit."""
+    import torch
+    import evoc_gb300 as E
+    import oracle as O
+    torch.cuda.init()
+    cfg, idx32, dist, x = make_workload("hierarchical_2m", args.n, keep_points=True)
+    n, k, dim, d = cfg["n"], cfg["k"], cfg["dim"], cfg["d"]
+    ctx = E.Context(0)
+    g = ctx.fuzzy_set_device(idx32.data_ptr(), dist.data_ptr(), n, k, float(k), True)
+    out = torch.empty(n, dim, dtype=torch.float32, device="cuda")
+    for _ in range(args.warmup):
+        ctx.label_propagation_init_device(g, dim, x.data_ptr(), d, cfg["seed"], out.data_ptr())
+    ts = []
+    with ClockSampler() as clk:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            ctx.label_propagation_init_device(g, dim, x.data_ptr(), d, cfg["seed"], out.data_ptr())
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t)
+    ms = float(np.median(ts)) * 1e3
+    gpu = out.cpu().numpy()
+    ip, ix, w = g.export()
+    xh = x.cpu().numpy()
+    del x
+    torch.cuda.empty_cache()
+    t = time.perf_counter()
+    want = O.lp_init(ip, ix, w, dim, xh, cfg["seed"])
+    cpu_s = time.perf_counter() - t
+    same = bool(np.array_equal(gpu.view(np.uint32), want.view(np.uint32)))
+    g.free()
+    ctx.close()
+    return {
+        "metric": "label-propagation initialisation time at 2M pts (768-d data, dim 8)",
+        "value": ms, "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms, 3), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, no dataset)",
+        "config": {"workload": "lp_init_2m", "n": n, "d": d, "k": k, "dim": dim,
+                   "nnz": int(len(ix)),
+                   "time": "wall clock, synchronised, median of steps; device graph and points "
+                           "to the device initial embedding"},
+        "matches_oracle": same,
+        "cpu_baseline": {"value": round(cpu_s * 1e3, 1), "unit": "ms",
+                         "cores": O.max_threads(), "kind": "port",
+                         "sample": "the whole initialisation of the same graph and points "
+                                   "(the oracle, OpenMP where the reference uses rayon)"},
+        "gpu_launches": None,
+        "clocks": clk.summary(),
+    }
+
+
 def run_reference(args) -> dict:
     """The reference's CPU path (the C++ restatement; Rust is not available)
     on the same workload: each step is one epoch of the embedding loop
@@ -956,6 +1018,9 @@ def main() -> None:
         return
     if args.workload == "mlp_forward":
         print(json.dumps(run_mlp_forward(args)))
+        return
+    if args.workload == "lp_init_2m":
+        print(json.dumps(run_lp_init(args)))
         return
     if args.workload == "label_prop_2m":
         print(json.dumps(run_label_prop(args)))

@@ -25,11 +25,13 @@ LIB = PKG / "libevoc_gb300.so"
 ORACLE_SRCS = [ROOT / "oracle" / "evoc_oracle.cpp", ROOT / "oracle" / "evoc_labels_oracle.cpp"]
 ORACLE_LIB = ROOT / "oracle" / "liboracle.so"
 
-SOURCES = ["primitives.cu", "fuzzy_set.cu", "embed.cu", "capi.cu", "noalloc.cu", "measure.cu", "mlp.cu", "label_prop.cu"]
+SOURCES = ["primitives.cu", "fuzzy_set.cu", "embed.cu", "capi.cu", "noalloc.cu", "measure.cu", "mlp.cu",
+           "label_prop.cu", "lp_init.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
     "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+    "-Xcompiler", "-ffp-contract=off",  # host arithmetic as written (no FMA contraction)
     "-Xptxas", "-warn-spills",
 ]
 

@@ -666,6 +666,40 @@ int evoc_label_prop_partition(evoc_ctx_t* ctx, const evoc_graph_t* g, int64_t ap
   EVOC_API_END(ctx)
 }
 
+int evoc_label_propagation_init(evoc_ctx_t* ctx, const evoc_graph_t* g, int32_t dim,
+                                const float* data, int64_t d, uint64_t seed, float* out) {
+  EVOC_API_BEGIN
+  if (!ctx || !g || !out) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL argument");
+  use_device(ctx);
+  cudaStream_t s = ctx->stream;
+  const int64_t n = g->n;
+  evoc::DevBuf<float> dd, dout(n * (int64_t)std::max(dim, 1), s);
+  if (data) {
+    if (d <= 0) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "data dimension must be > 0");
+    dd.alloc(n * d, s);
+    EVOC_CUDA(cudaMemcpyAsync(dd.get(), data, dd.bytes(), cudaMemcpyHostToDevice, s));
+  }
+  evoc::label_propagation_init_device(ctx, g, dim, data ? dd.get() : nullptr, d, seed,
+                                      dout.get());
+  EVOC_CUDA(cudaMemcpyAsync(out, dout.get(), n * (int64_t)dim * sizeof(float),
+                            cudaMemcpyDeviceToHost, s));
+  EVOC_CUDA(cudaStreamSynchronize(s));
+  evoc::check_status(ctx, "label_propagation_init");
+  EVOC_API_END(ctx)
+}
+
+int evoc_label_propagation_init_device(evoc_ctx_t* ctx, const evoc_graph_t* g, int32_t dim,
+                                       const float* d_data, int64_t d, uint64_t seed,
+                                       float* d_out) {
+  EVOC_API_BEGIN
+  if (!ctx || !g || !d_out) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL argument");
+  use_device(ctx);
+  evoc::label_propagation_init_device(ctx, g, dim, d_data, d, seed, d_out);
+  EVOC_CUDA(cudaStreamSynchronize(ctx->stream));
+  evoc::check_status(ctx, "label_propagation_init");
+  EVOC_API_END(ctx)
+}
+
 // ---- learned warm start ----------------------------------------------------
 
 void evoc_mlp_train_params_default(evoc_mlp_train_params_t* p) {

@@ -98,6 +98,9 @@ struct evoc_plan {
   unsigned slot_grid = 0;                     // persistent grid of the slots kernel
   int32_t kvariant = 0;                       // slots-kernel variant (SLOT_VARIANTS)
   int32_t blocks_per_sm = 0;                  // persistent blocks per SM (0: as many as fit)
+  bool all_epochs = false;                    // one cooperative launch for all epochs
+  evoc::DevBuf<float4> ep_params;             // per epoch: gamma, lr * ad_scale, eps'
+  evoc::DevBuf<unsigned> grid_bar;            // the all-epochs launch's barrier words
   bool stats_done = false;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
@@ -471,12 +474,15 @@ struct EpochArgs {
   float noise, gamma, lr_ad, epsc, one_m_b1, one_m_b2;
 };
 
-template <int DIMP>
+// COH: the row may have been written earlier in the same launch (the
+// persistent all-epochs kernel), so it is read through L2 (ld.global.cg)
+// rather than the non-coherent read-only path.
+template <int DIMP, bool COH = false>
 __device__ __forceinline__ void load_row(const float* __restrict__ p, float (&r)[DIMP]) {
   const float4* p4 = reinterpret_cast<const float4*>(p);
 #pragma unroll
   for (int i = 0; i < DIMP / 4; ++i) {
-    const float4 x = __ldg(p4 + i);
+    const float4 x = COH ? __ldcg(p4 + i) : __ldg(p4 + i);
     r[4 * i + 0] = x.x;
     r[4 * i + 1] = x.y;
     r[4 * i + 2] = x.z;
@@ -1006,19 +1012,21 @@ __device__ __forceinline__ int nth_set_bit(uint32_t m, int r) {
 // the order of the reference's serial sum: entries in incidence order, each
 // attraction followed by its negatives.
 constexpr int FILL_EPB = 8;
-constexpr int FILL_SEG = 4096;
-constexpr int FILL_Q = 128;  // queued draws per warp and window
+constexpr int FILL_SEG = 2048;
+constexpr int FILL_Q = 128;      // queued draws per warp and window
+constexpr int FILL_STAGE = 384;  // staged slots per warp and window
 struct FillJob {
-  int64_t q;        // slot index
+  int64_t q;        // slot index (global, or within the staged window)
   uint32_t eidx;    // edge id
   uint32_t jn;      // draw index j | tile-local node << 8
 };
 struct PlaneFillSmem {
+  uint2 stage[FILL_EPB][FILL_STAGE]; // per-warp slots of the current window
+  FillJob job[FILL_EPB][FILL_Q];     // per-warp draw queues
   uint32_t part[FILL_SEG];           // partner of each staged entry
-  uint8_t node[FILL_SEG];            // tile-local node of each staged entry
   int64_t pb[TILE + 1];              // incidence offsets of the tile's nodes
   int64_t eb[TILE];                  // edge-id bases of the tile's nodes
-  FillJob job[FILL_EPB][FILL_Q];     // per-warp draw queues
+  uint8_t node[FILL_SEG];            // tile-local node of each staged entry
 };
 
 __device__ __forceinline__ uint2 negative_slot(uint64_t seed, uint32_t j, int32_t t, uint32_t eidx,
@@ -1043,7 +1051,8 @@ __global__ void __launch_bounds__(32 * FILL_EPB) k_plane_fill(
     const uint32_t* __restrict__ nplane1, const int64_t* __restrict__ tile_off,
     const uint32_t* __restrict__ prob_of_node, const ProbInfo* __restrict__ prob,
     uint64_t seed, uint2* __restrict__ slots) {
-  __shared__ PlaneFillSmem sm;
+  extern __shared__ __align__(16) unsigned char fill_raw[];
+  PlaneFillSmem& sm = *reinterpret_cast<PlaneFillSmem*>(fill_raw);
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int ngroups = (ne + FILL_EPB - 1) / FILL_EPB;
@@ -1060,7 +1069,6 @@ __global__ void __launch_bounds__(32 * FILL_EPB) k_plane_fill(
   int64_t cur = active ? tile_off[(int64_t)t * ntiles + tile] : 0;
   const int64_t po = (int64_t)t * W;
   FillJob* job = sm.job[wid];
-  const uint32_t lt = (1u << lane) - 1u;
   for (int64_t sb = P0; sb < P1; sb += FILL_SEG) {
     const int64_t se = min(sb + (int64_t)FILL_SEG, P1);
     __syncthreads();  // the previous segment's readers are done
@@ -1095,16 +1103,20 @@ __global__ void __launch_bounds__(32 * FILL_EPB) k_plane_fill(
       const int stot = __shfl_sync(FULL, sincl, 31), jtot = __shfl_sync(FULL, jincl, 31);
       if (stot == 0) continue;
       const bool queued = jtot <= FILL_Q;
-      int64_t q = cur + sincl - (__popc(f) + nneg);
+      // a window that fits is assembled in shared memory and leaves with
+      // coalesced stores; a larger one is written in place
+      const bool staged = stot <= FILL_STAGE;
+      uint2* dst = staged ? sm.stage[wid] : slots + cur;
+      int64_t q = sincl - (__popc(f) + nneg);  // within the window
       int jq = jincl - nneg;
-      __syncwarp();  // the previous window's drain has read its jobs
+      __syncwarp();  // the previous window's drain and flush are done
       while (f) {
         const int b = __ffs(f) - 1;
         f &= f - 1;
         const int64_t p = (w << 5) + b;
         const int li = (int)(p - sb);
         const uint32_t node = sm.node[li];
-        slots[q++] = make_uint2(sm.part[li], node);
+        dst[q++] = make_uint2(sm.part[li], node);
         const uint32_t nn = ((g0 >> b) & 1u) | (((g1 >> b) & 1u) << 1);
         if (nn) {
           const uint32_t eidx = (uint32_t)(p + sm.eb[node]);
@@ -1112,20 +1124,24 @@ __global__ void __launch_bounds__(32 * FILL_EPB) k_plane_fill(
             if (queued)
               job[jq++] = FillJob{q, eidx, j | (node << 8)};
             else
-              slots[q] = negative_slot(seed, j, t, eidx, node, v0, (uint32_t)n, prob_of_node, prob);
+              dst[q] = negative_slot(seed, j, t, eidx, node, v0, (uint32_t)n, prob_of_node, prob);
           }
         }
       }
-      cur += stot;
       if (queued && jtot > 0) {
         __syncwarp();  // the jobs are in shared memory
         for (int i = lane; i < jtot; i += 32) {
           const FillJob jb = job[i];
           const uint32_t node = jb.jn >> 8;
-          slots[jb.q] = negative_slot(seed, jb.jn & 0xffu, t, jb.eidx, node, v0, (uint32_t)n,
-                                      prob_of_node, prob);
+          dst[jb.q] = negative_slot(seed, jb.jn & 0xffu, t, jb.eidx, node, v0, (uint32_t)n,
+                                    prob_of_node, prob);
         }
       }
+      if (staged) {
+        __syncwarp();  // the window's slots are in shared memory
+        for (int i = lane; i < stot; i += 32) slots[cur + i] = sm.stage[wid][i];
+      }
+      cur += stot;
     }
   }
 }
@@ -1340,7 +1356,7 @@ __device__ __forceinline__ void slot_contrib(float (&c)[DIMP], bool neg,
 }
 
 // Phase 1 for U slots per lane: window slots ib + 32 u + lane, u < U.
-template <int DIMP, int WIN, int U>
+template <int DIMP, int WIN, int U, bool COH>
 __device__ __forceinline__ void slot_group(const EpochArgs& a, SlotSmem<DIMP, WIN>& sm,
                                            const uint2* __restrict__ wslots, int ib, int wn,
                                            int lane, int& carry, uint32_t& act_mask,
@@ -1354,7 +1370,7 @@ __device__ __forceinline__ void slot_group(const EpochArgs& a, SlotSmem<DIMP, WI
     sl[u] = __ldcs(wslots + (i < wn ? i : wn - 1));
   }
 #pragma unroll
-  for (int u = 0; u < U; ++u) load_row<DIMP>(a.e_cur + (size_t)sl[u].x * DIMP, row[u]);
+  for (int u = 0; u < U; ++u) load_row<DIMP, COH>(a.e_cur + (size_t)sl[u].x * DIMP, row[u]);
 #pragma unroll
   for (int u = 0; u < U; ++u) {  // run starts (a repeated last slot starts nothing)
     const int i = ib + 32 * u + lane;
@@ -1382,7 +1398,7 @@ __device__ __forceinline__ void slot_group(const EpochArgs& a, SlotSmem<DIMP, WI
   }
 }
 
-template <int DIMP, int WIN, int SU>
+template <int DIMP, int WIN, int SU, bool COH>
 __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP, WIN>& sm, int64_t tile,
                                           int lane) {
   const unsigned FULL = 0xffffffffu;
@@ -1393,7 +1409,7 @@ __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP, WIN
   {
     const float4* src = reinterpret_cast<const float4*>(a.e_cur + (size_t)v0 * DIMP);
     float4* dst = reinterpret_cast<float4*>(&sm.rows[0][0]);
-    for (int i = lane; i < nt * (DIMP / 4); i += 32) dst[i] = __ldg(src + i);
+    for (int i = lane; i < nt * (DIMP / 4); i += 32) dst[i] = COH ? __ldcg(src + i) : __ldg(src + i);
     float4* sz = reinterpret_cast<float4*>(&sm.S[0][0]);
     for (int i = lane; i < TILE * (DIMP / 4); i += 32) sz[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
@@ -1408,9 +1424,11 @@ __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP, WIN
     int carry = -1;  // node of the previous slot of the window
     int ib = 0;
     for (; ib + 32 * SU <= wn; ib += 32 * SU)
-      slot_group<DIMP, WIN, SU>(a, sm, wslots, ib, wn, lane, carry, act_mask, two_noise, gamma4);
+      slot_group<DIMP, WIN, SU, COH>(a, sm, wslots, ib, wn, lane, carry, act_mask, two_noise,
+                                     gamma4);
     for (; ib < wn; ib += 32)
-      slot_group<DIMP, WIN, 1>(a, sm, wslots, ib, wn, lane, carry, act_mask, two_noise, gamma4);
+      slot_group<DIMP, WIN, 1, COH>(a, sm, wslots, ib, wn, lane, carry, act_mask, two_noise,
+                                    gamma4);
     __syncwarp();
     // run of node l: [start[l], first start of a later node or wn)
     const int st = sm.start[lane];
@@ -1466,7 +1484,8 @@ __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP, WIN
       float mm[DIMP], vv[DIMP];
 #pragma unroll
       for (int i = 0; i < DIMP / 4; ++i) {
-        const float4 x = __ldcs(m4 + i), y = __ldcs(v4 + i);
+        const float4 x = COH ? __ldcg(m4 + i) : __ldcs(m4 + i);
+        const float4 y = COH ? __ldcg(v4 + i) : __ldcs(v4 + i);
         mm[4 * i] = x.x; mm[4 * i + 1] = x.y; mm[4 * i + 2] = x.z; mm[4 * i + 3] = x.w;
         vv[4 * i] = y.x; vv[4 * i + 1] = y.y; vv[4 * i + 2] = y.z; vv[4 * i + 3] = y.w;
       }
@@ -1514,7 +1533,99 @@ __global__ void __launch_bounds__(128, DIMP <= 8 ? 7 : 4) k_epoch_slot(EpochArgs
     if (lane == 0) w = atomicAdd(a.work_ctr, 1ull);
     w = __shfl_sync(0xffffffffu, w, 0);
     if ((int64_t)w >= ntiles) break;
-    slot_tile<DIMP, WIN, SU>(a, sm, (int64_t)a.tile_order[w], lane);
+    slot_tile<DIMP, WIN, SU, false>(a, sm, (int64_t)a.tile_order[w], lane);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// All epochs in one persistent launch (cooperative: every block resident).
+// Each epoch runs exactly as k_epoch_slot (tiles from the epoch's work
+// counter, heaviest first), reading rows and moments through L2 because they
+// were written earlier in the same launch; a grid-wide barrier separates the
+// epochs. The barrier waits at most GRID_WAIT_NS; on expiry it records
+// ST_WAIT_TIMEOUT, raises an abort word that every block checks, and the
+// launch returns.
+// ---------------------------------------------------------------------------
+struct EpochAllArgs {
+  const float4* ep;               // per epoch: gamma, lr * ad_scale, eps', 0
+  const int64_t* tile_off;        // all epochs: [t * ntiles + tile]
+  unsigned long long* work_ctr;   // per epoch, zeroed before the launch
+  float* e0;                      // embedding at epoch t0 (ping-pong with e1)
+  float* e1;
+  unsigned* bar;                  // arrivals, generation, abort (zeroed)
+  int32_t* status;
+  int32_t t0, t1;                 // epochs [t0, t1)
+  unsigned nblocks;
+};
+constexpr unsigned long long GRID_WAIT_NS = 2000000000ull;
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ bool grid_barrier(unsigned* bar, unsigned nblocks, int32_t* status) {
+  __shared__ int ok_s;
+  __syncthreads();  // the block's epoch is done
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    volatile unsigned* vbar = bar;
+    const unsigned gen = vbar[1];
+    __threadfence();  // this block's writes before its arrival
+    if (atomicAdd(bar, 1u) == nblocks - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      const uint64_t start = globaltimer_ns();
+      while (vbar[1] == gen) {
+        if (vbar[2]) {
+          ok = 0;
+          break;
+        }
+        if (globaltimer_ns() - start > GRID_WAIT_NS) {
+          atomicOr(status, (int32_t)ST_WAIT_TIMEOUT);
+          atomicExch(bar + 2, 1u);
+          ok = 0;
+          break;
+        }
+      }
+    }
+    __threadfence();
+    ok_s = ok && !vbar[2];
+  }
+  __syncthreads();
+  return ok_s != 0;
+}
+
+template <int DIMP, int WIN, int SU>
+__global__ void __launch_bounds__(128, DIMP <= 8 ? 7 : 4)
+    k_epoch_slot_all(EpochArgs base, EpochAllArgs x) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31;
+  SlotSmem<DIMP, WIN>& sm = reinterpret_cast<SlotSmem<DIMP, WIN>*>(smem_raw)[threadIdx.x >> 5];
+  const int64_t ntiles = ((int64_t)base.n_total + TILE - 1) / TILE;
+  for (int32_t t = x.t0; t < x.t1; ++t) {
+    EpochArgs a = base;
+    const int k = t - x.t0;
+    a.e_cur = (k & 1) ? x.e1 : x.e0;
+    a.e_next = (k & 1) ? x.e0 : x.e1;
+    a.tile_off = x.tile_off + (size_t)t * ntiles;
+    a.work_ctr = x.work_ctr + t;
+    const float4 ep = x.ep[t];
+    a.gamma = ep.x;
+    a.lr_ad = ep.y;
+    a.epsc = ep.z;
+    a.epoch = (uint32_t)t;
+    for (;;) {
+      unsigned long long w = 0;
+      if (lane == 0) w = atomicAdd(a.work_ctr, 1ull);
+      w = __shfl_sync(0xffffffffu, w, 0);
+      if ((int64_t)w >= ntiles) break;
+      slot_tile<DIMP, WIN, SU, true>(a, sm, (int64_t)a.tile_order[w], lane);
+    }
+    if (t + 1 < x.t1 && !grid_barrier(x.bar, x.nblocks, x.status)) return;
   }
 }
 
@@ -1551,6 +1662,21 @@ EpochKernel pick_slot_kernel(int dimp, int kv) {
     case 2: return pick_slot_wu<256, 2>(dimp);
     case 3: return pick_slot_wu<128, 1>(dimp);
     default: return pick_slot_wu<128, 2>(dimp);
+  }
+}
+using EpochAllKernel = void (*)(EpochArgs, EpochAllArgs);
+template <int WIN, int SU>
+EpochAllKernel pick_all_wu(int dimp) {
+  if (dimp == 4) return k_epoch_slot_all<4, WIN, SU>;
+  if (dimp == 8) return k_epoch_slot_all<8, WIN, SU>;
+  return k_epoch_slot_all<16, WIN, SU>;
+}
+EpochAllKernel pick_all_kernel(int dimp, int kv) {
+  switch (kv) {
+    case 1: return pick_all_wu<64, 2>(dimp);
+    case 2: return pick_all_wu<256, 2>(dimp);
+    case 3: return pick_all_wu<128, 1>(dimp);
+    default: return pick_all_wu<128, 2>(dimp);
   }
 }
 template <int WIN>
@@ -1619,6 +1745,43 @@ void launch_epoch(evoc_plan* pl, int32_t t, const float* e_cur, float* e_next,
     pick_kernel(pl->dimp)<<<grid, 32 * wpb, wpb * tile_smem(pl->dimp), s>>>(a);
   }
   EVOC_CHECK_LAUNCH();
+}
+
+// Epochs [t0, t1) in one cooperative launch (slots path): from e0, ending in
+// e0 or e1 by the parity of t1 - t0. Work counters and barrier words are
+// zeroed first.
+void launch_all_epochs(evoc_plan* pl, int32_t t0, int32_t t1, cudaStream_t s) {
+  EpochArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.m = pl->m.get();
+  a.v = pl->v.get();
+  a.prob_of_node = pl->n_problems > 1 ? pl->prob_of_node.get() : nullptr;
+  a.prob = pl->n_problems > 1 ? pl->prob.get() : nullptr;
+  a.n_total = (uint32_t)pl->n;
+  a.seed = pl->seeds.empty() ? 0 : pl->seeds[0];
+  a.noise = pl->params.noise_level;
+  a.one_m_b1 = pl->one_m_b1;
+  a.one_m_b2 = pl->one_m_b2;
+  a.tile_order = pl->tile_order.get();
+  a.slots = pl->slots.get();
+  EpochAllArgs x;
+  x.ep = pl->ep_params.get();
+  x.tile_off = pl->tile_off.get();
+  x.work_ctr = pl->work_ctr.get();
+  x.e0 = pl->e0;
+  x.e1 = pl->e1;
+  x.bar = pl->grid_bar.get();
+  x.status = pl->ctx->status.get();
+  x.t0 = t0;
+  x.t1 = t1;
+  x.nblocks = pl->slot_grid;
+  EVOC_CUDA(cudaMemsetAsync(pl->work_ctr.get(), 0, pl->work_ctr.bytes(), s));
+  EVOC_CUDA(cudaMemsetAsync(pl->grid_bar.get(), 0, pl->grid_bar.bytes(), s));
+  void* args[] = {&a, &x};
+  const int wpb = pl->lanes;
+  EVOC_CUDA(cudaLaunchCooperativeKernel((const void*)pick_all_kernel(pl->dimp, pl->kvariant),
+                                        dim3(pl->slot_grid), dim3(32 * wpb), args,
+                                        wpb * slot_smem(pl->dimp, pl->kvariant), s));
 }
 
 unsigned blocks_for(int64_t threads, int bs = 256) {
@@ -1768,7 +1931,10 @@ static bool build_slots(evoc_plan* pl, const float* inc_ps, const uint8_t* inc_u
   const uint64_t seed0 = pl->seeds.empty() ? 0 : pl->seeds[0];
   if (use_planes) {
     const int64_t ngroups = (ne + FILL_EPB - 1) / FILL_EPB;
-    k_plane_fill<<<(unsigned)(ngroups * pl->ntiles), 32 * FILL_EPB, 0, s>>>(
+    EVOC_CUDA(cudaFuncSetAttribute((const void*)k_plane_fill,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)sizeof(PlaneFillSmem)));
+    k_plane_fill<<<(unsigned)(ngroups * pl->ntiles), 32 * FILL_EPB, sizeof(PlaneFillSmem), s>>>(
         pl->inc_ptr.get(), pl->inc_other.get(), pl->eidx_base.get(), n, pl->ntiles, planes_w,
         ne, fpl.get(), npl0.get(), npl1.get(), off.get(), pon, pinfo, seed0, pl->slots.get());
   } else {
@@ -1811,15 +1977,18 @@ void plan_apply_tuned(evoc_plan* pl);
 // persistent grid is recomputed and the captured epoch loop dropped (it is
 // captured again with the new launch shape on the next run). Results do not
 // depend on the configuration.
-void plan_configure(evoc_plan* pl, int kv, int wpb, int bps) {
-  if (kv < 0 || kv >= N_SLOT_VARIANTS)
+void plan_configure(evoc_plan* pl, int variant, int wpb, int bps) {
+  if (variant < 0 || variant >= 2 * N_SLOT_VARIANTS)
     throw Error(EVOC_ERR_INVALID_ARGUMENT, "epoch kernel variant out of range");
+  const int kv = variant % N_SLOT_VARIANTS;
+  const bool all = variant >= N_SLOT_VARIANTS;
   if (wpb != 1 && wpb != 2 && wpb != 4)
     throw Error(EVOC_ERR_INVALID_ARGUMENT, "warps per block must be 1, 2 or 4");
   if (bps < 0) throw Error(EVOC_ERR_INVALID_ARGUMENT, "blocks per SM must be >= 0");
   pl->kvariant = kv;
   pl->lanes = wpb;
   pl->blocks_per_sm = bps;
+  pl->all_epochs = all && pl->use_slots;
   if (pl->graph_exec) {
     cudaGraphExecDestroy(pl->graph_exec);
     pl->graph_exec = nullptr;
@@ -1829,7 +1998,8 @@ void plan_configure(evoc_plan* pl, int kv, int wpb, int bps) {
     pl->graph = nullptr;
   }
   if (!pl->use_slots) return;
-  const void* fn = (const void*)pick_slot_kernel(pl->dimp, kv);
+  const void* fn = all ? (const void*)pick_all_kernel(pl->dimp, kv)
+                       : (const void*)pick_slot_kernel(pl->dimp, kv);
   const size_t smem = (size_t)wpb * slot_smem(pl->dimp, kv);
   if (smem > 48 * 1024)
     EVOC_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1866,7 +2036,7 @@ void tune_load_locked() {
     std::istringstream ls(line);
     std::string key;
     TuneEntry e{};
-    if (ls >> key >> e.kv >> e.wpb >> e.bps >> e.ms && e.kv >= 0 && e.kv < N_SLOT_VARIANTS &&
+    if (ls >> key >> e.kv >> e.wpb >> e.bps >> e.ms && e.kv >= 0 && e.kv < 2 * N_SLOT_VARIANTS &&
         (e.wpb == 1 || e.wpb == 2 || e.wpb == 4) && e.bps >= 0)
       g_tune[key] = e;
   }
@@ -1968,6 +2138,35 @@ void plan_autotune(evoc_plan* pl, int32_t* config, float* ms_out) {
         cudaEventDestroy(e1);
         throw;
       }
+      // the chosen variant launched per epoch (the captured loop) or as one
+      // cooperative launch for all epochs: the faster over a whole run
+      {
+        float per_epoch_ms = 0.0f, all_ms = 0.0f;
+        for (int mode = 0; mode < 2; ++mode) {
+          plan_configure(pl, best.kv + (mode ? N_SLOT_VARIANTS : 0), best.wpb, best.bps);
+          float el = 0.0f;
+          for (int rep = 0; rep < 2; ++rep) {  // the first run captures / warms up
+            load_init(pl, nullptr, s);
+            EVOC_CUDA(cudaMemsetAsync(pl->m.get(), 0, pl->m.bytes(), s));
+            EVOC_CUDA(cudaMemsetAsync(pl->v.get(), 0, pl->v.bytes(), s));
+            EVOC_CUDA(cudaEventRecord(e0, s));
+            if (mode) {
+              launch_all_epochs(pl, 0, ne, s);
+            } else {
+              EVOC_CUDA(cudaMemsetAsync(pl->work_ctr.get(), 0, pl->work_ctr.bytes(), s));
+              for (int32_t t = 0; t < ne; ++t)
+                launch_epoch(pl, t, (t & 1) ? pl->e1 : pl->e0, (t & 1) ? pl->e0 : pl->e1,
+                             nullptr, s);
+            }
+            EVOC_CUDA(cudaEventRecord(e1, s));
+            EVOC_CUDA(cudaEventSynchronize(e1));
+            EVOC_CUDA(cudaEventElapsedTime(&el, e0, e1));
+          }
+          (mode ? all_ms : per_epoch_ms) = el;
+        }
+        check_status(pl->ctx, "autotune (all-epochs launch)");
+        if (all_ms < per_epoch_ms) best.kv += N_SLOT_VARIANTS;
+      }
       cudaEventDestroy(e0);
       cudaEventDestroy(e1);
       plan_configure(pl, best.kv, best.wpb, best.bps);
@@ -1983,7 +2182,7 @@ void plan_autotune(evoc_plan* pl, int32_t* config, float* ms_out) {
     }
   }
   if (config) {
-    config[0] = pl->kvariant;
+    config[0] = pl->kvariant + (pl->all_epochs ? N_SLOT_VARIANTS : 0);
     config[1] = pl->lanes;
     config[2] = pl->blocks_per_sm;
   }
@@ -2288,6 +2487,13 @@ evoc_plan* plan_create(evoc_ctx* ctx, const std::vector<ProblemDesc>& probs,
   pl->lanes = default_wpb();
   if (pl->use_slots) {
     pl->work_ctr.alloc(std::max<int32_t>(ne, 1), s);
+    std::vector<float4> ep(std::max<int32_t>(ne, 1), make_float4(0.f, 0.f, 0.f, 0.f));
+    for (int32_t t = 0; t < ne; ++t) ep[t] = make_float4(pl->gamma[t], pl->lr_ad[t], pl->epsc[t], 0.f);
+    pl->ep_params.alloc(ep.size(), s);
+    EVOC_CUDA(cudaMemcpyAsync(pl->ep_params.get(), ep.data(), ep.size() * sizeof(float4),
+                              cudaMemcpyHostToDevice, s));
+    pl->grid_bar.alloc(4, s);
+    EVOC_CUDA(cudaStreamSynchronize(s));  // ep goes out of scope
     plan_configure(pl.get(), 0, pl->lanes, 0);
     plan_apply_tuned(pl.get());  // a configuration tuned for this shape, if any
   }
@@ -2346,6 +2552,10 @@ void plan_run_device(evoc_plan* pl, const float* d_init, float* d_out) {
   if (pl->has_edges && ne > 0) {
     EVOC_CUDA(cudaMemsetAsync(pl->m.get(), 0, pl->m.bytes(), s));
     EVOC_CUDA(cudaMemsetAsync(pl->v.get(), 0, pl->v.bytes(), s));
+    if (pl->all_epochs) {  // one cooperative launch for all epochs
+      launch_all_epochs(pl, 0, ne, s);
+      EVOC_CHECK_LAUNCH();
+    } else {
     if (pl->use_slots)  // tile counters of the slots kernel, one per epoch
       EVOC_CUDA(cudaMemsetAsync(pl->work_ctr.get(), 0, pl->work_ctr.bytes(), s));
     if (!pl->graph_exec) {
@@ -2366,6 +2576,7 @@ void plan_run_device(evoc_plan* pl, const float* d_init, float* d_out) {
       EVOC_CUDA(cudaGraphInstantiate(&pl->graph_exec, pl->graph, 0));
     }
     EVOC_CUDA(cudaGraphLaunch(pl->graph_exec, s));
+    }
   }
   const float* fin = (pl->has_edges && (ne & 1)) ? pl->e1 : pl->e0;
   k_unpad<<<blocks_for(n * pl->dim), 256, 0, s>>>(fin, d_out, n, pl->dim, pl->dimp);

@@ -208,6 +208,13 @@ struct ProblemDesc {
 int64_t label_prop_partition(evoc_ctx* ctx, const evoc_graph* g, int64_t approx_n_parts,
                              int32_t n_iter, uint64_t seed, uint32_t* d_partition);
 
+// ---- lp_init.cu ------------------------------------------------------------
+// label_propagation_init (label_prop.rs:537-564) of g: the n x dim initial
+// embedding into d_out (device); d_data (device n x d) feeds the PCA base
+// case, or is null (random base case).
+void label_propagation_init_device(evoc_ctx* ctx, const evoc_graph* g, int32_t dim,
+                                   const float* d_data, int64_t d, uint64_t seed, float* d_out);
+
 // ---- mlp.cu ----------------------------------------------------------------
 }  // namespace evoc
 

@@ -52,7 +52,8 @@ EXPORTED = [
     "evoc_mlp_predict_device", "evoc_mlp_gradients", "evoc_mlp_fit_device",
     "evoc_to_bf16_device", "evoc_procrustes", "evoc_fuzzy_set_device_raw",
     "evoc_label_prop_partition", "evoc_selftest_wait_timeout", "evoc_ctx_smooth_knn_steps",
-    "evoc_plan_set_config", "evoc_plan_autotune",
+    "evoc_plan_set_config", "evoc_plan_autotune", "evoc_label_propagation_init",
+    "evoc_label_propagation_init_device",
 ]
 
 
@@ -156,6 +157,10 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
         "evoc_ctx_smooth_knn_steps": ([vp, C.POINTER(C.c_int64)], C.c_int),
         "evoc_plan_set_config": ([vp, C.c_int32, C.c_int32, C.c_int32], C.c_int),
         "evoc_plan_autotune": ([vp, vp, C.POINTER(C.c_float)], C.c_int),
+        "evoc_label_propagation_init": ([vp, vp, C.c_int32, vp, C.c_int64, C.c_uint64, vp],
+                                        C.c_int),
+        "evoc_label_propagation_init_device": ([vp, vp, C.c_int32, vp, C.c_int64, C.c_uint64,
+                                               vp], C.c_int),
         "evoc_smooth_knn_dist": ([vp, vp, vp, i64, i32, u64, f32, i32, vp, vp], C.c_int),
         "evoc_fuzzy_set": ([vp, vp, vp, i64, i32, f32, C.c_int, pp], C.c_int),
         "evoc_fuzzy_set_device": ([vp, vp, vp, i64, i32, f32, C.c_int, vp, vp, pp], C.c_int),
@@ -555,6 +560,24 @@ class Context:
                                                        int(approx_n_parts), int(n_iter),
                                                        int(seed), _ptr(part), C.byref(k)))
         return part, k.value
+
+    def label_propagation_init(self, graph: Graph, dim: int, data=None,
+                               seed: int = 42) -> np.ndarray:
+        """label_propagation_init (label_prop.rs:537-564): the n x dim initial
+        embedding of evoc(); data (n x d f32) feeds the PCA base case."""
+        n = graph.n
+        out = np.zeros((n, dim), dtype=np.float32)
+        x = None if data is None else _f32(data)
+        d = 0 if x is None else x.shape[1]
+        self._check(self.lib.evoc_label_propagation_init(self.handle, graph.handle, int(dim),
+                                                         _ptr(x), int(d), int(seed), _ptr(out)))
+        return out
+
+    def label_propagation_init_device(self, graph: Graph, dim: int, d_data: int | None,
+                                      d: int, seed: int, d_out: int) -> None:
+        self._check(self.lib.evoc_label_propagation_init_device(
+            self.handle, graph.handle, int(dim), C.c_void_p(d_data) if d_data else None, int(d),
+            int(seed), C.c_void_p(d_out)))
 
     def graph_from_csr(self, indptr, indices, weights) -> Graph:
         ip = np.ascontiguousarray(indptr, dtype=np.int64)

@@ -309,9 +309,13 @@ EVOC_API int evoc_gather_peak(evoc_ctx_t* ctx, int64_t bytes, double* gbs);
 
 /* Epoch-kernel configuration of a plan (no counterpart): variant 0..3 of the
  * gradient-slots kernel as (slot window, slots per lane per group) = (128, 2),
- * (64, 2), (256, 2), (128, 1); warps (32-node tiles) per thread block 1, 2
- * or 4; persistent blocks per SM capped at blocks_per_sm (0: as many as
- * fit). Every configuration gives identical results; only speed differs. */
+ * (64, 2), (256, 2), (128, 1), launched once per epoch (the epoch loop is
+ * captured in a CUDA graph); variants 4..7 the same kernels with all epochs
+ * in one persistent cooperative launch, a grid-wide barrier between epochs
+ * (a barrier wait that exceeds 2 s ends the launch with EVOC_ERR_INTERNAL);
+ * warps (32-node tiles) per thread block 1, 2 or 4; persistent blocks per SM
+ * capped at blocks_per_sm (0: as many as fit). Every configuration gives
+ * identical results; only speed differs. */
 EVOC_API int evoc_plan_set_config(evoc_plan_t* plan, int32_t variant,
                                   int32_t warps_per_block, int32_t blocks_per_sm);
 
@@ -321,8 +325,9 @@ EVOC_API int evoc_plan_set_config(evoc_plan_t* plan, int32_t variant,
  * counts on a half-octave grid, one or many problems, epochs, SM count) for
  * the process, and in the file named by the EVOC_TUNE_CACHE environment
  * variable when it is set; a cached shape is configured without timing.
- * config (3 values, may be NULL) receives (variant, warps_per_block,
- * blocks_per_sm); *ms_per_launch (may be NULL) the chosen configuration's
+ * The variant found fastest on sampled epochs is also timed over a whole run
+ * in both launch forms. config (3 values, may be NULL) receives (variant,
+ * warps_per_block, blocks_per_sm); *ms_per_launch (may be NULL) the chosen configuration's
  * time per epoch launch (0 when nothing was tuned: no slots, no edges, or
  * fewer than 2 epochs). */
 EVOC_API int evoc_plan_autotune(evoc_plan_t* plan, int32_t* config, float* ms_per_launch);
@@ -375,6 +380,27 @@ EVOC_API int evoc_embed_batched(evoc_ctx_t* ctx, int32_t n_problems,
 EVOC_API int evoc_label_prop_partition(evoc_ctx_t* ctx, const evoc_graph_t* g,
                                        int64_t approx_n_parts, int32_t n_iter, uint64_t seed,
                                        uint32_t* partition, int64_t* n_parts);
+
+/* label_propagation_init (src/graph/label_prop.rs:537-564), the initial
+ * embedding evoc() computes before the embedding (lib.rs:271-284): recursive
+ * coarsening by the label-propagation partition (clamp(8 sqrt(n), 256,
+ * 16384) parts at the top, a quarter per level; 20 rounds), coarse graph
+ * clip(N^T G B) and coarse data per level, a PCA (data given, dim <= d) or
+ * random base case below 64 nodes, a 50-epoch embedding of each coarse graph
+ * (initial_alpha 0.05, seed + 4000), and the expansion averaged with the
+ * direct term, centred and scaled by 0.1 (:403-535). g is the fuzzy set of
+ * the points; data (host, n x d f32) or NULL; out (host, n x dim) receives
+ * the initial embedding, for evoc_embed's init. Sums follow the reference's
+ * sparse-algebra orders (sparse.rs:256-568); random draws are Philox, and the
+ * PCA base case signs each component so its largest entry is positive. */
+EVOC_API int evoc_label_propagation_init(evoc_ctx_t* ctx, const evoc_graph_t* g,
+                                         int32_t dim, const float* data, int64_t d,
+                                         uint64_t seed, float* out);
+
+/* The same with device-resident data (d_data may be NULL) and output. */
+EVOC_API int evoc_label_propagation_init_device(evoc_ctx_t* ctx, const evoc_graph_t* g,
+                                                int32_t dim, const float* d_data,
+                                                int64_t d, uint64_t seed, float* d_out);
 
 /* ---- learned warm start ----------------------------------------------------
  * No counterpart in the reference: a multilayer perceptron

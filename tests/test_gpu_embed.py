@@ -323,19 +323,27 @@ def test_blocks_reject_bad_input(ctx):
 
 def test_every_epoch_kernel_config_gives_the_same_embedding(ctx, blobs_knn):
     """All slots-kernel variants x warps per block x a blocks-per-SM cap give
-    bit-identical embeddings (the autotuner may pick any of them)."""
+    bit-identical embeddings (the autotuner may pick any of them), launched
+    per epoch (variants 0-3) or as one cooperative launch for all epochs
+    (4-7, run through the plan's normal run path)."""
+    import torch
     idx, dist, _ = blobs_knn
     g = ctx.fuzzy_set(idx, dist, 15.0, True)
     plan = ctx.plan(g, 4, seed=3)
     ref = plan.debug_run(None, 0, plan.n_epochs)
-    for variant in range(4):
+    out_d = torch.empty(g.n, 4, dtype=torch.float32, device="cuda")
+    for variant in range(8):
         for wpb in (1, 2, 4):
             for bps in (0, 2):
                 plan.set_config(variant, wpb, bps)
-                out = plan.debug_run(None, 0, plan.n_epochs)
+                if variant < 4:
+                    out = plan.debug_run(None, 0, plan.n_epochs)
+                else:
+                    plan.run_device(None, out_d.data_ptr())
+                    out = out_d.cpu().numpy()
                 assert np.array_equal(out.view(np.uint32), ref.view(np.uint32)), (variant, wpb, bps)
     with pytest.raises(Exception):
-        plan.set_config(4, 2, 0)
+        plan.set_config(8, 2, 0)
     with pytest.raises(Exception):
         plan.set_config(0, 3, 0)
     plan.free()
@@ -347,7 +355,7 @@ def test_autotune_keeps_results_and_caches_the_shape(ctx, blobs_knn, oracle):
     ip, ix, w = g.export()
     plan = ctx.plan(g, 8, seed=5)
     cfg = plan.autotune()
-    assert cfg["variant"] in range(4) and cfg["warps_per_block"] in (1, 2, 4)
+    assert cfg["variant"] in range(8) and cfg["warps_per_block"] in (1, 2, 4)
     assert cfg["ms_per_launch"] > 0
     out = plan.debug_run(None, 0, plan.n_epochs)
     ref = oracle.evoc_embedding(ip, ix, w, 8, seed=5)
