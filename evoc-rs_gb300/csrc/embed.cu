@@ -1012,21 +1012,19 @@ __device__ __forceinline__ int nth_set_bit(uint32_t m, int r) {
 // the order of the reference's serial sum: entries in incidence order, each
 // attraction followed by its negatives.
 constexpr int FILL_EPB = 8;
-constexpr int FILL_SEG = 2048;
-constexpr int FILL_Q = 128;      // queued draws per warp and window
-constexpr int FILL_STAGE = 384;  // staged slots per warp and window
+constexpr int FILL_SEG = 4096;
+constexpr int FILL_Q = 128;  // queued draws per warp and window
 struct FillJob {
-  int64_t q;        // slot index (global, or within the staged window)
+  int64_t q;        // slot index
   uint32_t eidx;    // edge id
   uint32_t jn;      // draw index j | tile-local node << 8
 };
 struct PlaneFillSmem {
-  uint2 stage[FILL_EPB][FILL_STAGE]; // per-warp slots of the current window
-  FillJob job[FILL_EPB][FILL_Q];     // per-warp draw queues
   uint32_t part[FILL_SEG];           // partner of each staged entry
+  uint8_t node[FILL_SEG];            // tile-local node of each staged entry
   int64_t pb[TILE + 1];              // incidence offsets of the tile's nodes
   int64_t eb[TILE];                  // edge-id bases of the tile's nodes
-  uint8_t node[FILL_SEG];            // tile-local node of each staged entry
+  FillJob job[FILL_EPB][FILL_Q];     // per-warp draw queues
 };
 
 __device__ __forceinline__ uint2 negative_slot(uint64_t seed, uint32_t j, int32_t t, uint32_t eidx,
@@ -1051,8 +1049,7 @@ __global__ void __launch_bounds__(32 * FILL_EPB) k_plane_fill(
     const uint32_t* __restrict__ nplane1, const int64_t* __restrict__ tile_off,
     const uint32_t* __restrict__ prob_of_node, const ProbInfo* __restrict__ prob,
     uint64_t seed, uint2* __restrict__ slots) {
-  extern __shared__ __align__(16) unsigned char fill_raw[];
-  PlaneFillSmem& sm = *reinterpret_cast<PlaneFillSmem*>(fill_raw);
+  __shared__ PlaneFillSmem sm;
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int ngroups = (ne + FILL_EPB - 1) / FILL_EPB;
@@ -1103,20 +1100,16 @@ __global__ void __launch_bounds__(32 * FILL_EPB) k_plane_fill(
       const int stot = __shfl_sync(FULL, sincl, 31), jtot = __shfl_sync(FULL, jincl, 31);
       if (stot == 0) continue;
       const bool queued = jtot <= FILL_Q;
-      // a window that fits is assembled in shared memory and leaves with
-      // coalesced stores; a larger one is written in place
-      const bool staged = stot <= FILL_STAGE;
-      uint2* dst = staged ? sm.stage[wid] : slots + cur;
-      int64_t q = sincl - (__popc(f) + nneg);  // within the window
+      int64_t q = cur + sincl - (__popc(f) + nneg);
       int jq = jincl - nneg;
-      __syncwarp();  // the previous window's drain and flush are done
+      __syncwarp();  // the previous window's drain has read its jobs
       while (f) {
         const int b = __ffs(f) - 1;
         f &= f - 1;
         const int64_t p = (w << 5) + b;
         const int li = (int)(p - sb);
         const uint32_t node = sm.node[li];
-        dst[q++] = make_uint2(sm.part[li], node);
+        slots[q++] = make_uint2(sm.part[li], node);
         const uint32_t nn = ((g0 >> b) & 1u) | (((g1 >> b) & 1u) << 1);
         if (nn) {
           const uint32_t eidx = (uint32_t)(p + sm.eb[node]);
@@ -1124,24 +1117,20 @@ __global__ void __launch_bounds__(32 * FILL_EPB) k_plane_fill(
             if (queued)
               job[jq++] = FillJob{q, eidx, j | (node << 8)};
             else
-              dst[q] = negative_slot(seed, j, t, eidx, node, v0, (uint32_t)n, prob_of_node, prob);
+              slots[q] = negative_slot(seed, j, t, eidx, node, v0, (uint32_t)n, prob_of_node, prob);
           }
         }
       }
+      cur += stot;
       if (queued && jtot > 0) {
         __syncwarp();  // the jobs are in shared memory
         for (int i = lane; i < jtot; i += 32) {
           const FillJob jb = job[i];
           const uint32_t node = jb.jn >> 8;
-          dst[jb.q] = negative_slot(seed, jb.jn & 0xffu, t, jb.eidx, node, v0, (uint32_t)n,
-                                    prob_of_node, prob);
+          slots[jb.q] = negative_slot(seed, jb.jn & 0xffu, t, jb.eidx, node, v0, (uint32_t)n,
+                                      prob_of_node, prob);
         }
       }
-      if (staged) {
-        __syncwarp();  // the window's slots are in shared memory
-        for (int i = lane; i < stot; i += 32) slots[cur + i] = sm.stage[wid][i];
-      }
-      cur += stot;
     }
   }
 }
@@ -1931,10 +1920,7 @@ static bool build_slots(evoc_plan* pl, const float* inc_ps, const uint8_t* inc_u
   const uint64_t seed0 = pl->seeds.empty() ? 0 : pl->seeds[0];
   if (use_planes) {
     const int64_t ngroups = (ne + FILL_EPB - 1) / FILL_EPB;
-    EVOC_CUDA(cudaFuncSetAttribute((const void*)k_plane_fill,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)sizeof(PlaneFillSmem)));
-    k_plane_fill<<<(unsigned)(ngroups * pl->ntiles), 32 * FILL_EPB, sizeof(PlaneFillSmem), s>>>(
+    k_plane_fill<<<(unsigned)(ngroups * pl->ntiles), 32 * FILL_EPB, 0, s>>>(
         pl->inc_ptr.get(), pl->inc_other.get(), pl->eidx_base.get(), n, pl->ntiles, planes_w,
         ne, fpl.get(), npl0.get(), npl1.get(), off.get(), pon, pinfo, seed0, pl->slots.get());
   } else {
