@@ -3,10 +3,12 @@ training the MLP on the GPU, and judging its initialisation.
 
 Points come from the seeded hierarchical generator (`workloads.py`); each
 instance's cosine kNN graph is built on the GPU, turned into a fuzzy
-simplicial set and embedded by the plain method (random init, full epochs) to
-give the layouts the network learns from. A fresh instance is then embedded
-twice: plain (random init, 50 epochs) and warm (network prediction as the
-initial embedding, fewer epochs).
+simplicial set and embedded by the plain method to give the layouts the
+network learns from. The plain method is evoc()'s own pipeline: the
+label-propagation initialisation with the points feeding its PCA base case
+(lib.rs:281), then 50 epochs; random initialisation with 50 epochs is the
+fallback form. A fresh instance is then embedded by the plain method and
+warm (network prediction as the initial embedding, fewer epochs).
 
 Quality is measured on the embedding against the input points:
   * trustworthiness@k (Venna & Kaski, 2001), estimated over a seeded sample
@@ -69,15 +71,27 @@ def embed_device(ctx, graph, n: int, dim: int, n_epochs: int, seed: int, init=No
     return out
 
 
+def lp_init(ctx, graph, inst: dict, dim: int, seed: int):
+    """label_propagation_init (label_prop.rs:537-564) of the instance's graph,
+    its f32 points feeding the PCA base case, as evoc() runs it (lib.rs:281)."""
+    torch = _torch()
+    out = torch.empty(inst["n"], dim, dtype=torch.float32, device="cuda")
+    ctx.label_propagation_init_device(graph, dim, inst["x"].data_ptr(), inst["d"], seed,
+                                      out.data_ptr())
+    return out
+
+
 def training_instance(ctx, n: int, d: int, k: int, dim: int, seed: int, n_epochs: int = 50,
-                      **gen) -> dict:
-    """Points and the plain method's layout of one training instance (device)."""
-    inst = make_instance(ctx, n, d, k, seed, **gen)
+                      init: str = "lp", **gen) -> dict:
+    """Points and the plain method's layout of one training instance (device):
+    init "lp" (label-propagation initialisation, evoc()'s own) or "random"."""
+    inst = make_instance(ctx, n, d, k, seed, keep_points=(init == "lp"), **gen)
     g = fuzzy_graph(ctx, inst)
-    inst["layout"] = embed_device(ctx, g, n, dim, n_epochs, seed)
+    start = lp_init(ctx, g, inst, dim, seed) if init == "lp" else None
+    inst["layout"] = embed_device(ctx, g, n, dim, n_epochs, seed, init=start)
     g.free()
-    for key in ("idx", "dist", "labels"):
-        inst.pop(key)
+    for key in ("idx", "dist", "labels", "x"):
+        inst.pop(key, None)
     return inst
 
 

@@ -232,7 +232,8 @@ def test_warm_start_beats_random_init_at_reduced_epochs(ctx):
     import evoc_gb300 as E
     import warm_start as WS
     gen = dict(n_parents=10, n_children=5)
-    train = [WS.training_instance(ctx, 20_000, 768, 15, 8, seed=100 + s, **gen) for s in range(3)]
+    train = [WS.training_instance(ctx, 20_000, 768, 15, 8, seed=100 + s, init="random", **gen)
+             for s in range(3)]
     net, hist, _ = WS.train(ctx, train, 512, 8,
                             E.MlpTrainParams(steps=600, batch=4096, align_every=100,
                                              align_rows=20_000, seed=1))
