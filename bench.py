@@ -26,13 +26,15 @@ the undirected edges fired (epoch_of_next_sample <= t) / time.
 768 -> 512 -> 512 -> 8 (BF16 tensor-core GEMMs, FP32 accumulation, GELU) is
 trained on the GPU on plain-method layouts of 20 seeded 2M-point instances of
 the generator above (seeds 100-119), then a fresh 1M-point instance (seed 777)
-is embedded plain (random init, 50 epochs) and warm (prediction as the
-initial embedding, fewer epochs). Its value is the plain time-to-embedding
-(fuzzy set + set-up + init + epochs, from the device kNN graph) over the warm
-one at the smallest epoch count whose trustworthiness@15 and kNN label
-accuracy match the plain run's (within 0.005); the reduced-epoch runs use
-initial_alpha 0.2 (the plain run keeps the default 0.1), and the same epoch
-count from a random init is reported beside it.
+is embedded plain (evoc()'s pipeline: label-propagation init, 50 epochs) and
+warm (prediction as the initial embedding, fewer epochs). Its value is the
+plain time-to-embedding (fuzzy set + init + set-up + epochs, from the device
+kNN graph) over the warm one at the smallest epoch count whose
+trustworthiness@15 and kNN label accuracy match the plain run's (within
+0.005); the reduced-epoch runs use initial_alpha 0.2 (the plain run keeps the
+default 0.1), and the same epoch count from a random init and from the
+label-propagation init is reported beside it, as is the plain method with a
+random init (the fallback form).
 
 --workload batch_c4 measures the batched configuration instead: 256
 independent problems, n log-uniform in [2,000, 150,000], 384-d, 5-60
@@ -74,6 +76,8 @@ WORKLOADS = {
     "label_prop_2m": dict(n=2_000_000, d=768, k=30, dim=8, seed=2),
     # the whole label-propagation initialisation of the 2M graph with its points
     "lp_init_2m": dict(n=2_000_000, d=768, k=30, dim=8, seed=2),
+    # build_mst of the plain 50-epoch embedding of the hierarchical points at 1M
+    "mst_1m": dict(n=1_000_000, d=768, k=30, dim=8, seed=2, min_samples=5),
     # the warm-start network's forward pass alone (n = rows)
     "mlp_forward": dict(n=1_000_000, d=768, k=0, dim=8, seed=777, hidden=512),
 }
@@ -611,11 +615,12 @@ def run_warm_start(args) -> dict:
     n_tr = args.c5_train_n or cfg["train_n"]
     m_tr = args.c5_train_instances or cfg["train_instances"]
     d, k, dim, seed, hid = cfg["d"], cfg["k"], cfg["dim"], cfg["seed"], cfg["hidden"]
+    plain_init = args.c5_plain_init
     ctx = E.Context(0)
     ctx_net = E.Context(0)  # the network's own stream: its prediction overlaps the fuzzy set
     t0 = time.time()
-    train = [WS.training_instance(ctx, n_tr, d, k, dim, seed=cfg["train_seed"] + s)
-             for s in range(m_tr)]
+    train = [WS.training_instance(ctx, n_tr, d, k, dim, seed=cfg["train_seed"] + s,
+                                  init=plain_init) for s in range(m_tr)]
     prep_s = time.time() - t0
     tp = E.MlpTrainParams(steps=args.c5_steps, batch=8192, align_every=250, align_rows=65536,
                           lr=1e-3, lr_end=1e-5, seed=1)
@@ -624,9 +629,17 @@ def run_warm_start(args) -> dict:
     torch.cuda.empty_cache()
     ev = WS.make_instance(ctx, n, d, k, seed, keep_points=True)
 
-    def plain_run(n_epochs, init_fn=None, alpha=0.1, run_seed=seed):
+    def run(n_epochs, start, alpha=0.1, run_seed=seed):
+        """Time to embedding from the device kNN graph: fuzzy set, the initial
+        embedding ("lp": label-propagation init; "net": the network's
+        prediction; "random"), plan set-up and epochs."""
         g = WS.fuzzy_graph(ctx, ev)
-        init = init_fn() if init_fn else None
+        if start == "lp":
+            init = WS.lp_init(ctx, g, ev, dim, run_seed)
+        elif start == "net":
+            init = WS.predict(net, ev)
+        else:
+            init = None
         out = WS.embed_device(ctx, g, n, dim, n_epochs, run_seed, init=init, initial_alpha=alpha)
         g.free()
         return out
@@ -655,16 +668,25 @@ def run_warm_start(args) -> dict:
         g.free()
         return out
 
+    def judged(emb, lab_ref):
+        q = WS.quality(ev["x"], emb, ev["labels"], n_queries=args.c5_queries)
+        q["ari_vs_plain"] = ari(labels_of(emb), lab_ref)
+        return q
+
     with ClockSampler() as clk:
-        t_plain, e_plain = WS.timed(lambda: plain_run(50), args.c5_reps)
+        t_plain, e_plain = WS.timed(lambda: run(50, plain_init), args.c5_reps)
         q_plain = WS.quality(ev["x"], e_plain, ev["labels"], n_queries=args.c5_queries)
         t_lab = time.time()
         lab_plain = labels_of(e_plain)
         labels_s = time.time() - t_lab
         del e_plain
-        e_reseed = plain_run(50, run_seed=seed + 1)
+        e_reseed = run(50, plain_init, run_seed=seed + 1)
         ari_reseed = ari(labels_of(e_reseed), lab_plain)
         del e_reseed
+        other = "random" if plain_init == "lp" else "lp"
+        t_other, e_other = WS.timed(lambda: run(50, other), args.c5_reps)
+        q_other = judged(e_other, lab_plain)
+        del e_other
         # the network's forward pass alone (device time, CUDA events)
         pred = WS.predict(net, ev)
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -677,25 +699,26 @@ def run_warm_start(args) -> dict:
         torch.cuda.synchronize()
         predict_ms = ev0.elapsed_time(ev1) / 5
         q_pred = WS.quality(ev["x"], pred, ev["labels"], n_queries=args.c5_queries)
-        rows, chosen, chosen_ari = [], None, None
+        q_pred["ari_vs_plain"] = ari(labels_of(pred), lab_plain)
+        del pred
+        rows, chosen, chosen_ari, chosen_ari_reseed = [], None, None, None
         for ew in args.c5_epochs:
-            t_w, e_w = WS.timed(lambda: plain_run(ew, lambda: WS.predict(net, ev), args.c5_alpha),
-                                args.c5_reps)
-            q_w = WS.quality(ev["x"], e_w, ev["labels"], n_queries=args.c5_queries)
-            q_w["ari_vs_plain"] = ari(labels_of(e_w), lab_plain)
+            t_w, e_w = WS.timed(lambda: run(ew, "net", args.c5_alpha), args.c5_reps)
+            q_w = judged(e_w, lab_plain)
             del e_w
-            t_r, e_r = WS.timed(lambda: plain_run(ew, None, args.c5_alpha), 1)
-            q_r = WS.quality(ev["x"], e_r, ev["labels"], n_queries=args.c5_queries)
-            q_r["ari_vs_plain"] = ari(labels_of(e_r), lab_plain)
-            del e_r
             t_o, e_o = WS.timed(lambda: warm_overlapped(ew, args.c5_alpha), args.c5_reps)
-            same = bool(torch.equal(e_o, WS.embed_device(
-                ctx, WS.fuzzy_graph(ctx, ev), n, dim, ew, seed, init=WS.predict(net, ev),
-                initial_alpha=args.c5_alpha)))
+            same = bool(torch.equal(e_o, run(ew, "net", args.c5_alpha)))
             del e_o
             row = {"epochs": ew, "warm_sequential_ms": round(t_w * 1e3, 2),
                    "warm_ms": round(t_o * 1e3, 2), "overlapped_equals_sequential": same,
-                   "warm": q_w, "random_init_ms": round(t_r * 1e3, 2), "random_init": q_r}
+                   "warm": q_w}
+            if ew <= args.c5_ablation_max_epochs:  # the same epochs from the other inits
+                t_r, e_r = WS.timed(lambda: run(ew, "random", args.c5_alpha), 1)
+                row["random_init_ms"], row["random_init"] = round(t_r * 1e3, 2), judged(e_r, lab_plain)
+                del e_r
+                t_l, e_l = WS.timed(lambda: run(ew, "lp", args.c5_alpha), 1)
+                row["lp_init_ms"], row["lp_init"] = round(t_l * 1e3, 2), judged(e_l, lab_plain)
+                del e_l
             rows.append(row)
             ok = (q_w["trustworthiness"] >= q_plain["trustworthiness"] - args.c5_tol and
                   q_w["knn_label_acc"] >= q_plain["knn_label_acc"] - args.c5_tol)
@@ -703,6 +726,8 @@ def run_warm_start(args) -> dict:
                 chosen = row
             if q_w["ari_vs_plain"] >= 0.98 and chosen_ari is None:
                 chosen_ari = row
+            if q_w["ari_vs_plain"] >= ari_reseed - args.c5_ari_tol and chosen_ari_reseed is None:
+                chosen_ari_reseed = row
     flops_fwd = 2.0 * n * (d * hid + hid * hid + hid * dim)
     tflops = flops_fwd / (predict_ms / 1e3) / 1e12
     flops_train = 3.0 * 2.0 * 8192 * (d * hid + hid * hid + hid * dim) * args.c5_steps
@@ -711,6 +736,8 @@ def run_warm_start(args) -> dict:
     peak = float(pk["bf16_tflops"])
     value = (t_plain / (chosen["warm_ms"] / 1e3)) if chosen else None
     chunks = (n + 262143) // 262144
+    init_name = {"lp": "label-propagation init (evoc()'s own, lib.rs:281)",
+                 "random": "random init"}
     return {
         "metric": METRIC_C5, "value": value, "unit": "x", "n_gpus": 1,
         "steps": args.c5_reps, "warmup": 0, "ms_per_step": chosen["warm_ms"] if chosen else None,
@@ -720,6 +747,8 @@ def run_warm_start(args) -> dict:
         "config": {"workload": "warm_start_c5", "n": n, "d": d, "k": k, "dim": dim,
                    "mlp": f"{d}->{hid}->{hid}->{dim} GELU", "train_instances": m_tr,
                    "train_n": n_tr, "train_seeds": f"{cfg['train_seed']}..{cfg['train_seed'] + m_tr - 1}",
+                   "plain_method": f"{init_name[plain_init]}, 50 epochs",
+                   "train_layouts": f"the plain method's ({init_name[plain_init]}, 50 epochs)",
                    "eval_seed": seed, "train_steps": args.c5_steps, "batch": 8192,
                    "lr": "1e-3 falling linearly to 1e-5",
                    "reduced_run_initial_alpha": args.c5_alpha,
@@ -727,23 +756,31 @@ def run_warm_start(args) -> dict:
                    "train_tflops": round(flops_train / train_s / 1e12, 1),
                    "loss_first_last": [float(hist[:50].mean()), float(hist[-50:].mean())],
                    "quality_tolerance": args.c5_tol,
-                   "time": "wall clock, synchronised, median of reps: fuzzy set + plan set-up "
-                           "+ init (network prediction or random) + epochs, from the device kNN "
-                           "graph; warm_ms runs the prediction concurrently with the fuzzy set "
-                           "(second context and stream), warm_sequential_ms one after the other",
+                   "time": "wall clock, synchronised, median of reps: fuzzy set + initial "
+                           "embedding (label-propagation init, network prediction or random) "
+                           "+ plan set-up + epochs, from the device kNN graph; warm_ms runs the "
+                           "prediction concurrently with the fuzzy set (second context and "
+                           "stream), warm_sequential_ms one after the other",
                    "ari_note": "adjusted Rand index of each run's final labels against the "
-                               "plain method's (random init, 50 epochs); labels from the "
-                               "reference's clustering stage (MST, condensed tree, persistence "
-                               "layers), which stays on the CPU, computed by its restatement in "
-                               "the oracle as the checker, untimed; ari_plain_reseed is the plain "
-                               "method with seed + 1 against the plain method, the run-to-run "
-                               "spread of the clustering itself",
+                               "plain method's; labels from the reference's clustering stage "
+                               "(MST, condensed tree, persistence layers), which stays on the "
+                               "CPU, computed by its restatement in the oracle as the checker, "
+                               "untimed; ari_plain_reseed is the plain method with seed + 1 "
+                               "against the plain method, the run-to-run spread of the "
+                               "clustering itself",
                    "chosen_by": "first reduced epoch count within quality_tolerance of the "
                                 "plain method's trustworthiness and kNN label accuracy"},
         "ari_plain_reseed": ari_reseed,
         "labels_cpu_s": round(labels_s, 1),
         "chosen_epochs_ari_098": chosen_ari["epochs"] if chosen_ari else None,
-        "plain": {"epochs": 50, "ms": round(t_plain * 1e3, 2), **q_plain},
+        "chosen_epochs_ari_within_reseed": chosen_ari_reseed["epochs"] if chosen_ari_reseed else None,
+        "ari_within_reseed_tolerance": args.c5_ari_tol,
+        "speedup_at_ari_within_reseed": (t_plain / (chosen_ari_reseed["warm_ms"] / 1e3))
+        if chosen_ari_reseed else None,
+        "plain": {"epochs": 50, "init": plain_init, "ms": round(t_plain * 1e3, 2), **q_plain},
+        f"plain_{other}_init": {"epochs": 50, "init": other, "ms": round(t_other * 1e3, 2),
+                                **q_other},
+        f"speedup_vs_plain_{other}_init": (t_other / (chosen["warm_ms"] / 1e3)) if chosen else None,
         "prediction_only": q_pred,
         "warm_sequential_speedup": (t_plain / (chosen["warm_sequential_ms"] / 1e3)) if chosen else None,
         "warm": rows, "chosen_epochs": chosen["epochs"] if chosen else None,
@@ -933,6 +970,73 @@ def run_lp_init(args) -> dict:
     }
 
 
+def run_mst(args) -> dict:
+    """build_mst (src/clustering/mst.rs:82-166) on the GPU, of the plain
+    method's embedding (random init, 50 epochs) of the hierarchical points at
+    1M: device points to device edges (median of steps), the oracle's CPU
+    restatement of the same call beside it (one run), and the two edge lists
+    compared edge for edge."""
+    import torch
+    import evoc_gb300 as E
+    import oracle as O
+    torch.cuda.init()
+    cfg = dict(WORKLOADS["mst_1m"])
+    n = args.n or cfg["n"]
+    wl, idx32, dist = make_workload("hierarchical_2m", n)
+    k, dim, ms = wl["k"], cfg["dim"], cfg["min_samples"]
+    ctx = E.Context(0)
+    g = ctx.fuzzy_set_device(idx32.data_ptr(), dist.data_ptr(), n, k, float(k), True)
+    plan = ctx.plan(g, dim, E.EvocEmbeddingParams(), seed=wl["seed"])
+    emb = torch.empty(n, dim, dtype=torch.float32, device="cuda")
+    plan.run_device(None, emb.data_ptr())
+    plan.free()
+    g.free()
+    del idx32, dist
+    du = torch.empty(n - 1, dtype=torch.int64, device="cuda")
+    dv = torch.empty_like(du)
+    dw = torch.empty(n - 1, dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        ctx.build_mst_device(emb.data_ptr(), n, dim, ms, du.data_ptr(), dv.data_ptr(),
+                             dw.data_ptr())
+    ts = []
+    with ClockSampler() as clk:
+        for _ in range(args.steps):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            m = ctx.build_mst_device(emb.data_ptr(), n, dim, ms, du.data_ptr(), dv.data_ptr(),
+                                     dw.data_ptr())
+            torch.cuda.synchronize()
+            ts.append(time.perf_counter() - t)
+    ms_gpu = float(np.median(ts)) * 1e3
+    gu, gv, gw = du.cpu().numpy()[:m], dv.cpu().numpy()[:m], dw.cpu().numpy()[:m]
+    eh = emb.cpu().numpy()
+    t = time.perf_counter()
+    ru, rv, rw = O.build_mst(eh, ms)
+    cpu_s = time.perf_counter() - t
+    same = bool(len(gu) == len(ru) and np.array_equal(gu, ru) and np.array_equal(gv, rv)
+                and np.array_equal(gw.view(np.uint32), rw.view(np.uint32)))
+    ctx.close()
+    return {
+        "metric": "build_mst time at 1M pts (dim 8 embedding, min_samples 5)",
+        "value": ms_gpu, "unit": "ms", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms_gpu, 3), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded, no dataset)",
+        "config": {"workload": "mst_1m", "n": n, "dim": dim, "min_samples": ms,
+                   "points": "the plain method's embedding (random init, 50 epochs) of the "
+                             "hierarchical generator's points, kNN k 30",
+                   "time": "wall clock, synchronised, median of steps; device points to device "
+                           "edges"},
+        "n_edges": int(m), "matches_oracle": same,
+        "cpu_baseline": {"value": round(cpu_s * 1e3, 1), "unit": "ms",
+                         "cores": O.max_threads(), "kind": "port",
+                         "sample": "the whole MST of the same points (the oracle: KD-tree "
+                                   "Boruvka, OpenMP queries)"},
+        "gpu_launches": None,
+        "clocks": clk.summary(),
+    }
+
+
 def run_reference(args) -> dict:
     """The reference's CPU path (the C++ restatement; Rust is not available)
     on the same workload: each step is one epoch of the embedding loop
@@ -986,12 +1090,19 @@ def main() -> None:
     ap.add_argument("--c5-train-instances", type=int, default=None)
     ap.add_argument("--c5-train-n", type=int, default=None)
     ap.add_argument("--c5-steps", type=int, default=8000)
-    ap.add_argument("--c5-epochs", type=int, nargs="+", default=[8, 10, 12, 15, 20])
+    ap.add_argument("--c5-epochs", type=int, nargs="+", default=[8, 10, 12, 15, 20, 25, 30, 40])
+    ap.add_argument("--c5-ablation-max-epochs", type=int, default=20,
+                    help="largest reduced epoch count also run from the random and the "
+                         "label-propagation inits")
     ap.add_argument("--c5-alpha", type=float, default=0.2,
                     help="initial_alpha of the reduced-epoch runs (warm and its random-init ablation)")
     ap.add_argument("--c5-reps", type=int, default=3)
     ap.add_argument("--c5-queries", type=int, default=2048)
     ap.add_argument("--c5-tol", type=float, default=0.005)
+    ap.add_argument("--c5-ari-tol", type=float, default=0.02,
+                    help="ARI tolerance below the plain method's own reseed ARI")
+    ap.add_argument("--c5-plain-init", choices=["lp", "random"], default="lp",
+                    help="initialisation of the plain method (and of the training layouts)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -1018,6 +1129,9 @@ def main() -> None:
         return
     if args.workload == "mlp_forward":
         print(json.dumps(run_mlp_forward(args)))
+        return
+    if args.workload == "mst_1m":
+        print(json.dumps(run_mst(args)))
         return
     if args.workload == "lp_init_2m":
         print(json.dumps(run_lp_init(args)))

@@ -26,7 +26,7 @@ ORACLE_SRCS = [ROOT / "oracle" / "evoc_oracle.cpp", ROOT / "oracle" / "evoc_labe
 ORACLE_LIB = ROOT / "oracle" / "liboracle.so"
 
 SOURCES = ["primitives.cu", "fuzzy_set.cu", "embed.cu", "capi.cu", "noalloc.cu", "measure.cu", "mlp.cu",
-           "label_prop.cu", "lp_init.cu"]
+           "label_prop.cu", "lp_init.cu", "mst.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",

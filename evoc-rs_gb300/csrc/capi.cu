@@ -700,6 +700,51 @@ int evoc_label_propagation_init_device(evoc_ctx_t* ctx, const evoc_graph_t* g, i
   EVOC_API_END(ctx)
 }
 
+// ---- clustering: minimum spanning tree -------------------------------------
+
+int evoc_build_mst(evoc_ctx_t* ctx, const float* data, int64_t n, int32_t dim,
+                   int32_t min_samples, int64_t* u, int64_t* v, float* w, int64_t* n_edges) {
+  EVOC_API_BEGIN
+  if (!ctx || !n_edges || (n > 1 && (!data || !u || !v || !w)))
+    throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL argument");
+  use_device(ctx);
+  cudaStream_t s = ctx->stream;
+  *n_edges = 0;
+  if (dim < 1 || dim > 16) throw evoc::Error(EVOC_ERR_UNSUPPORTED, "dim must be in 1..16");
+  if (n < 0) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "n must be >= 0");
+  const int64_t m = std::max<int64_t>(n - 1, 0);
+  evoc::DevBuf<float> dd(n * (int64_t)dim, s), dw(m, s);
+  evoc::DevBuf<int64_t> du(m, s), dv(m, s);
+  if (n > 1)
+    EVOC_CUDA(cudaMemcpyAsync(dd.get(), data, dd.bytes(), cudaMemcpyHostToDevice, s));
+  const int64_t k = evoc::build_mst_device(ctx, dd.get(), n, dim, min_samples, du.get(), dv.get(),
+                                           dw.get());
+  EVOC_CUDA(cudaStreamSynchronize(s));
+  evoc::check_status(ctx, "build_mst");
+  if (k > 0) {
+    EVOC_CUDA(cudaMemcpyAsync(u, du.get(), k * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    EVOC_CUDA(cudaMemcpyAsync(v, dv.get(), k * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    EVOC_CUDA(cudaMemcpyAsync(w, dw.get(), k * sizeof(float), cudaMemcpyDeviceToHost, s));
+    EVOC_CUDA(cudaStreamSynchronize(s));
+  }
+  *n_edges = k;
+  EVOC_API_END(ctx)
+}
+
+int evoc_build_mst_device(evoc_ctx_t* ctx, const float* d_data, int64_t n, int32_t dim,
+                          int32_t min_samples, int64_t* d_u, int64_t* d_v, float* d_w,
+                          int64_t* n_edges) {
+  EVOC_API_BEGIN
+  if (!ctx || !n_edges) throw evoc::Error(EVOC_ERR_INVALID_ARGUMENT, "NULL argument");
+  use_device(ctx);
+  *n_edges = 0;
+  const int64_t k = evoc::build_mst_device(ctx, d_data, n, dim, min_samples, d_u, d_v, d_w);
+  EVOC_CUDA(cudaStreamSynchronize(ctx->stream));
+  evoc::check_status(ctx, "build_mst");
+  *n_edges = k;
+  EVOC_API_END(ctx)
+}
+
 // ---- learned warm start ----------------------------------------------------
 
 void evoc_mlp_train_params_default(evoc_mlp_train_params_t* p) {

@@ -215,6 +215,13 @@ int64_t label_prop_partition(evoc_ctx* ctx, const evoc_graph* g, int64_t approx_
 void label_propagation_init_device(evoc_ctx* ctx, const evoc_graph* g, int32_t dim,
                                    const float* d_data, int64_t d, uint64_t seed, float* d_out);
 
+// ---- mst.cu ----------------------------------------------------------------
+// build_mst (mst.rs:82-166) of the n x dim device points d_data: writes the
+// minimum spanning tree's edges (u, v, weight) in the reference's insertion
+// order into d_u, d_v, d_w (n - 1 entries each); returns the edge count.
+int64_t build_mst_device(evoc_ctx* ctx, const float* d_data, int64_t n, int32_t dim,
+                         int32_t min_samples, int64_t* d_u, int64_t* d_v, float* d_w);
+
 // ---- mlp.cu ----------------------------------------------------------------
 }  // namespace evoc
 

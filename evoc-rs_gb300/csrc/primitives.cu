@@ -35,7 +35,8 @@ void check_status(evoc_ctx* ctx, const char* where) {
   if (st & ST_BAD_INDEX)
     throw Error(EVOC_ERR_INVALID_INPUT, w + ": an index is >= n");
   if (st & ST_BAD_VALUE)
-    throw Error(EVOC_ERR_INVALID_INPUT, w + ": a distance or weight is NaN");
+    throw Error(EVOC_ERR_INVALID_INPUT, w + ": a distance or weight is NaN, or a coordinate "
+                                            "is not finite");
   if (st & ST_EMPTY_ROW)
     throw Error(EVOC_ERR_INVALID_INPUT,
                 w + ": empty kNN row with local_connectivity > 0");

@@ -7,6 +7,8 @@ The binding mirrors the Rust functions the library replaces in evoc-rs 0.2.7:
     smooth_knn_dist              src/graph/fuzzy_graph.rs:33-98
     evoc_embedding               src/graph/embedding.rs:48-298
     EvocEmbeddingParams          src/graph/mod.rs:22-67
+    label_propagation_init       src/graph/label_prop.rs:537-564
+    build_mst                    src/clustering/mst.rs:82-166
 
 There is no CPU fallback: importing works anywhere, but creating a Context
 raises EvocError when the shared library or an sm_103 GPU is missing.
@@ -53,7 +55,7 @@ EXPORTED = [
     "evoc_to_bf16_device", "evoc_procrustes", "evoc_fuzzy_set_device_raw",
     "evoc_label_prop_partition", "evoc_selftest_wait_timeout", "evoc_ctx_smooth_knn_steps",
     "evoc_plan_set_config", "evoc_plan_autotune", "evoc_label_propagation_init",
-    "evoc_label_propagation_init_device",
+    "evoc_label_propagation_init_device", "evoc_build_mst", "evoc_build_mst_device",
 ]
 
 
@@ -161,6 +163,10 @@ def load_library(path: Path | str | None = None) -> C.CDLL:
                                         C.c_int),
         "evoc_label_propagation_init_device": ([vp, vp, C.c_int32, vp, C.c_int64, C.c_uint64,
                                                vp], C.c_int),
+        "evoc_build_mst": ([vp, vp, C.c_int64, C.c_int32, C.c_int32, vp, vp, vp,
+                            C.POINTER(C.c_int64)], C.c_int),
+        "evoc_build_mst_device": ([vp, vp, C.c_int64, C.c_int32, C.c_int32, vp, vp, vp,
+                                   C.POINTER(C.c_int64)], C.c_int),
         "evoc_smooth_knn_dist": ([vp, vp, vp, i64, i32, u64, f32, i32, vp, vp], C.c_int),
         "evoc_fuzzy_set": ([vp, vp, vp, i64, i32, f32, C.c_int, pp], C.c_int),
         "evoc_fuzzy_set_device": ([vp, vp, vp, i64, i32, f32, C.c_int, vp, vp, pp], C.c_int),
@@ -578,6 +584,34 @@ class Context:
         self._check(self.lib.evoc_label_propagation_init_device(
             self.handle, graph.handle, int(dim), C.c_void_p(d_data) if d_data else None, int(d),
             int(seed), C.c_void_p(d_out)))
+
+    def build_mst(self, data, min_samples: int = 5):
+        """build_mst (src/clustering/mst.rs:82-166): the minimum spanning tree
+        over mutual reachability of the rows of data (n x dim f32), as
+        (u, v, weight) arrays of its edges in insertion order."""
+        x = _f32(data)
+        if x.ndim != 2:
+            raise EvocError(EVOC_ERR_INVALID_ARGUMENT, "data must be n x dim")
+        n, dim = x.shape
+        m = max(n - 1, 0)
+        u = np.zeros(max(m, 1), np.int64)
+        v = np.zeros(max(m, 1), np.int64)
+        w = np.zeros(max(m, 1), np.float32)
+        ne = C.c_int64()
+        self._check(self.lib.evoc_build_mst(self.handle, _ptr(x), int(n), int(dim),
+                                            int(min_samples), _ptr(u), _ptr(v), _ptr(w),
+                                            C.byref(ne)))
+        k = ne.value
+        return u[:k], v[:k], w[:k]
+
+    def build_mst_device(self, d_data: int, n: int, dim: int, min_samples: int, d_u: int,
+                         d_v: int, d_w: int) -> int:
+        """build_mst of device points into device outputs; returns the edge count."""
+        ne = C.c_int64()
+        self._check(self.lib.evoc_build_mst_device(
+            self.handle, C.c_void_p(d_data), int(n), int(dim), int(min_samples),
+            C.c_void_p(d_u), C.c_void_p(d_v), C.c_void_p(d_w), C.byref(ne)))
+        return ne.value
 
     def graph_from_csr(self, indptr, indices, weights) -> Graph:
         ip = np.ascontiguousarray(indptr, dtype=np.int64)

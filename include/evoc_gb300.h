@@ -381,6 +381,28 @@ EVOC_API int evoc_label_prop_partition(evoc_ctx_t* ctx, const evoc_graph_t* g,
                                        int64_t approx_n_parts, int32_t n_iter, uint64_t seed,
                                        uint32_t* partition, int64_t* n_parts);
 
+/* build_mst (src/clustering/mst.rs:82-166): Boruvka's minimum spanning tree
+ * of n points (row-major n x dim f32, dim 1..16, finite) over mutual
+ * reachability distance, the first step of the clustering stage. Core
+ * distance = squared distance to the min(min_samples, n - 1)-th nearest
+ * other point (min_samples <= 64 after that clamp); edge weight = the square
+ * root of max(d^2, core_u, core_v). Ties follow fixed rules where the
+ * reference leaves them to its KD-tree's traversal and hash-map order: a
+ * point's nearest other-component point is the smallest index among equal
+ * values, a component's pick the point with the smallest index among equal
+ * values, and each round's picks are added in ascending order of their
+ * component's smallest point index. u, v, w (host, n - 1 entries each)
+ * receive the edges in insertion order; *n_edges the count (n - 1 for n >= 1
+ * and finite distances). */
+EVOC_API int evoc_build_mst(evoc_ctx_t* ctx, const float* data, int64_t n, int32_t dim,
+                            int32_t min_samples, int64_t* u, int64_t* v, float* w,
+                            int64_t* n_edges);
+
+/* The same with device-resident points and outputs. */
+EVOC_API int evoc_build_mst_device(evoc_ctx_t* ctx, const float* d_data, int64_t n,
+                                   int32_t dim, int32_t min_samples, int64_t* d_u,
+                                   int64_t* d_v, float* d_w, int64_t* n_edges);
+
 /* label_propagation_init (src/graph/label_prop.rs:537-564), the initial
  * embedding evoc() computes before the embedding (lib.rs:271-284): recursive
  * coarsening by the label-propagation partition (clamp(8 sqrt(n), 256,

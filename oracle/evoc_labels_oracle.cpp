@@ -30,13 +30,16 @@
 // and comparison orders.
 //
 // Documented deviations:
-//   1. The KD-tree median split uses std::nth_element instead of Rust's
-//      select_nth_unstable_by, so the order of points inside a node, and with
-//      it which of several points at an equal mutual-reachability distance a
-//      Boruvka query returns, can differ. With distinct distances the minimum
-//      spanning tree is unique and identical.
+//   1. Among several points at an equal mutual-reachability distance, a
+//      Boruvka query returns the one with the smallest index; the reference
+//      returns the first its tree traversal meets, which depends on the
+//      order of points inside its nodes (set by select_nth_unstable_by; the
+//      median split here uses std::nth_element). The result no longer
+//      depends on the tree. With distinct distances the minimum spanning
+//      tree is unique and identical.
 //   2. Boruvka merges each round's per-component best edges in ascending
-//      component id; the reference iterates an FxHashMap (mst.rs:140), whose
+//      order of the component's smallest point index; the reference
+//      iterates an FxHashMap keyed by disjoint-set roots (mst.rs:140), whose
 //      order depends on rustc-hash. Again only ties are affected.
 //   3. The squared distance is the serial left fold sum_d (a_d - b_d)^2, as in
 //      evoc_oracle.cpp (ann-search-rs euclidean_simd is not vendored).
@@ -214,7 +217,7 @@ struct KdTree {
         if (core[j] > bd) continue;
         const f32 sq = sq_dist(q, pt(j), dim);
         const f32 mr = std::max(std::max(sq, core[qi]), core[j]);
-        if (mr < bd) {
+        if (mr < bd || (mr == bd && bj != qi && j < bj)) {  // ties: smallest index
           bd = mr;
           bj = j;
         }
@@ -255,9 +258,9 @@ struct KdTree {
 
 // disjoint_set.rs:12-60
 struct DisjointSet {
-  std::vector<int64_t> parent, rank;
-  explicit DisjointSet(int64_t n) : parent(n), rank(n, 0) {
-    for (int64_t i = 0; i < n; ++i) parent[i] = i;
+  std::vector<int64_t> parent, rank, lo;  // lo: smallest element of each root's set
+  explicit DisjointSet(int64_t n) : parent(n), rank(n, 0), lo(n) {
+    for (int64_t i = 0; i < n; ++i) parent[i] = lo[i] = i;
   }
   int64_t find(int64_t x) {
     while (parent[x] != x) {
@@ -277,6 +280,7 @@ struct DisjointSet {
       parent[ry] = rx;
       rank[rx] += 1;
     }
+    lo[rx] = lo[ry] = std::min(lo[rx], lo[ry]);
     return true;
   }
 };
@@ -312,7 +316,7 @@ std::vector<Edge> build_mst(const f32* data, int64_t n, int64_t dim, int64_t min
   uint32_t fmax_bits;
   std::memcpy(&fmax_bits, &fmax, 4);
   for (;;) {
-    for (int64_t i = 0; i < n; ++i) pc[i] = ds.find(i);
+    for (int64_t i = 0; i < n; ++i) pc[i] = ds.lo[ds.find(i)];  // id: smallest point index
     tree.update_node_components(pc.data(), nc.data());
     std::fill(cbest.begin(), cbest.end(), fmax_bits);
 #pragma omp parallel for schedule(dynamic, 256)
@@ -685,12 +689,11 @@ int64_t n_clusters_of(const std::vector<int64_t>& l) {
   return m + 1;
 }
 
-// persistence.rs:387-463
-Layers build_cluster_layers(const f32* emb, int64_t n, int64_t dim, int64_t min_samples,
-                            int64_t base_mcs, double thr, int64_t max_layers) {
+// persistence.rs:387-463, from the minimum spanning tree on (:396-400 build it)
+Layers cluster_layers_from_mst(std::vector<Edge> mst, int64_t n, int64_t base_mcs, double thr,
+                               int64_t max_layers) {
   Layers out;
   if (n == 0) return out;
-  std::vector<Edge> mst = build_mst(emb, n, dim, min_samples);
   const std::vector<LinkRow> L = mst_to_linkage(mst, n);
   const std::vector<CNode> T = condense_tree(L, n, base_mcs);
   const std::vector<int64_t> leaves = extract_leaves(T, n);
@@ -728,6 +731,14 @@ Layers build_cluster_layers(const f32* emb, int64_t n, int64_t dim, int64_t min_
     out.persistence.push_back(all_p[i]);
   }
   return out;
+}
+
+// persistence.rs:387-463
+Layers build_cluster_layers(const f32* emb, int64_t n, int64_t dim, int64_t min_samples,
+                            int64_t base_mcs, double thr, int64_t max_layers) {
+  if (n == 0) return Layers();
+  return cluster_layers_from_mst(build_mst(emb, n, dim, min_samples), n, base_mcs, thr,
+                                 max_layers);
 }
 
 }  // namespace
@@ -790,6 +801,17 @@ OracleLayers* oracle_cluster_layers(const float* emb, int64_t n, int64_t dim, in
   OracleLayers* o = new OracleLayers();
   o->l = build_cluster_layers(emb, n, dim, min_samples, base_min_cluster_size, min_similarity,
                               max_layers);
+  return o;
+}
+// The same from a given minimum spanning tree (m edges u, v, weight).
+OracleLayers* oracle_cluster_layers_mst(const int64_t* u, const int64_t* v, const float* w,
+                                        int64_t m, int64_t n, int64_t base_min_cluster_size,
+                                        double min_similarity, int64_t max_layers) {
+  std::vector<Edge> mst((size_t)m);
+  for (int64_t i = 0; i < m; ++i) mst[i] = Edge{u[i], v[i], w[i]};
+  OracleLayers* o = new OracleLayers();
+  o->l = cluster_layers_from_mst(std::move(mst), n, base_min_cluster_size, min_similarity,
+                                 max_layers);
   return o;
 }
 int64_t oracle_layers_count(const OracleLayers* o) { return (int64_t)o->l.labels.size(); }

@@ -73,6 +73,7 @@ def lib() -> C.CDLL:
             "oracle_linkage": ([vp, vp, vp, i64, i64, vp, vp], None),
             "oracle_leaf_labels": ([vp, i64, i64, i64, i64, vp, vp], i64),
             "oracle_cluster_layers": ([vp, i64, i64, i64, i64, C.c_double, i64], vp),
+            "oracle_cluster_layers_mst": ([vp, vp, vp, i64, i64, i64, C.c_double, i64], vp),
             "oracle_layers_count": ([vp], i64),
             "oracle_layers_get": ([vp, i64, vp, vp, vp], None),
             "oracle_layers_free": ([vp], None),
@@ -342,6 +343,24 @@ def build_cluster_layers(embedding, min_samples: int = 5, base_min_cluster_size:
     L = lib()
     h = L.oracle_cluster_layers(_p(e), n, d, int(min_samples), int(base_min_cluster_size),
                                 float(min_similarity_threshold), int(max_layers))
+    return _layers(L, h, n)
+
+
+def build_cluster_layers_from_mst(u, v, w, n: int, base_min_cluster_size: int = 5,
+                                  min_similarity_threshold: float = 0.2, max_layers: int = 10):
+    """build_cluster_layers from a given minimum spanning tree (the MST built
+    by persistence.rs:396-400 replaced by (u, v, weight) in insertion order)."""
+    u = np.ascontiguousarray(u, np.int64)
+    v = np.ascontiguousarray(v, np.int64)
+    w = np.ascontiguousarray(w, np.float32)
+    L = lib()
+    h = L.oracle_cluster_layers_mst(_p(u), _p(v), _p(w), len(u), int(n),
+                                    int(base_min_cluster_size), float(min_similarity_threshold),
+                                    int(max_layers))
+    return _layers(L, h, n)
+
+
+def _layers(L, h, n: int):
     labels, strengths, pers = [], [], []
     try:
         for i in range(L.oracle_layers_count(h)):
