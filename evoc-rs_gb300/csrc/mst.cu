@@ -10,19 +10,22 @@
 // pruning bounds come from it, never a result.
 //
 // Core distances (mst.rs:101-113): per point, the k-th smallest squared
-// distance to another point, k = min(min_samples, n - 1); a thread per point
-// walks the tree with an explicit stack, nearer child first, and skips a node
-// whose box lower bound exceeds the current k-th distance (knn_recurse,
-// kd_tree.rs:489-535).
+// distance to another point, k = min(min_samples, n - 1); a warp walks the
+// tree for 32 consecutive points at once (see the traversal kernels), nearer
+// child first, and skips a node whose box lower bound exceeds every lane's
+// current k-th distance (knn_recurse, kd_tree.rs:489-535).
 //
 // Boruvka rounds (mst.rs:115-160):
 //   1. node components, bottom-up (update_node_components, kd_tree.rs:387-419);
 //   2. per point, the nearest point of another component under squared mutual
 //      reachability max(d^2, core_i, core_j) (nearest_other_component,
 //      kd_tree.rs:275-378), with the same three pruning rules; among equal
-//      values the smallest point index. A per-component bound (the best value
-//      found so far this round) starts each query just above it; that changes
-//      no component's pick;
+//      values the smallest point index. A per-component bound starts each
+//      query just above it and is lowered while the round runs: first the
+//      smallest value over the component's leaving kNN edges (kept from the
+//      core-distance pass), then the best value found so far by its points.
+//      Each is the value of a real edge leaving the component, so no
+//      component's pick changes;
 //   3. per component (its id is its smallest point index), the pick with the
 //      smallest value, then the smallest point index: one 64-bit atomicMin of
 //      (value bits, point index);
@@ -48,7 +51,6 @@ namespace evoc {
 namespace {
 
 constexpr int MST_LEAF = 32;     // points per leaf
-constexpr int MST_STACK = 48;    // traversal stack (tree depth <= 28)
 constexpr uint32_t NC_MIXED = 0xffffffffu;  // node holds points of several components
 constexpr uint32_t NC_EMPTY = 0xfffffffeu;  // node holds no point
 constexpr uint32_t NO_POINT = 0xffffffffu;
@@ -237,85 +239,184 @@ __global__ void k_mst_level_boxes(float* __restrict__ lo, float* __restrict__ hi
   }
 }
 
-// Push node v's children, nearer on top; children whose bound already
-// exceeds `bound` are not pushed (they would be skipped when popped).
+// Warp-cooperative traversal. A warp serves 32 consecutive sorted points
+// (spatially close in Morton order) and walks the union of their searches in
+// lockstep: it enters a node when any lane's own pruning rule keeps it,
+// descends first into the child most lanes find nearer and pushes the other
+// (re-tested when popped); the stack is warp-uniform, entry i held by lane i
+// (the tree is at most 28 levels deep). A leaf's points are staged once in
+// shared memory and every lane that needs the leaf scans them.
+constexpr int MST_WARPS = 4;  // warps per block
+
 template <int DIMP>
-__device__ __forceinline__ bool mst_push_children(const float* __restrict__ lo,
-                                                  const float* __restrict__ hi, int64_t v,
-                                                  const float (&q)[DIMP], float bound,
-                                                  uint32_t (&sv)[MST_STACK],
-                                                  float (&sl)[MST_STACK], int& sp) {
-  const float l0 = mst_box_lb<DIMP>(lo, hi, 2 * v, q), l1 = mst_box_lb<DIMP>(lo, hi, 2 * v + 1, q);
-  if (sp + 2 > MST_STACK) return false;
-  const bool left_first = l0 <= l1;
-  const uint32_t near = (uint32_t)(left_first ? 2 * v : 2 * v + 1);
-  const float lnear = left_first ? l0 : l1, lfar = left_first ? l1 : l0;
-  if (!(lfar > bound)) {
-    sv[sp] = near ^ 1u;
-    sl[sp] = lfar;
-    ++sp;
+struct MstLeafStage {
+  float4 pt[MST_LEAF][DIMP / 4];
+  uint32_t comp[MST_LEAF];
+  float core[MST_LEAF];
+  uint32_t orig[MST_LEAF];
+};
+
+template <int DIMP>
+__device__ __forceinline__ void mst_stage_leaf(MstLeafStage<DIMP>& st,
+                                               const float* __restrict__ xs, int64_t b0, int cnt,
+                                               int lane) {
+  if (lane < cnt) {
+    const float4* src = reinterpret_cast<const float4*>(xs + (b0 + lane) * DIMP);
+#pragma unroll
+    for (int q = 0; q < DIMP / 4; ++q) st.pt[lane][q] = __ldg(src + q);
   }
-  if (!(lnear > bound)) {
-    sv[sp] = near;
-    sl[sp] = lnear;
-    ++sp;
+}
+
+template <int DIMP>
+__device__ __forceinline__ void mst_staged(const MstLeafStage<DIMP>& st, int s2,
+                                           float (&y)[DIMP]) {
+#pragma unroll
+  for (int q = 0; q < DIMP / 4; ++q) {
+    const float4 t = st.pt[s2][q];
+    y[4 * q] = t.x;
+    y[4 * q + 1] = t.y;
+    y[4 * q + 2] = t.z;
+    y[4 * q + 3] = t.w;
   }
-  return true;
 }
 
 // Core distances: per sorted point, the k-th smallest squared distance to
-// another point (the k smallest kept sorted in registers).
+// another point (the k smallest kept sorted in registers); a node is skipped
+// when its box bound exceeds the current k-th distance (kd_tree.rs:499).
 template <int DIMP, int KMAX>
-__global__ void __launch_bounds__(128) k_mst_core(const float* __restrict__ xs, int64_t n,
-                                                  int64_t P, int64_t L,
-                                                  const float* __restrict__ lo,
-                                                  const float* __restrict__ hi, int k,
-                                                  float* __restrict__ core,
-                                                  int32_t* __restrict__ status) {
-  const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (pos >= n) return;
+__global__ void __launch_bounds__(32 * MST_WARPS) k_mst_core(
+    const float* __restrict__ xs, int64_t n, int64_t P, int64_t L, const float* __restrict__ lo,
+    const float* __restrict__ hi, int k, float* __restrict__ core, uint32_t* __restrict__ knn_j,
+    float* __restrict__ knn_d, int32_t* __restrict__ status) {
+  __shared__ MstLeafStage<DIMP> stage_s[MST_WARPS];
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t q0 = ((int64_t)blockIdx.x * MST_WARPS + wid) * 32;
+  if (q0 >= n) return;
+  MstLeafStage<DIMP>& st = stage_s[wid];
+  const int64_t pos = q0 + lane;
+  const bool act = pos < n;
   float q[DIMP];
-  mst_load<DIMP>(xs, pos, q);
+  mst_load<DIMP>(xs, act ? pos : q0, q);
   const float INF = __int_as_float(0x7f800000);
   float kd[KMAX];
+  uint32_t kj[KMAX];
 #pragma unroll
-  for (int t = 0; t < KMAX; ++t) kd[t] = INF;
-  float kth = INF;
-  uint32_t sv[MST_STACK];
-  float sl[MST_STACK];
-  sv[0] = 1u;
-  sl[0] = 0.0f;
-  int sp = 1;
-  while (sp > 0) {
-    --sp;
-    const int64_t v = sv[sp];
-    if (sl[sp] > kth) continue;
-    if (v >= P) {
-      const int64_t l = v - P;
-      if (l >= L) continue;
-      const int64_t e = min(n, (l + 1) * MST_LEAF);
-      for (int64_t j = l * MST_LEAF; j < e; ++j) {
-        if (j == pos) continue;
-        float y[DIMP];
-        mst_load<DIMP>(xs, j, y);
-        const float d = mst_sqd<DIMP>(q, y);
-        if (d < kth) {
+  for (int t = 0; t < KMAX; ++t) {
+    kd[t] = INF;
+    kj[t] = NO_POINT;
+  }
+  float kth = act ? INF : -1.0f;  // an idle lane needs no node
+  const unsigned actm = __ballot_sync(FULL, act);
+  uint32_t stk = 0;
+  int sp = 0;
+  int64_t v = 1;
+  float lbv = 0.0f;
+  for (;;) {
+    if (__any_sync(FULL, lbv <= kth)) {
+      if (v >= P) {
+        const int64_t l = v - P;
+        if (l < L) {
+          const int64_t b0 = l * MST_LEAF;
+          const int cnt = (int)min((int64_t)MST_LEAF, n - b0);
+          __syncwarp();
+          mst_stage_leaf<DIMP>(st, xs, b0, cnt, lane);
+          __syncwarp();
+          if (lbv <= kth) {
+            for (int s2 = 0; s2 < cnt; ++s2) {
+              if (b0 + s2 == pos) continue;
+              float y[DIMP];
+              mst_staged<DIMP>(st, s2, y);
+              const float d = mst_sqd<DIMP>(q, y);
+              if (d < kth) {
+                const uint32_t j = (uint32_t)(b0 + s2);
 #pragma unroll
-          for (int t = KMAX - 1; t > 0; --t) kd[t] = fmaxf(kd[t - 1], fminf(kd[t], d));
-          kd[0] = fminf(kd[0], d);
-          float kt = kd[0];
+                for (int t = KMAX - 1; t > 0; --t) {
+                  if (kd[t - 1] > d) {
+                    kd[t] = kd[t - 1];
+                    kj[t] = kj[t - 1];
+                  } else if (kd[t] > d) {
+                    kd[t] = d;
+                    kj[t] = j;
+                  }
+                }
+                if (kd[0] > d) {
+                  kd[0] = d;
+                  kj[0] = j;
+                }
+                float kt = kd[0];
 #pragma unroll
-          for (int t = 1; t < KMAX; ++t)
-            if (t == k - 1) kt = kd[t];
-          kth = kt;
+                for (int t = 1; t < KMAX; ++t)
+                  if (t == k - 1) kt = kd[t];
+                kth = kt;
+              }
+            }
+          }
+        }
+      } else {
+        const float l0 = mst_box_lb<DIMP>(lo, hi, 2 * v, q);
+        const float l1 = mst_box_lb<DIMP>(lo, hi, 2 * v + 1, q);
+        const bool n0 = __any_sync(FULL, l0 <= kth), n1 = __any_sync(FULL, l1 <= kth);
+        if (n0 || n1) {
+          const bool left = 2 * __popc(__ballot_sync(FULL, l0 <= l1) & actm) >= __popc(actm);
+          const bool na = left ? n0 : n1, nb = left ? n1 : n0;
+          const int64_t a = left ? 2 * v : 2 * v + 1;
+          if (na && nb) {
+            if (sp >= 32) {
+              if (lane == 0) set_status(status, ST_INTERNAL);
+              return;
+            }
+            if (lane == sp) stk = (uint32_t)(a ^ 1);
+            ++sp;
+          }
+          const int64_t c = na ? a : (a ^ 1);
+          lbv = (c == 2 * v) ? l0 : l1;
+          v = c;
+          continue;
         }
       }
-    } else if (!mst_push_children<DIMP>(lo, hi, v, q, kth, sv, sl, sp)) {
-      set_status(status, ST_INTERNAL);
-      return;
+    }
+    if (sp == 0) break;
+    --sp;
+    v = __shfl_sync(FULL, stk, sp);
+    lbv = mst_box_lb<DIMP>(lo, hi, v, q);
+  }
+  if (act) {
+    core[pos] = kth;
+#pragma unroll
+    for (int t = 0; t < KMAX; ++t)
+      if (t < k) {
+        knn_j[pos * k + t] = kj[t];
+        knn_d[pos * k + t] = kd[t];
+      }
+  }
+}
+
+// Upper bounds before a round's queries: per component, the smallest mutual
+// reachability value over the kNN edges (from the core-distance pass) that
+// leave it. Each is the value of a real edge leaving the component, so it is
+// never below the component's pick and starting the queries just above it
+// changes no pick.
+__global__ void k_mst_knn_bound(int64_t n, int k, const uint32_t* __restrict__ knn_j,
+                                const float* __restrict__ knn_d,
+                                const uint32_t* __restrict__ comp, const float* __restrict__ core,
+                                uint32_t* __restrict__ cbest) {
+  const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (pos >= n) return;
+  const uint32_t qc = comp[pos];
+  const float cq = core[pos];
+  float best = __uint_as_float(FMAX_BITS);
+  bool any = false;
+  for (int t = 0; t < k; ++t) {
+    const uint32_t j = knn_j[pos * k + t];
+    if (j >= n || comp[j] == qc) continue;  // an unfilled entry (no finite distance)
+    const float mr = fmaxf(fmaxf(knn_d[pos * k + t], cq), core[j]);
+    if (mr < best) {
+      best = mr;
+      any = true;
     }
   }
-  core[pos] = kth;
+  if (any) atomicMin(cbest + qc, __float_as_uint(best));
 }
 
 // Node components: a leaf's common component, NC_MIXED or NC_EMPTY.
@@ -352,59 +453,120 @@ __global__ void k_mst_round_reset(const uint32_t* __restrict__ A, int64_t m,
   ckey[c] = ~0ull;
 }
 
-// Nearest point of another component under squared mutual reachability.
+// Nearest point of another component under squared mutual reachability
+// (kd_tree.rs:318-378): a lane keeps a node when its box bound and its own
+// core distance do not exceed the lane's best value and the node is not
+// wholly of the lane's component. After each pop a lane lowers its bound to
+// just above its component's best value so far this round; a pick it holds
+// above that bound is dropped (it cannot be the component's pick).
 template <int DIMP>
-__global__ void __launch_bounds__(128) k_mst_noc(
+__global__ void __launch_bounds__(32 * MST_WARPS) k_mst_noc(
     const float* __restrict__ xs, int64_t n, int64_t P, int64_t L, const float* __restrict__ lo,
     const float* __restrict__ hi, const uint32_t* __restrict__ nd,
     const uint32_t* __restrict__ comp, const float* __restrict__ core,
     const uint32_t* __restrict__ orig, uint32_t* __restrict__ cbest,
     unsigned long long* __restrict__ ckey, uint32_t* __restrict__ bj_out,
     int32_t* __restrict__ status) {
-  const int64_t pos = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (pos >= n) return;
-  bj_out[pos] = NO_POINT;
-  const uint32_t qc = comp[pos];
-  if (nd[1] == qc) return;  // a single component
-  const float cq = core[pos];
-  // start just above the component's best so far (FLT_MAX when none)
-  const uint32_t bb = __ldcg(cbest + qc);
-  float bd = bb >= FMAX_BITS ? __uint_as_float(FMAX_BITS) : __uint_as_float(bb + 1u);
-  if (cq > bd) return;
-  uint32_t bj = NO_POINT, bo = 0;
+  __shared__ MstLeafStage<DIMP> stage_s[MST_WARPS];
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t q0 = ((int64_t)blockIdx.x * MST_WARPS + wid) * 32;
+  if (q0 >= n) return;
+  MstLeafStage<DIMP>& st = stage_s[wid];
+  const int64_t pos = q0 + lane;
+  const bool act = pos < n;
+  if (act) bj_out[pos] = NO_POINT;
+  const uint32_t root_c = nd[1];
+  const uint32_t qc = act ? comp[pos] : NC_MIXED;
+  const float cq = act ? core[pos] : 0.0f;
+  float bd = __uint_as_float(FMAX_BITS);
+  bool live = act && root_c != qc;  // root_c == qc: a single component
+  if (live) {
+    const uint32_t bb = __ldcg(cbest + qc);
+    if (bb < FMAX_BITS) bd = __uint_as_float(bb + 1u);
+    live = !(cq > bd);
+  }
+  if (!__any_sync(FULL, live)) return;
+  const unsigned actm = __ballot_sync(FULL, act);
   float q[DIMP];
-  mst_load<DIMP>(xs, pos, q);
-  uint32_t sv[MST_STACK];
-  float sl[MST_STACK];
-  sv[0] = 1u;
-  sl[0] = 0.0f;
-  int sp = 1;
-  while (sp > 0) {
-    --sp;
-    const int64_t v = sv[sp];
-    if (sl[sp] > bd) continue;
-    if (cq > bd) break;
-    if (nd[v] == qc) continue;
-    if (v >= P) {
-      const int64_t l = v - P;
-      if (l >= L) continue;
-      const int64_t e = min(n, (l + 1) * MST_LEAF);
-      for (int64_t j = l * MST_LEAF; j < e; ++j) {
-        if (comp[j] == qc) continue;
-        const float cj = core[j];
-        if (cj > bd) continue;
-        float y[DIMP];
-        mst_load<DIMP>(xs, j, y);
-        const float mr = fmaxf(fmaxf(mst_sqd<DIMP>(q, y), cq), cj);
-        if (mr < bd || (mr == bd && bj != NO_POINT && orig[j] < bo)) {
-          bd = mr;
-          bj = (uint32_t)j;
-          bo = orig[j];
+  mst_load<DIMP>(xs, act ? pos : q0, q);
+  uint32_t bj = NO_POINT, bo = 0;
+  uint32_t stk = 0;
+  int sp = 0;
+  int64_t v = 1;
+  float lbv = 0.0f;
+  for (;;) {
+    const bool need = live && !(lbv > bd) && nd[v] != qc;
+    if (__any_sync(FULL, need)) {
+      if (v >= P) {
+        const int64_t l = v - P;
+        if (l < L) {
+          const int64_t b0 = l * MST_LEAF;
+          const int cnt = (int)min((int64_t)MST_LEAF, n - b0);
+          __syncwarp();
+          mst_stage_leaf<DIMP>(st, xs, b0, cnt, lane);
+          if (lane < cnt) {
+            st.comp[lane] = comp[b0 + lane];
+            st.core[lane] = core[b0 + lane];
+            st.orig[lane] = orig[b0 + lane];
+          }
+          __syncwarp();
+          if (need) {
+            for (int s2 = 0; s2 < cnt; ++s2) {
+              if (st.comp[s2] == qc) continue;
+              const float cj = st.core[s2];
+              if (cj > bd) continue;
+              float y[DIMP];
+              mst_staged<DIMP>(st, s2, y);
+              const float mr = fmaxf(fmaxf(mst_sqd<DIMP>(q, y), cq), cj);
+              const uint32_t oj = st.orig[s2];
+              if (mr < bd || (mr == bd && bj != NO_POINT && oj < bo)) {
+                bd = mr;
+                bj = (uint32_t)(b0 + s2);
+                bo = oj;
+              }
+            }
+          }
+        }
+      } else {
+        const float l0 = mst_box_lb<DIMP>(lo, hi, 2 * v, q);
+        const float l1 = mst_box_lb<DIMP>(lo, hi, 2 * v + 1, q);
+        const bool ok = live && !(cq > bd);
+        const bool n0 = __any_sync(FULL, ok && !(l0 > bd) && nd[2 * v] != qc);
+        const bool n1 = __any_sync(FULL, ok && !(l1 > bd) && nd[2 * v + 1] != qc);
+        if (n0 || n1) {
+          const bool left = 2 * __popc(__ballot_sync(FULL, l0 <= l1) & actm) >= __popc(actm);
+          const bool na = left ? n0 : n1, nb = left ? n1 : n0;
+          const int64_t a = left ? 2 * v : 2 * v + 1;
+          if (na && nb) {
+            if (sp >= 32) {
+              if (lane == 0) set_status(status, ST_INTERNAL);
+              return;
+            }
+            if (lane == sp) stk = (uint32_t)(a ^ 1);
+            ++sp;
+          }
+          const int64_t c = na ? a : (a ^ 1);
+          lbv = (c == 2 * v) ? l0 : l1;
+          v = c;
+          continue;
         }
       }
-    } else if (!mst_push_children<DIMP>(lo, hi, v, q, bd, sv, sl, sp)) {
-      set_status(status, ST_INTERNAL);
-      return;
+    }
+    if (sp == 0) break;
+    --sp;
+    v = __shfl_sync(FULL, stk, sp);
+    lbv = mst_box_lb<DIMP>(lo, hi, v, q);
+    if (live) {  // the component's best so far, found by other lanes and warps
+      const uint32_t cb = __ldcg(cbest + qc);
+      if (cb < FMAX_BITS) {
+        const float nb = __uint_as_float(cb + 1u);
+        if (nb < bd) {
+          bd = nb;
+          bj = NO_POINT;
+        }
+      }
+      live = !(cq > bd);
     }
   }
   if (bj != NO_POINT) {
@@ -553,14 +715,14 @@ int log2_ceil(int64_t m) {
 
 template <int DIMP>
 void launch_core(int kmax_bucket, const float* xs, int64_t n, int64_t P, int64_t L,
-                 const float* lo, const float* hi, int k, float* core, int32_t* st,
-                 cudaStream_t s) {
-  const unsigned g = grid_of(n, 128);
+                 const float* lo, const float* hi, int k, float* core, uint32_t* kj, float* kd,
+                 int32_t* st, cudaStream_t s) {
+  const unsigned g = grid_of((n + 31) / 32, MST_WARPS);
   switch (kmax_bucket) {
-    case 8: k_mst_core<DIMP, 8><<<g, 128, 0, s>>>(xs, n, P, L, lo, hi, k, core, st); break;
-    case 16: k_mst_core<DIMP, 16><<<g, 128, 0, s>>>(xs, n, P, L, lo, hi, k, core, st); break;
-    case 32: k_mst_core<DIMP, 32><<<g, 128, 0, s>>>(xs, n, P, L, lo, hi, k, core, st); break;
-    default: k_mst_core<DIMP, 64><<<g, 128, 0, s>>>(xs, n, P, L, lo, hi, k, core, st); break;
+    case 8: k_mst_core<DIMP, 8><<<g, 32 * MST_WARPS, 0, s>>>(xs, n, P, L, lo, hi, k, core, kj, kd, st); break;
+    case 16: k_mst_core<DIMP, 16><<<g, 32 * MST_WARPS, 0, s>>>(xs, n, P, L, lo, hi, k, core, kj, kd, st); break;
+    case 32: k_mst_core<DIMP, 32><<<g, 32 * MST_WARPS, 0, s>>>(xs, n, P, L, lo, hi, k, core, kj, kd, st); break;
+    default: k_mst_core<DIMP, 64><<<g, 32 * MST_WARPS, 0, s>>>(xs, n, P, L, lo, hi, k, core, kj, kd, st); break;
   }
   EVOC_CHECK_LAUNCH();
 }
@@ -580,6 +742,7 @@ int64_t mst_run(evoc_ctx* ctx, const float* d_data, int64_t n, int dim, int k, i
     k_mst_bbox<<<dim3(gx, dim), 256, 0, s>>>(d_data, n, dim, bmin.get(), bmax.get(), st);
     EVOC_CHECK_LAUNCH();
   }
+  check_status(ctx, "build_mst");  // non-finite coordinates are rejected before any search
   const int bits = std::min(16, 64 / dim), total_bits = bits * dim;
   DevBuf<uint32_t> key(n, s);
   DevBuf<uint2> val(n, s);
@@ -613,12 +776,14 @@ int64_t mst_run(evoc_ctx* ctx, const float* d_data, int64_t n, int dim, int k, i
   }
   tr.mark("tree boxes");
   // core distances
-  DevBuf<float> core(n, s);
+  DevBuf<float> core(n, s), knn_d(n * (int64_t)k, s);
+  DevBuf<uint32_t> knn_j(n * (int64_t)k, s);
   if (k == 0) {
     EVOC_CUDA(cudaMemsetAsync(core.get(), 0, core.bytes(), s));
   } else {
     const int kb = k <= 8 ? 8 : k <= 16 ? 16 : k <= 32 ? 32 : 64;
-    launch_core<DIMP>(kb, xs.get(), n, P, L, lo.get(), hi.get(), k, core.get(), st, s);
+    launch_core<DIMP>(kb, xs.get(), n, P, L, lo.get(), hi.get(), k, core.get(), knn_j.get(),
+                      knn_d.get(), st, s);
   }
   tr.mark("core distances");
   // Boruvka rounds
@@ -643,7 +808,12 @@ int64_t mst_run(evoc_ctx* ctx, const float* d_data, int64_t n, int dim, int k, i
     }
     k_mst_round_reset<<<gm, 256, 0, s>>>(A.get(), m, cbest.get(), ckey.get());
     EVOC_CHECK_LAUNCH();
-    k_mst_noc<DIMP><<<grid_of(n, 128), 128, 0, s>>>(xs.get(), n, P, L, lo.get(), hi.get(),
+    if (k > 0) {
+      k_mst_knn_bound<<<gn, 256, 0, s>>>(n, k, knn_j.get(), knn_d.get(), comp.get(), core.get(),
+                                         cbest.get());
+      EVOC_CHECK_LAUNCH();
+    }
+    k_mst_noc<DIMP><<<grid_of((n + 31) / 32, MST_WARPS), 32 * MST_WARPS, 0, s>>>(xs.get(), n, P, L, lo.get(), hi.get(),
                                                      nd.get(), comp.get(), core.get(), orig.get(),
                                                      cbest.get(), ckey.get(), bj.get(), st);
     EVOC_CHECK_LAUNCH();
@@ -692,10 +862,13 @@ int64_t mst_run(evoc_ctx* ctx, const float* d_data, int64_t n, int dim, int k, i
     std::swap(A, A2);
     const int64_t kept = h_tot[0];
     len += kept;
+    if (tr.on) {
+      const std::string name = "round, " + std::to_string(m) + " components";
+      tr.mark(name.c_str());
+    }
     m = h_tot[1];
     if (kept == 0) break;  // no pick merged anything (mst.rs:143-160)
   }
-  tr.mark("boruvka rounds");
   return len;
 }
 
