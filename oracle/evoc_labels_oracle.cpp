@@ -689,7 +689,7 @@ int64_t n_clusters_of(const std::vector<int64_t>& l) {
   return m + 1;
 }
 
-// persistence.rs:387-463, from the minimum spanning tree on (:396-400 build it)
+// persistence.rs:387-463, from the minimum spanning tree on (:402 builds it)
 Layers cluster_layers_from_mst(std::vector<Edge> mst, int64_t n, int64_t base_mcs, double thr,
                                int64_t max_layers) {
   Layers out;

@@ -349,7 +349,7 @@ def build_cluster_layers(embedding, min_samples: int = 5, base_min_cluster_size:
 def build_cluster_layers_from_mst(u, v, w, n: int, base_min_cluster_size: int = 5,
                                   min_similarity_threshold: float = 0.2, max_layers: int = 10):
     """build_cluster_layers from a given minimum spanning tree (the MST built
-    by persistence.rs:396-400 replaced by (u, v, weight) in insertion order)."""
+    by persistence.rs:402 replaced by (u, v, weight) in insertion order)."""
     u = np.ascontiguousarray(u, np.int64)
     v = np.ascontiguousarray(v, np.int64)
     w = np.ascontiguousarray(w, np.float32)
