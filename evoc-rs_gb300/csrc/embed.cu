@@ -1311,10 +1311,13 @@ struct alignas(16) SlotSmem {
   int32_t end[TILE];           // one past its last
 };
 
-// Contribution of one slot; +0 where the reference adds nothing (adding +0
-// leaves the running sum unchanged: it starts at +0 and never becomes -0).
-// One division serves both kinds; a negative sample equal to the node itself
-// has dsq = 0 and contributes nothing, like the reference's skip.
+// Contribution of one slot; a signed zero where the reference adds nothing
+// (adding +0 or -0 leaves the running sum unchanged: it starts at +0 and never
+// becomes -0). One division serves both kinds; a negative sample equal to the
+// node itself has dsq = 0 and contributes nothing, like the reference's skip.
+// The "adds nothing" case zeroes the coefficient before the product, and an
+// attraction's clamp bounds are infinite, so each dimension is one product,
+// one max and one min.
 template <int DIMP>
 __device__ __forceinline__ void slot_contrib(float (&c)[DIMP], bool neg,
                                              const float (&ev)[DIMP],
@@ -1332,15 +1335,15 @@ __device__ __forceinline__ void slot_contrib(float (&c)[DIMP], bool neg,
   const float num = neg ? gamma4 : fsub(-fmul(two_noise, dist), 2.0f);
   const float den = neg ? fmul(fadd(1.0f, fmul(0.25f, dsq)), dsq)
                         : fadd(fsub(fmul(2.0f, dsq), fmul(0.5f, dist)), 1.0f);
-  const float k = fdiv(num, den);
   const bool on = neg ? (dsq > 0.01f) : (dsq >= 1e-8f);
+  const float k = on ? fdiv(num, den) : 0.0f;
+  const float lo = neg ? -4.0f : -__int_as_float(0x7f800000);
+  const float hi = neg ? 4.0f : __int_as_float(0x7f800000);
 #pragma unroll
   for (int h = 0; h < DIMP / 2; ++h) {
     const float2 x = fmul2(make_float2(k, k), diff[h]);
-    const float y0 = neg ? fminf(fmaxf(x.x, -4.0f), 4.0f) : x.x;
-    const float y1 = neg ? fminf(fmaxf(x.y, -4.0f), 4.0f) : x.y;
-    c[2 * h] = on ? y0 : 0.0f;
-    c[2 * h + 1] = on ? y1 : 0.0f;
+    c[2 * h] = fminf(fmaxf(x.x, lo), hi);
+    c[2 * h + 1] = fminf(fmaxf(x.y, lo), hi);
   }
 }
 
@@ -1348,7 +1351,7 @@ __device__ __forceinline__ void slot_contrib(float (&c)[DIMP], bool neg,
 template <int DIMP, int WIN, int U, bool COH>
 __device__ __forceinline__ void slot_group(const EpochArgs& a, SlotSmem<DIMP, WIN>& sm,
                                            const uint2* __restrict__ wslots, int ib, int wn,
-                                           int lane, int& carry, uint32_t& act_mask,
+                                           int lane, int& carry,
                                            float two_noise, float gamma4) {
   const unsigned FULL = 0xffffffffu;
   uint2 sl[U];
@@ -1368,7 +1371,6 @@ __device__ __forceinline__ void slot_group(const EpochArgs& a, SlotSmem<DIMP, WI
     if (lane == 0) prev = carry;
     carry = __shfl_sync(FULL, node, 31);
     if (i < wn && node != prev) sm.start[node] = i;
-    act_mask |= __reduce_or_sync(FULL, (i < wn && !(sl[u].y & 32u)) ? (1u << node) : 0u);
   }
 #pragma unroll
   for (int u = 0; u < U; ++u) {
@@ -1413,10 +1415,10 @@ __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP, WIN
     int carry = -1;  // node of the previous slot of the window
     int ib = 0;
     for (; ib + 32 * SU <= wn; ib += 32 * SU)
-      slot_group<DIMP, WIN, SU, COH>(a, sm, wslots, ib, wn, lane, carry, act_mask, two_noise,
+      slot_group<DIMP, WIN, SU, COH>(a, sm, wslots, ib, wn, lane, carry, two_noise,
                                      gamma4);
     for (; ib < wn; ib += 32)
-      slot_group<DIMP, WIN, 1, COH>(a, sm, wslots, ib, wn, lane, carry, act_mask, two_noise,
+      slot_group<DIMP, WIN, 1, COH>(a, sm, wslots, ib, wn, lane, carry, two_noise,
                                     gamma4);
     __syncwarp();
     // run of node l: [start[l], first start of a later node or wn)
@@ -1431,6 +1433,7 @@ __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP, WIN
     if (lane == 31) en = wn;
     sm.end[lane] = en;
     const uint32_t present = __ballot_sync(FULL, st != WIN);
+    act_mask |= present;  // a node's first slot of the epoch is an attraction
     __syncwarp();
     constexpr int PARTS = slot_parts<DIMP>(), PD = DIMP / PARTS;  // dims per lane
     const int ntask = __popc(present) * PARTS;
