@@ -193,7 +193,7 @@ def profiled_traffic() -> tuple[float | None, str | None]:
 def algorithmic_hbm_bytes(n: int, info: dict, dimp: int, stats: np.ndarray) -> np.ndarray:
     """Per-epoch bytes the epoch kernel must move to/from HBM (the partner and
     negative row gathers are served by L2 and counted separately).
-    Slots path: tile offsets 8 (n/32 + 1), tile order 4 n/32, slots 8 per
+    Slots path: tile offsets 8 (n/32 + 1), tile order 4 n/32, slots 4 per
     fired directed entry (2 F_t) and per negative sample (N_t), own rows read +
     next rows written 2 * 4 dimp n, Adam moments read + written 4 * 4 dimp A_t.
     Bit-plane path: incidence offsets 8 (n + 1), fire + negative-count planes
@@ -202,7 +202,7 @@ def algorithmic_hbm_bytes(n: int, info: dict, dimp: int, stats: np.ndarray) -> n
     row = 4 * dimp
     common = 2 * row * n + 4 * row * A
     if info["n_slots"]:
-        return (8 * (n // 32 + 1) + 4 * (n // 32) + 8 * (2 * F + N) + common).astype(np.float64)
+        return (8 * (n // 32 + 1) + 4 * (n // 32) + 4 * (2 * F + N) + common).astype(np.float64)
     return (8 * (n + 1) + (1 + info["neg_planes"]) * info["n_incidence"] / 8 + 4 * 2 * F
             + common).astype(np.float64)
 

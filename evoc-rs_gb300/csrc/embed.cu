@@ -93,7 +93,7 @@ struct evoc_plan {
   int64_t n_slots = 0;
   evoc::DevBuf<int64_t> tile_off;
   evoc::DevBuf<uint32_t> tile_order;  // tiles by descending slot count (launch order)
-  evoc::DevBuf<uint2> slots;
+  evoc::DevBuf<uint32_t> slots;
   evoc::DevBuf<unsigned long long> work_ctr;  // per epoch
   unsigned slot_grid = 0;                     // persistent grid of the slots kernel
   int32_t kvariant = 0;                       // slots-kernel variant (SLOT_VARIANTS)
@@ -466,7 +466,7 @@ struct EpochArgs {
   const ProbInfo* prob;
   const int64_t* tile_off;     // slot offsets of this epoch (slots path)
   const uint32_t* tile_order;  // slots path: tiles in launch order, heaviest first
-  const uint2* slots;
+  const uint32_t* slots;
   unsigned long long* work_ctr;  // slots path: next tile of this epoch (zeroed per launch)
   uint32_t n_total;
   uint32_t epoch;
@@ -1027,7 +1027,15 @@ struct PlaneFillSmem {
   FillJob job[FILL_EPB][FILL_Q];     // per-warp draw queues
 };
 
-__device__ __forceinline__ uint2 negative_slot(uint64_t seed, uint32_t j, int32_t t, uint32_t eidx,
+// A gradient slot is one word: (source row << 6) | (1 << 5 for a negative
+// sample) | tile-local node. Plans with 2^26 or more nodes take the scan path.
+constexpr int SLOT_ROW_SHIFT = 6;
+constexpr int64_t SLOT_MAX_ROWS = (int64_t)1 << 26;
+__device__ __forceinline__ uint32_t make_slot(uint32_t row, uint32_t node_flags) {
+  return (row << SLOT_ROW_SHIFT) | node_flags;
+}
+
+__device__ __forceinline__ uint32_t negative_slot(uint64_t seed, uint32_t j, int32_t t, uint32_t eidx,
                                                uint32_t node, int64_t v0, uint32_t n_total,
                                                const uint32_t* __restrict__ prob_of_node,
                                                const ProbInfo* __restrict__ prob) {
@@ -1039,7 +1047,7 @@ __device__ __forceinline__ uint2 negative_slot(uint64_t seed, uint32_t j, int32_
     np = pi.n;
     sd = pi.seed;
   }
-  return make_uint2(nb + negative_draw(sd, j, (uint32_t)t, eidx, np), node | 32u);
+  return make_slot(nb + negative_draw(sd, j, (uint32_t)t, eidx, np), node | 32u);
 }
 
 __global__ void __launch_bounds__(32 * FILL_EPB) k_plane_fill(
@@ -1048,7 +1056,7 @@ __global__ void __launch_bounds__(32 * FILL_EPB) k_plane_fill(
     const uint32_t* __restrict__ fplane, const uint32_t* __restrict__ nplane0,
     const uint32_t* __restrict__ nplane1, const int64_t* __restrict__ tile_off,
     const uint32_t* __restrict__ prob_of_node, const ProbInfo* __restrict__ prob,
-    uint64_t seed, uint2* __restrict__ slots) {
+    uint64_t seed, uint32_t* __restrict__ slots) {
   __shared__ PlaneFillSmem sm;
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -1109,7 +1117,7 @@ __global__ void __launch_bounds__(32 * FILL_EPB) k_plane_fill(
         const int64_t p = (w << 5) + b;
         const int li = (int)(p - sb);
         const uint32_t node = sm.node[li];
-        slots[q++] = make_uint2(sm.part[li], node);
+        slots[q++] = make_slot(sm.part[li], node);
         const uint32_t nn = ((g0 >> b) & 1u) | (((g1 >> b) & 1u) << 1);
         if (nn) {
           const uint32_t eidx = (uint32_t)(p + sm.eb[node]);
@@ -1201,7 +1209,7 @@ __global__ void k_sched_fill(const int64_t* __restrict__ inc_ptr,
                              const int64_t* __restrict__ tile_off,
                              const uint32_t* __restrict__ prob_of_node,
                              const ProbInfo* __restrict__ prob, uint64_t seed,
-                             uint2* __restrict__ slots) {
+                             uint32_t* __restrict__ slots) {
   extern __shared__ int64_t cursors[];
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -1254,10 +1262,10 @@ __global__ void k_sched_fill(const int64_t* __restrict__ inc_ptr,
       o0 = __shfl_sync(FULL, o0, 0);
       if (f) {
         int64_t q = o0 + incl - c;
-        slots[q] = make_uint2(other, (uint32_t)node);
+        slots[q] = make_slot(other, (uint32_t)node);
         for (uint64_t j = 0; j < nn; ++j)
-          slots[++q] = make_uint2(nb + negative_draw(sd, (uint32_t)j, (uint32_t)t, eidx, np),
-                                  (uint32_t)node | 32u);
+          slots[++q] = make_slot(nb + negative_draw(sd, (uint32_t)j, (uint32_t)t, eidx, np),
+                                 (uint32_t)node | 32u);
       }
       const int64_t tot = __shfl_sync(FULL, incl, 31);
       if (lane == 0) cur[t] = o0 + tot;
@@ -1268,7 +1276,7 @@ __global__ void k_sched_fill(const int64_t* __restrict__ inc_ptr,
 // Per-epoch active nodes (a fired entry, i.e. an attraction slot) from the
 // slots (on request).
 __global__ void k_slot_stats(const int64_t* __restrict__ tile_off,
-                             const uint2* __restrict__ slots, int64_t ntiles, int32_t ne,
+                             const uint32_t* __restrict__ slots, int64_t ntiles, int32_t ne,
                              unsigned long long* __restrict__ active) {
   const unsigned FULL = 0xffffffffu;
   const int64_t tile = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -1279,7 +1287,7 @@ __global__ void k_slot_stats(const int64_t* __restrict__ tile_off,
     const int64_t r1 = tile_off[(int64_t)t * ntiles + tile + 1];
     uint32_t mask = 0;
     for (int64_t r = r0 + lane; r < r1; r += 32) {
-      const uint32_t y = slots[r].y;
+      const uint32_t y = slots[r];
       if (!(y & 32u)) mask |= 1u << (y & 31u);
     }
     mask = __reduce_or_sync(FULL, mask);
@@ -1350,11 +1358,11 @@ __device__ __forceinline__ void slot_contrib(float (&c)[DIMP], bool neg,
 // Phase 1 for U slots per lane: window slots ib + 32 u + lane, u < U.
 template <int DIMP, int WIN, int U, bool COH>
 __device__ __forceinline__ void slot_group(const EpochArgs& a, SlotSmem<DIMP, WIN>& sm,
-                                           const uint2* __restrict__ wslots, int ib, int wn,
+                                           const uint32_t* __restrict__ wslots, int ib, int wn,
                                            int lane, int& carry,
                                            float two_noise, float gamma4) {
   const unsigned FULL = 0xffffffffu;
-  uint2 sl[U];
+  uint32_t sl[U];
   float row[U][DIMP];
 #pragma unroll
   for (int u = 0; u < U; ++u) {  // past the end: the window's last slot again
@@ -1362,11 +1370,12 @@ __device__ __forceinline__ void slot_group(const EpochArgs& a, SlotSmem<DIMP, WI
     sl[u] = __ldcs(wslots + (i < wn ? i : wn - 1));
   }
 #pragma unroll
-  for (int u = 0; u < U; ++u) load_row<DIMP, COH>(a.e_cur + (size_t)sl[u].x * DIMP, row[u]);
+  for (int u = 0; u < U; ++u)
+    load_row<DIMP, COH>(a.e_cur + (size_t)(sl[u] >> SLOT_ROW_SHIFT) * DIMP, row[u]);
 #pragma unroll
   for (int u = 0; u < U; ++u) {  // run starts (a repeated last slot starts nothing)
     const int i = ib + 32 * u + lane;
-    const int node = (int)(sl[u].y & 31u);
+    const int node = (int)(sl[u] & 31u);
     int prev = __shfl_up_sync(FULL, node, 1);
     if (lane == 0) prev = carry;
     carry = __shfl_sync(FULL, node, 31);
@@ -1376,11 +1385,11 @@ __device__ __forceinline__ void slot_group(const EpochArgs& a, SlotSmem<DIMP, WI
   for (int u = 0; u < U; ++u) {
     const int i = ib + 32 * u + lane;
     if (i < wn) {
-      const int node = (int)(sl[u].y & 31u);
+      const int node = (int)(sl[u] & 31u);
       float ev[DIMP], c[DIMP];
 #pragma unroll
       for (int d = 0; d < DIMP; ++d) ev[d] = sm.rows[node][d];
-      slot_contrib<DIMP>(c, (sl[u].y & 32u) != 0, ev, row[u], two_noise, gamma4);
+      slot_contrib<DIMP>(c, (sl[u] & 32u) != 0, ev, row[u], two_noise, gamma4);
       float4* cd = reinterpret_cast<float4*>(&sm.c[i][0]);
 #pragma unroll
       for (int q = 0; q < DIMP / 4; ++q)
@@ -1409,7 +1418,7 @@ __device__ __forceinline__ void slot_tile(const EpochArgs& a, SlotSmem<DIMP, WIN
   uint32_t act_mask = 0;
   for (int64_t w0 = s0; w0 < s1; w0 += WIN) {
     const int wn = (int)min((int64_t)WIN, s1 - w0);
-    const uint2* wslots = a.slots + w0;
+    const uint32_t* wslots = a.slots + w0;
     sm.start[lane] = WIN;  // none
     __syncwarp();
     int carry = -1;  // node of the previous slot of the window
@@ -1825,6 +1834,7 @@ static bool build_slots(evoc_plan* pl, const float* inc_ps, const uint8_t* inc_u
   const bool force_scan = env && std::strcmp(env, "scan") == 0;
   const bool force_slots = env && std::strcmp(env, "slots") == 0;
   if (force_scan || (size_t)ne * sizeof(int64_t) > 200 * 1024) return false;
+  if (n >= SLOT_MAX_ROWS) return false;  // a slot's row field holds 26 bits
   const int wpb = (int)std::max<size_t>(
       1, std::min<size_t>(4, (200 * 1024) / ((size_t)ne * sizeof(int64_t))));
   const unsigned grid = (unsigned)((pl->ntiles + wpb - 1) / wpb);
@@ -1893,7 +1903,7 @@ static bool build_slots(evoc_plan* pl, const float* inc_ps, const uint8_t* inc_u
                 "(negative_sample_rate too large)");
   size_t free_b = 0, total_b = 0;
   EVOC_CUDA(cudaMemGetInfo(&free_b, &total_b));
-  const double need = (double)sizeof(uint2) * (double)total;
+  const double need = (double)sizeof(uint32_t) * (double)total;
   const double avail = (double)free_b + (double)pl->ctx->slot_cache.bytes();  // the cache is reusable
   if (!force_slots && need > 0.5 * avail) return false;
   pl->max_neg = maxneg;

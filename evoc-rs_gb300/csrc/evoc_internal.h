@@ -144,7 +144,7 @@ struct evoc_ctx {
   // The largest gradient-slot buffer of a freed plan, handed to the next plan
   // that fits in it (stream order makes the reuse safe): repeated one-shot
   // embeddings skip a multi-gigabyte allocation each.
-  evoc::DevBuf<uint2> slot_cache;
+  evoc::DevBuf<uint32_t> slot_cache;
   // Row-sum evaluations (bisection steps over all rows) of the most recent
   // smooth_knn pass on this context: the work figure of its ALU bound.
   evoc::DevBuf<unsigned long long> sk_steps;
