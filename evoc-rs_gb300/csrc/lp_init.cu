@@ -213,15 +213,26 @@ __global__ void k_runs_to_csr(const uint2* __restrict__ vals, int64_t m, float l
 // ---------------------------------------------------------------------------
 // Data reduction: block per part, thread per feature column.
 // ---------------------------------------------------------------------------
+// The sum over the part's nodes stays serial in node order; the loads of the
+// next eight nodes are issued before their adds, so they overlap.
 __global__ void k_reduce_data(const float* __restrict__ x, int64_t d,
                               const int64_t* __restrict__ poff, const uint2* __restrict__ nodes,
                               const float* __restrict__ rv, float* __restrict__ out) {
+  constexpr int U = 8;
   const int64_t P = blockIdx.x;
   const float v = rv[P];
   const int64_t a = poff[P], b = poff[P + 1];
   for (int64_t k = threadIdx.x; k < d; k += blockDim.x) {
     float acc = 0.0f;
-    for (int64_t q = a; q < b; ++q) acc = fadd(acc, fmul(v, x[(int64_t)nodes[q].x * d + k]));
+    int64_t q = a;
+    for (; q + U <= b; q += U) {
+      float xv[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) xv[u] = __ldg(x + (int64_t)nodes[q + u].x * d + k);
+#pragma unroll
+      for (int u = 0; u < U; ++u) acc = fadd(acc, fmul(v, xv[u]));
+    }
+    for (; q < b; ++q) acc = fadd(acc, fmul(v, __ldg(x + (int64_t)nodes[q].x * d + k)));
     out[P * d + k] = acc;
   }
 }
@@ -310,13 +321,35 @@ __global__ void k_expand_rows(const int64_t* __restrict__ eptr, const uint2* __r
 
 // Runs keyed by row i carry (Q, e) in vals; the row index of run e is keys[e].
 // Column centring (serial column sums over all rows), then scaling.
-__global__ void k_col_mean(const float* __restrict__ res, int64_t n, int32_t dim, float inv_n,
-                           float* __restrict__ mean) {
+// One block: the rows stream through shared memory in chunks (double
+// buffered, all threads loading) while thread j < dim adds column j's
+// values serially in row order.
+constexpr int COLMEAN_THREADS = 1024;
+constexpr int COLMEAN_ROWS = 256;  // rows per chunk (x dim <= 16 floats)
+__global__ void __launch_bounds__(COLMEAN_THREADS) k_col_mean(const float* __restrict__ res,
+                                                             int64_t n, int32_t dim, float inv_n,
+                                                             float* __restrict__ mean) {
+  __shared__ float buf[2][COLMEAN_ROWS * 16];
   const int j = threadIdx.x;
-  if (j >= dim) return;
+  const int64_t nch = (n + COLMEAN_ROWS - 1) / COLMEAN_ROWS;
+  auto load = [&](int64_t c, int b) {
+    const int64_t r0 = c * COLMEAN_ROWS;
+    const int64_t cnt = min((int64_t)COLMEAN_ROWS, n - r0) * dim;
+    for (int64_t q = j; q < cnt; q += COLMEAN_THREADS) buf[b][q] = __ldg(res + r0 * dim + q);
+  };
   float s = 0.0f;
-  for (int64_t i = 0; i < n; ++i) s = fadd(s, res[i * dim + j]);
-  mean[j] = fmul(s, inv_n);
+  if (nch > 0) load(0, 0);
+  __syncthreads();
+  for (int64_t c = 0; c < nch; ++c) {
+    const int b = (int)(c & 1);
+    if (c + 1 < nch) load(c + 1, b ^ 1);  // the next chunk loads during this one's adds
+    if (j < dim) {
+      const int rows = (int)min((int64_t)COLMEAN_ROWS, n - c * COLMEAN_ROWS);
+      for (int r = 0; r < rows; ++r) s = fadd(s, buf[b][r * dim + j]);
+    }
+    __syncthreads();
+  }
+  if (j < dim) mean[j] = fmul(s, inv_n);
 }
 
 __global__ void k_center_scale(float* __restrict__ res, int64_t n, int32_t dim,
@@ -477,9 +510,16 @@ void lp_init_inner(evoc_ctx* ctx, const evoc_graph* g, int32_t dim, const float*
     }
     return;
   }
+  // stage trace (EVOC_TRACE=1): one block per level, innermost level first
+  StageTrace tr(s);
+  const std::string lvl = "lp n=" + std::to_string(n) + ": ";
+  auto mark = [&](const char* what) {
+    if (tr.on) tr.mark((lvl + what).c_str());
+  };
   // 1. partition (label_prop.rs:448)
   DevBuf<uint32_t> part(n, s);
   const int64_t np = label_prop_partition(ctx, g, approx_parts, lp.n_lp_iter, seed, part.get());
+  mark("partition");
   if (np <= 0) throw Error(EVOC_ERR_INTERNAL, "label propagation produced no parts");
   // 2. per-part constants and node lists
   DevBuf<int32_t> cnt(np, s);
@@ -557,6 +597,7 @@ void lp_init_inner(evoc_ctx* ctx, const evoc_graph* g, int32_t dim, const float*
       coarse.nnz = 0;
     }
   }
+  mark("coarse graph");
   // 4. coarse data: per part, its nodes in order (stable sort of node ids by part)
   DevBuf<float> cdata;
   if (d_data) {
@@ -574,11 +615,13 @@ void lp_init_inner(evoc_ctx* ctx, const evoc_graph* g, int32_t dim, const float*
                                                cdata.get());
     EVOC_CHECK_LAUNCH();
   }
+  mark("coarse data");
   // 5. recursion
   const int32_t e = std::min(n_emb_epochs, 255);
   DevBuf<float> cinit(np * dim, s), layout(np * dim, s);
   lp_init_inner(ctx, &coarse, dim, d_data ? cdata.get() : nullptr, d, e, approx_parts / 4,
                 seed + 3000, lp, cinit.get());
+  mark("coarser levels");
   // 6. short embedding of the coarse graph (label_prop.rs:486-498)
   {
     evoc_embed_params_t ep;
@@ -596,6 +639,7 @@ void lp_init_inner(evoc_ctx* ctx, const evoc_graph* g, int32_t dim, const float*
     EVOC_CUDA(cudaStreamSynchronize(s));
     plan_free(pl);
   }
+  mark("coarse embedding");
   // 7. expansion (label_prop.rs:500-534)
   {
     // the transpose of g (rows of G^T, entries in row order)
@@ -662,13 +706,14 @@ void lp_init_inner(evoc_ctx* ctx, const evoc_graph* g, int32_t dim, const float*
     EVOC_CHECK_LAUNCH();
     DevBuf<float> mean(dim, s);
     const float inv_n = (float)(1.0 / (double)n);
-    k_col_mean<<<1, 32, 0, s>>>(d_out, n, dim, inv_n, mean.get());
+    k_col_mean<<<1, COLMEAN_THREADS, 0, s>>>(d_out, n, dim, inv_n, mean.get());
     EVOC_CHECK_LAUNCH();
     k_center_scale<<<grid_of(n * dim), 256, 0, s>>>(d_out, n, dim, mean.get(),
                                                     (float)lp.scaling);
     EVOC_CHECK_LAUNCH();
     EVOC_CUDA(cudaStreamSynchronize(s));
   }
+  mark("expansion");
 }
 
 }  // namespace
