@@ -213,28 +213,41 @@ __global__ void k_runs_to_csr(const uint2* __restrict__ vals, int64_t m, float l
 // ---------------------------------------------------------------------------
 // Data reduction: block per part, thread per feature column.
 // ---------------------------------------------------------------------------
-// The sum over the part's nodes stays serial in node order; the loads of the
-// next eight nodes are issued before their adds, so they overlap.
-__global__ void k_reduce_data(const float* __restrict__ x, int64_t d,
-                              const int64_t* __restrict__ poff, const uint2* __restrict__ nodes,
-                              const float* __restrict__ rv, float* __restrict__ out) {
-  constexpr int U = 8;
+// Block (part, 128 feature columns); thread per column. The sum over the
+// part's nodes stays serial in node order. Node ids come through shared
+// memory 128 at a time, and each thread issues the loads of the next 16
+// nodes before their adds, so a large part is not one long chain of
+// dependent loads.
+constexpr int RD_THREADS = 128;
+__global__ void __launch_bounds__(RD_THREADS) k_reduce_data(
+    const float* __restrict__ x, int64_t d, const int64_t* __restrict__ poff,
+    const uint2* __restrict__ nodes, const float* __restrict__ rv, float* __restrict__ out) {
+  constexpr int U = 16;
+  __shared__ uint32_t ids[RD_THREADS];
   const int64_t P = blockIdx.x;
+  const int64_t k = (int64_t)blockIdx.y * RD_THREADS + threadIdx.x;
+  const bool on = k < d;
   const float v = rv[P];
   const int64_t a = poff[P], b = poff[P + 1];
-  for (int64_t k = threadIdx.x; k < d; k += blockDim.x) {
-    float acc = 0.0f;
-    int64_t q = a;
-    for (; q + U <= b; q += U) {
-      float xv[U];
+  float acc = 0.0f;
+  for (int64_t c = a; c < b; c += RD_THREADS) {
+    const int cnt = (int)min((int64_t)RD_THREADS, b - c);
+    __syncthreads();  // the previous chunk's ids are read
+    if ((int)threadIdx.x < cnt) ids[threadIdx.x] = nodes[c + threadIdx.x].x;
+    __syncthreads();
+    if (on) {
+      int q = 0;
+      for (; q + U <= cnt; q += U) {
+        float xv[U];
 #pragma unroll
-      for (int u = 0; u < U; ++u) xv[u] = __ldg(x + (int64_t)nodes[q + u].x * d + k);
+        for (int u = 0; u < U; ++u) xv[u] = __ldg(x + (int64_t)ids[q + u] * d + k);
 #pragma unroll
-      for (int u = 0; u < U; ++u) acc = fadd(acc, fmul(v, xv[u]));
+        for (int u = 0; u < U; ++u) acc = fadd(acc, fmul(v, xv[u]));
+      }
+      for (; q < cnt; ++q) acc = fadd(acc, fmul(v, __ldg(x + (int64_t)ids[q] * d + k)));
     }
-    for (; q < b; ++q) acc = fadd(acc, fmul(v, __ldg(x + (int64_t)nodes[q].x * d + k)));
-    out[P * d + k] = acc;
   }
+  if (on) out[P * d + k] = acc;
 }
 
 // ---------------------------------------------------------------------------
@@ -343,9 +356,17 @@ __global__ void __launch_bounds__(COLMEAN_THREADS) k_col_mean(const float* __res
   for (int64_t c = 0; c < nch; ++c) {
     const int b = (int)(c & 1);
     if (c + 1 < nch) load(c + 1, b ^ 1);  // the next chunk loads during this one's adds
-    if (j < dim) {
+    if (j < dim) {  // eight values read ahead; the adds stay in row order
       const int rows = (int)min((int64_t)COLMEAN_ROWS, n - c * COLMEAN_ROWS);
-      for (int r = 0; r < rows; ++r) s = fadd(s, buf[b][r * dim + j]);
+      int r = 0;
+      for (; r + 8 <= rows; r += 8) {
+        float t[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) t[u] = buf[b][(r + u) * dim + j];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s = fadd(s, t[u]);
+      }
+      for (; r < rows; ++r) s = fadd(s, buf[b][r * dim + j]);
     }
     __syncthreads();
   }
@@ -611,8 +632,9 @@ void lp_init_inner(evoc_ctx* ctx, const evoc_graph* g, int32_t dim, const float*
     DevBuf<int64_t> poff(np + 1, s);
     exclusive_scan_i32_to_i64(cnt.get(), poff.get(), np, s);
     cdata.alloc(np * d, s);
-    k_reduce_data<<<(unsigned)np, 256, 0, s>>>(d_data, d, poff.get(), nodes.get(), rv.get(),
-                                               cdata.get());
+    k_reduce_data<<<dim3((unsigned)np, (unsigned)((d + RD_THREADS - 1) / RD_THREADS)),
+                    RD_THREADS, 0, s>>>(d_data, d, poff.get(), nodes.get(), rv.get(),
+                                        cdata.get());
     EVOC_CHECK_LAUNCH();
   }
   mark("coarse data");
@@ -671,6 +693,7 @@ void lp_init_inner(evoc_ctx* ctx, const evoc_graph* g, int32_t dim, const float*
       bi = tidx.get();
       bw = tw.get();
     }
+    mark("expansion: transpose");
     DevBuf<int32_t> sc(n, s);
     DevBuf<int64_t> soff(n + 1, s);
     k_sym_count<<<grid_of(n), 256, 0, s>>>(g->indptr.get(), g->indices.get(), bp, bi, n,
@@ -692,8 +715,10 @@ void lp_init_inner(evoc_ctx* ctx, const evoc_graph* g, int32_t dim, const float*
       // keys Q, vals (i, prod): order (i, Q, j) -> runs (i, (Q, e))
       k_swap_keys<<<grid_of(ms), 256, 0, s>>>(keys.get(), vals.get(), ms);  // keys i, vals (Q, .)
       EVOC_CHECK_LAUNCH();
+      mark("expansion: symmetric products");
       runs = sort_and_sum(keys.get(), vals.get(), ms, nbits, pbits, s);
     }
+    mark("expansion: sort and sum");
     DevBuf<int32_t> rc(n, s);
     EVOC_CUDA(cudaMemsetAsync(rc.get(), 0, n * sizeof(int32_t), s));
     if (runs > 0) {
@@ -704,6 +729,7 @@ void lp_init_inner(evoc_ctx* ctx, const evoc_graph* g, int32_t dim, const float*
     k_expand_rows<<<grid_of(n, 128), 128, 0, s>>>(eptr.get(), vals.get(), n, dim, layout.get(),
                                                   part.get(), u.get(), d_out);
     EVOC_CHECK_LAUNCH();
+    mark("expansion: rows");
     DevBuf<float> mean(dim, s);
     const float inv_n = (float)(1.0 / (double)n);
     k_col_mean<<<1, COLMEAN_THREADS, 0, s>>>(d_out, n, dim, inv_n, mean.get());
@@ -713,7 +739,7 @@ void lp_init_inner(evoc_ctx* ctx, const evoc_graph* g, int32_t dim, const float*
     EVOC_CHECK_LAUNCH();
     EVOC_CUDA(cudaStreamSynchronize(s));
   }
-  mark("expansion");
+  mark("expansion: centring");
 }
 
 }  // namespace
