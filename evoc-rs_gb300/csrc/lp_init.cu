@@ -334,20 +334,22 @@ __global__ void k_expand_rows(const int64_t* __restrict__ eptr, const uint2* __r
 
 // Runs keyed by row i carry (Q, e) in vals; the row index of run e is keys[e].
 // Column centring (serial column sums over all rows), then scaling.
-// One block: the rows stream through shared memory in chunks (double
-// buffered, all threads loading) while thread j < dim adds column j's
-// values serially in row order.
+// One block: the rows stream through shared memory in chunks of
+// COLMEAN_FLOATS values (double buffered, all threads loading) while thread
+// j < dim adds column j's values serially in row order, the next eight values
+// read while the current eight are added.
 constexpr int COLMEAN_THREADS = 1024;
-constexpr int COLMEAN_ROWS = 256;  // rows per chunk (x dim <= 16 floats)
+constexpr int COLMEAN_FLOATS = 5120;  // per chunk: 5120 / dim rows
 __global__ void __launch_bounds__(COLMEAN_THREADS) k_col_mean(const float* __restrict__ res,
                                                              int64_t n, int32_t dim, float inv_n,
                                                              float* __restrict__ mean) {
-  __shared__ float buf[2][COLMEAN_ROWS * 16];
+  __shared__ float buf[2][COLMEAN_FLOATS];
   const int j = threadIdx.x;
-  const int64_t nch = (n + COLMEAN_ROWS - 1) / COLMEAN_ROWS;
+  const int64_t rows_per = COLMEAN_FLOATS / dim;
+  const int64_t nch = (n + rows_per - 1) / rows_per;
   auto load = [&](int64_t c, int b) {
-    const int64_t r0 = c * COLMEAN_ROWS;
-    const int64_t cnt = min((int64_t)COLMEAN_ROWS, n - r0) * dim;
+    const int64_t r0 = c * rows_per;
+    const int64_t cnt = min(rows_per, n - r0) * dim;
     for (int64_t q = j; q < cnt; q += COLMEAN_THREADS) buf[b][q] = __ldg(res + r0 * dim + q);
   };
   float s = 0.0f;
@@ -356,17 +358,27 @@ __global__ void __launch_bounds__(COLMEAN_THREADS) k_col_mean(const float* __res
   for (int64_t c = 0; c < nch; ++c) {
     const int b = (int)(c & 1);
     if (c + 1 < nch) load(c + 1, b ^ 1);  // the next chunk loads during this one's adds
-    if (j < dim) {  // eight values read ahead; the adds stay in row order
-      const int rows = (int)min((int64_t)COLMEAN_ROWS, n - c * COLMEAN_ROWS);
+    if (j < dim) {
+      const float* col = buf[b] + j;
+      const int rows = (int)min(rows_per, n - c * rows_per);
       int r = 0;
-      for (; r + 8 <= rows; r += 8) {
+      if (rows >= 8) {
         float t[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) t[u] = buf[b][(r + u) * dim + j];
+        for (int u = 0; u < 8; ++u) t[u] = col[u * dim];
+        for (r = 8; r + 8 <= rows; r += 8) {
+          float nx[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) s = fadd(s, t[u]);
+          for (int u = 0; u < 8; ++u) nx[u] = col[(r + u) * dim];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) s = fadd(s, t[u]);
+#pragma unroll
+          for (int u = 0; u < 8; ++u) t[u] = nx[u];
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) s = fadd(s, t[u]);  // rows r - 8 .. r - 1
       }
-      for (; r < rows; ++r) s = fadd(s, buf[b][r * dim + j]);
+      for (; r < rows; ++r) s = fadd(s, col[r * dim]);
     }
     __syncthreads();
   }
