@@ -258,3 +258,78 @@ def test_adjusted_rand_index():
     assert O.adjusted_rand_index(a, c) == pytest.approx(_ari_pairs(a, c), abs=1e-12)
     skl = pytest.importorskip("sklearn.metrics")
     assert O.adjusted_rand_index(a, c) == pytest.approx(skl.adjusted_rand_score(a, c), abs=1e-12)
+
+
+# ---------------------------------------------------------------------------
+# The tie rules of the oracle's Boruvka MST, against an independent
+# restatement with brute-force queries: a query takes the smallest point
+# index among equal mutual-reachability values, a component's pick is its
+# (value, point index) minimum, and each round adds the picks in ascending
+# order of the component's smallest point index through a disjoint set.
+# ---------------------------------------------------------------------------
+def _sqd(a, b):
+    s = np.float32(0.0)
+    for t in (a - b).astype(np.float32):
+        s = np.float32(s + np.float32(t * t))
+    return s
+
+
+def _mst_by_rules(x, min_samples):
+    n = len(x)
+    D = np.array([[_sqd(x[i], x[j]) for j in range(n)] for i in range(n)], np.float32)
+    k = min(min_samples, n - 1)
+    core = np.zeros(n, np.float32)
+    if k > 0:
+        for i in range(n):
+            core[i] = np.sort(np.delete(D[i], i))[k - 1]
+    parent = list(range(n))
+
+    def find(a):
+        while parent[a] != a:
+            parent[a] = parent[parent[a]]
+            a = parent[a]
+        return a
+    out = []
+    while len(out) < n - 1:
+        comp = [min(j for j in range(n) if find(j) == find(i)) for i in range(n)]
+        picks = {}
+        for i in range(n):
+            best = None
+            for j in range(n):
+                if comp[j] == comp[i]:
+                    continue
+                mr = max(D[i, j], core[i], core[j])
+                if best is None or (mr, j) < best:
+                    best = (mr, j)
+            if best is not None and (comp[i] not in picks or (best[0], i) < picks[comp[i]][:2]):
+                picks[comp[i]] = (best[0], i, best[1])
+        if not picks:
+            break
+        merged = False
+        for c in sorted(picks):
+            w, i, j = picks[c]
+            ri, rj = find(i), find(j)
+            if ri != rj:
+                parent[ri] = rj
+                out.append((i, j, np.sqrt(np.float32(w))))
+                merged = True
+        if not merged:
+            break
+    return (np.array([e[0] for e in out], np.int64), np.array([e[1] for e in out], np.int64),
+            np.array([e[2] for e in out], np.float32))
+
+
+@pytest.mark.parametrize("min_samples", [0, 1, 3, 5])
+def test_mst_tie_rules_match_restatement(min_samples):
+    """Integer grid points with duplicates (many equal values) and a small
+    blob set: the oracle's edge list equals the rule-by-rule restatement."""
+    rng = np.random.default_rng(1)
+    g = np.stack(np.meshgrid(np.arange(8), np.arange(6)), -1).reshape(-1, 2)
+    grid = np.concatenate([g, g[::5]]).astype(np.float32)
+    grid = grid[rng.permutation(len(grid))]
+    blobs = (rng.normal(size=(60, 3)) + 3 * rng.integers(0, 3, (60, 1))).astype(np.float32)
+    for x in (grid, blobs, np.ones((12, 2), np.float32)):
+        u, v, w = O.build_mst(x, min_samples)
+        ru, rv, rw = _mst_by_rules(x, min_samples)
+        assert np.array_equal(u, ru) and np.array_equal(v, rv)
+        assert np.array_equal(w.view(np.uint32), rw.view(np.uint32))
