@@ -85,8 +85,9 @@ def test_null_context_arguments_rejected():
 
 
 def test_null_handles_rejected_by_the_newer_entry_points():
-    """The warm-start, kNN-handoff, partition and self-test entry points reject
-    NULL handles with EVOC_ERR_INVALID_ARGUMENT before any device work."""
+    """The warm-start, kNN-handoff, partition, self-test, autotuner,
+    initialisation and MST entry points reject NULL handles with
+    EVOC_ERR_INVALID_ARGUMENT before any device work."""
     ensure_library()
     import evoc_gb300 as E
     lib = E.load_library()
@@ -109,6 +110,16 @@ def test_null_handles_rejected_by_the_newer_entry_points():
     assert lib.evoc_label_prop_partition(None, None, 1, 1, 0, None, ctypes.byref(k)) == bad
     assert lib.evoc_selftest_wait_timeout(None, 10) == bad
     assert "NULL" in lib.evoc_last_error(None).decode() or lib.evoc_last_error(None)
+    # the autotuner, the bisection-work counter, the label-propagation
+    # initialisation and the minimum spanning tree
+    assert lib.evoc_plan_set_config(None, 0, 2, 0) == bad
+    assert lib.evoc_plan_autotune(None, None, None) == bad
+    assert lib.evoc_ctx_smooth_knn_steps(None, ctypes.byref(k)) == bad
+    assert lib.evoc_label_propagation_init(None, None, 8, None, 0, 0, None) == bad
+    assert lib.evoc_label_propagation_init_device(None, None, 8, None, 0, 0, None) == bad
+    assert lib.evoc_build_mst(None, None, 10, 4, 5, None, None, None, ctypes.byref(k)) == bad
+    assert lib.evoc_build_mst_device(None, None, 10, 4, 5, None, None, None,
+                                     ctypes.byref(k)) == bad
 
 
 def test_mlp_train_params_default():
